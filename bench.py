@@ -1,0 +1,362 @@
+"""Benchmark: options/sec of the Hull-White trinomial-tree batch pricer on one GB300
+(or N replicas under torchrun), with the FP64 oracle's CPU time beside it.
+
+Workload (default): the 30,000-option uneven batch (seed 1): option maturity
+U{1..10} y, bond maturity = option maturity + U{1..10} y, steps/year U{6..48},
+a U[0.02,0.20], sigma U[0.005,0.02], strike = forward bond price x U[0.9,1.1],
+11-node curve.  The headline is the batched mixed-precision tree (the fastest
+mode whose prices stay within 1e-4 absolute per 100 face of the FP64 oracle; the
+error is measured in this run and reported).  One step = one hwt_price call on
+the whole batch.
+
+  value  options/s with inputs resident in device memory (hwt_price_device),
+         device time from CUDA events on the pricer's stream, L2 flushed between
+         steps (256 MB memset)
+  e2e    options/s through hwt_price with pinned host inputs/outputs: host clock
+         around the call, which includes the H2D copy of the options, validation,
+         binning, pricing and the D2H copy of the prices
+
+`--impl reference` times the reference's CPU algorithm instead (the oracle: the
+C restatement of seq/, OpenMP over options, all host threads) on a bounded sample.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "options/sec at <=1e-4 abs err: FP64 tree vs mixed/batched tree vs surrogate"
+# FLOP per active node of the two sweeps (forward: Q*E*G 2 + 3-term gather 5 +
+# alpha accumulate 2; backward: gather 5 + discount 2), the fixed work unit.
+FLOP_PER_NODE = 16
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def init_dist(world: int, backend: str):
+    if world <= 1:
+        return None
+    import torch.distributed as dist
+    os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+    dist.init_process_group(backend=backend)
+    return dist
+
+
+def max_over_ranks(value: float, dist, device=None) -> float:
+    """Max of a float over ranks (barrier included)."""
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def shard_lpt(work: np.ndarray, world: int) -> list[np.ndarray]:
+    """Longest-processing-time partition of options by work (16 x active nodes):
+    how a batch splits across GPUs when it is sharded instead of replicated."""
+    order = np.argsort(-work, kind="stable")
+    loads = np.zeros(world)
+    parts = [[] for _ in range(world)]
+    for i in order:
+        r = int(np.argmin(loads))
+        parts[r].append(i)
+        loads[r] += work[i]
+    return [np.array(sorted(p), dtype=np.int64) for p in parts]
+
+
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi while running."""
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.QUERY,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = max(mx, float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def load_json(path):
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return None
+
+
+def cpu_reference(args, rank, world):
+    """--impl reference: the reference's CPU algorithm (oracle port) on the host."""
+    import __graft_entry__ as g
+    if rank != 0:
+        return 0
+    pkg, orc = g.package(), g.oracle()
+    orc.build()
+    wl = pkg.workloads
+    batch = wl.WORKLOADS[args.workload]()
+    rates, days = wl.yield_curve()
+    y = pkg.Yield(rates, days)
+    n_total = len(batch["strike"])
+    sample = min(n_total, args.ref_sample)
+    opts = pkg.Options.from_batch({k: v[:sample] for k, v in batch.items()})
+    threads = orc.max_threads()
+    for _ in range(args.warmup):
+        orc.price(opts, y, "f64")
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        orc.price(opts, y, "f64")
+        times.append(time.perf_counter() - t0)
+    per = sum(times) / len(times)
+    value = sample / per
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "options/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": per * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded numpy)",
+        "config": {"workload": args.workload, "options": n_total, "sample_options": sample,
+                   "implementation": "oracle/hwt_seq.c: C restatement of the reference seq/ pricer, OpenMP over options"},
+        "cpu_baseline": {"value": value, "unit": "options/s", "cores": threads, "kind": "port",
+                         "sample": f"first {sample} options of {args.workload}, {args.steps} timed passes"},
+        "e2e": {"value": value, "unit": "options/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_ours(args, rank, world, local):
+    import torch
+    import __graft_entry__ as g
+
+    pkg = g.package()
+    wl = pkg.workloads
+    dist = init_dist(world, "nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    batch = wl.WORKLOADS[args.workload]()
+    opts = pkg.Options.from_batch(batch)
+    rates, days = wl.yield_curve()
+    y = pkg.Yield(rates, days)
+    n = opts.N
+    shp = pkg.shape(opts)
+    nodes = int(np.sum(pkg.active_nodes(shp["height"], shp["jmax"])))
+    flop_per_batch = FLOP_PER_NODE * nodes
+
+    pricer = pkg.Pricer(local, os.path.join(ROOT, "profiles", "tune_cache.txt") if args.tune else None)
+    mode = {"mixed": pkg.BATCHED_MIXED, "fp64": pkg.BATCHED_FP64, "fp32": pkg.BATCHED_FP32,
+            "plain": pkg.PLAIN_FP64}[args.mode]
+    if args.tune:
+        pricer.autotune(opts, y, mode)
+
+    # device-resident inputs
+    fields = {"strike": opts.StrikePrices, "bond_maturity": opts.Maturities, "option_maturity": opts.Lengths,
+              "term_unit": opts.TermUnits.view(np.int16), "term_steps": opts.TermStepCounts.view(np.int16),
+              "a": opts.ReversionRates, "sigma": opts.Volatilities, "type": opts.Types}
+    dev_t = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for k, v in fields.items()}
+    dev_ptr = {k: t.data_ptr() for k, t in dev_t.items()}
+    dev_out = torch.empty(n, dtype=torch.float64, device=dev)
+    # pinned host inputs / outputs for the end-to-end path
+    host_t = {k: torch.from_numpy(np.ascontiguousarray(v)).pin_memory() for k, v in fields.items()}
+    host_ptr = {k: t.data_ptr() for k, t in host_t.items()}
+    host_out = torch.empty(n, dtype=torch.float64).pin_memory()
+    h2d_bytes = int(sum(t.numel() * t.element_size() for t in host_t.values()))
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def flush_l2():
+        flush.zero_()
+        torch.cuda.synchronize(dev)
+
+    def device_steps(m, steps, warm):
+        for _ in range(warm):
+            pricer.price_device(dev_ptr, n, y, dev_out.data_ptr(), m)
+        times, launches, stats = [], 0, None
+        for _ in range(steps):
+            flush_l2()
+            st = pricer.price_device(dev_ptr, n, y, dev_out.data_ptr(), m)
+            times.append(st.total_ms)
+            launches += st.kernel_launches
+            stats = pkg.Stats.from_buffer_copy(st)
+        return times, launches, stats
+
+    # CPU baseline first (rank 0, N=1): also gives the FP64 reference prices
+    cpu = None
+    ref_prices = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        orc = g.oracle()
+        orc.build()
+        t0 = time.perf_counter()
+        ref_prices = orc.price(opts, y, "f64")
+        dt = time.perf_counter() - t0
+        cpu = {"value": n / dt, "unit": "options/s", "cores": orc.max_threads(), "kind": "port",
+               "sample": f"all {n} options of {args.workload}, one pass, OpenMP over options"}
+
+    # per-mode survey (prices + errors + device time), untimed by the contract
+    modes = {}
+    for m in (pkg.BATCHED_MIXED, pkg.BATCHED_FP32, pkg.BATCHED_FP64, pkg.PLAIN_FP64):
+        name = pkg.MODE_NAMES[m]
+        k = args.steps if m != pkg.PLAIN_FP64 else max(1, min(args.steps, 3))
+        t, _, st = device_steps(m, k, 1)
+        entry = {"options_per_s": n / (sum(t) / len(t) / 1e3), "ms_per_step": sum(t) / len(t),
+                 "pricing_ms": st.pricing_ms}
+        if ref_prices is not None:
+            got = dev_out.cpu().numpy()
+            err = np.abs(got - ref_prices)
+            entry.update({"max_abs_err": float(np.max(err)), "p99_abs_err": float(np.percentile(err, 99)),
+                          "max_rel_err": float(np.max(err / np.maximum(np.abs(ref_prices), 1e-300)))})
+        modes[name] = entry
+    fp64_rate = modes["batched_fp64"]["options_per_s"]
+    plain_rate = modes["plain_fp64"]["options_per_s"]
+    for e in modes.values():
+        e["x_batched_fp64"] = e["options_per_s"] / fp64_rate
+        e["x_plain_fp64"] = e["options_per_s"] / plain_rate
+
+    # ---- timed region: K device-resident steps of the headline mode
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize(dev)
+    with ClockSampler(local) as clk:
+        times, launches, st = device_steps(mode, args.steps, args.warmup)
+        torch.cuda.synchronize(dev)
+        if dist is not None:
+            dist.barrier()
+        # e2e through the public host-memory API (pinned buffers), host clock
+        for _ in range(args.warmup):
+            pricer.price_host_ptrs(host_ptr, n, y, host_out.data_ptr(), mode)
+        e2e_t = []
+        for _ in range(args.steps):
+            flush_l2()
+            t0 = time.perf_counter()
+            pricer.price_host_ptrs(host_ptr, n, y, host_out.data_ptr(), mode)
+            e2e_t.append(time.perf_counter() - t0)
+    ms = sum(times) / len(times)
+    ms = max_over_ranks(ms, dist, dev)
+    e2e_ms = max_over_ranks(1e3 * sum(e2e_t) / len(e2e_t), dist, dev)
+    pricing_ms = st.pricing_ms
+
+    peaks = pricer.measure_peaks()
+    measured = load_json(os.path.join(ROOT, "MEASURED_PEAKS.json")) or {}
+    fp32_peak = peaks[1]
+    achieved = flop_per_batch / (pricing_ms * 1e-3) / 1e12
+    prof = load_json(os.path.join(ROOT, "profiles", f"pricing_{args.workload}_{args.mode}.json")) or {}
+    traffic = prof.get("dram_bytes_per_launch")
+    bound = {"mixed": "fp32", "fp32": "fp32", "fp64": "fp64", "plain": "fp64"}[args.mode]
+    peak = fp32_peak if bound == "fp32" else peaks[0]
+
+    if rank == 0:
+        line = {
+            "metric": METRIC,
+            "value": world * n / (ms * 1e-3),
+            "unit": "options/s",
+            "n_gpus": world,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": ms,
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": {"mixed": "f32+f64", "fp32": "f32", "fp64": "f64", "plain": "f64"}[args.mode],
+            "data": "synthetic (seeded numpy; no public data set exists for this workload)",
+            "config": {"workload": args.workload, "options": n, "mode": pkg.MODE_NAMES[mode],
+                       "active_nodes_per_pass": nodes, "parallelism": "replicas" if world > 1 else "single",
+                       "l2": "flushed between steps (256 MB memset), inputs 1.35 MB",
+                       "block_size": st.block_size, "grid": st.grid},
+            "clocks": clk.summary(),
+            "gpu_launches": launches,
+            "e2e": {"value": world * n / (e2e_ms * 1e-3), "unit": "options/s", "h2d_bytes_per_step": h2d_bytes,
+                    "d2h_bytes_per_step": 8 * n},
+            "roofline": {"bound": bound, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "work": f"{FLOP_PER_NODE} FLOP x {nodes} active nodes per launch; peak = FMA microbenchmark "
+                                 f"on this GPU (MEASURED_PEAKS.json has no FP32/FP64 entries; its HBM figure is "
+                                 f"{measured.get('hbm_gbs')} GB/s)",
+                         "kernel_ms": pricing_ms},
+            "peaks_measured": {"fp64_tflops": peaks[0], "fp32_tflops": peaks[1]},
+            "modes": modes,
+        }
+        if cpu is not None:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line))
+    pricer.close()
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="uneven_30k", choices=["uniform_1k", "uneven_30k", "skewed_100k"])
+    ap.add_argument("--mode", default="mixed", choices=["mixed", "fp64", "fp32", "plain"])
+    ap.add_argument("--ref-sample", type=int, default=6000)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--tune", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        return cpu_reference(args, rank, world)
+    return run_ours(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

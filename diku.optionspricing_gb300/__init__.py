@@ -1,0 +1,455 @@
+"""GB300 Hull-White trinomial-tree batch pricer - Python side of the C ABI.
+
+Mirrors the reference project's batch pricing interface (MartinMetaksov/
+diku.OptionsPricing) for Python callers and tests:
+
+  Options / Yield        common/Options.hpp:48-125, common/Yield.hpp:14-40 (SoA records,
+                         same .in text files)
+  read_array/write_array common/Arrays.hpp:15-46 ("[a, b, c]", std::fixed, max_digits10)
+  compute_options        seq::computeOptions (seq/Seq.hpp:181-190)
+  KernelRun.run          KernelRunBase::run (cuda-option/Kernel.cuh:303-314)
+
+Every pricing call goes through libhwtree.so (include/hwtree.h) to the sm_103a
+kernels; there is no CPU pricing path in this package.  Loading fails loudly when
+the library has not been built (``python diku.optionspricing_gb300/build.py`` or
+``__graft_entry__.build()``).
+"""
+from __future__ import annotations
+
+import ctypes
+import enum
+import io
+import os
+import re
+from dataclasses import dataclass, field
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libhwtree.so")
+
+# Status codes (hwtree.h)
+HWT_OK, HWT_EINVAL, HWT_ECUDA, HWT_ENOMEM, HWT_EUNSUPPORTED, HWT_ENODEV = 0, -1, -2, -3, -4, -5
+
+# Pricing modes (hwtree.h)
+PLAIN_FP64, BATCHED_FP64, BATCHED_FP32, BATCHED_MIXED = 0, 1, 2, 3
+MODE_NAMES = {PLAIN_FP64: "plain_fp64", BATCHED_FP64: "batched_fp64", BATCHED_FP32: "batched_fp32",
+              BATCHED_MIXED: "batched_mixed"}
+
+
+class OptionType(enum.IntEnum):
+    """common/Options.hpp:24-28"""
+    CALL = 0
+    PUT = 1
+
+
+class SortType(str, enum.Enum):
+    """common/Options.hpp:15-22 (accepted; results never depend on it)."""
+    WIDTH_DESC = "W"
+    WIDTH_ASC = "w"
+    HEIGHT_DESC = "H"
+    HEIGHT_ASC = "h"
+    NONE = "-"
+
+
+class HwtError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(f"[{code}] {message}")
+        self.code = code
+
+
+class InvalidInput(HwtError, ValueError):
+    pass
+
+
+# ---------------------------------------------------------------------------
+# C ABI
+# ---------------------------------------------------------------------------
+class _Options(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int32), ("strike", ctypes.c_void_p), ("bond_maturity", ctypes.c_void_p),
+                ("option_maturity", ctypes.c_void_p), ("term_unit", ctypes.c_void_p),
+                ("term_steps", ctypes.c_void_p), ("a", ctypes.c_void_p), ("sigma", ctypes.c_void_p),
+                ("type", ctypes.c_void_p)]
+
+
+class _Yield(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int32), ("rate", ctypes.c_void_p), ("day", ctypes.c_void_p)]
+
+
+class Config(ctypes.Structure):
+    """hwt_config: mode, block_size, sort, big_threshold, use_graph, record_busy."""
+    _fields_ = [("mode", ctypes.c_int32), ("block_size", ctypes.c_int32), ("sort", ctypes.c_int32),
+                ("big_threshold", ctypes.c_int32), ("use_graph", ctypes.c_int32), ("record_busy", ctypes.c_int32)]
+
+
+class Stats(ctypes.Structure):
+    """hwt_stats (see include/hwtree.h for field meanings)."""
+    _fields_ = [("total_ms", ctypes.c_double), ("pricing_ms", ctypes.c_double), ("sizing_ms", ctypes.c_double),
+                ("nodes", ctypes.c_int64), ("h2d_bytes", ctypes.c_int64), ("d2h_bytes", ctypes.c_int64),
+                ("device_bytes", ctypes.c_int64), ("kernel_launches", ctypes.c_int32),
+                ("n_block_trees", ctypes.c_int32), ("n_warp_tasks", ctypes.c_int32), ("grid", ctypes.c_int32),
+                ("block_size", ctypes.c_int32), ("max_width", ctypes.c_int32), ("max_height", ctypes.c_int32),
+                ("graph_replayed", ctypes.c_int32), ("busy_max_ms", ctypes.c_double),
+                ("busy_mean_ms", ctypes.c_double)]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+_lib = None
+
+# Every function the header declares, with its ctypes signature.
+_SIGNATURES = {
+    "hwt_abi_version": (ctypes.c_int, []),
+    "hwt_create": (ctypes.c_void_p, [ctypes.c_int, ctypes.c_char_p]),
+    "hwt_create_status": (ctypes.c_int, []),
+    "hwt_destroy": (None, [ctypes.c_void_p]),
+    "hwt_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
+    "hwt_price": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(_Options), ctypes.POINTER(_Yield), ctypes.c_int,
+                                 ctypes.c_void_p, ctypes.POINTER(Stats)]),
+    "hwt_price_ex": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(_Options), ctypes.POINTER(_Yield),
+                                    ctypes.POINTER(Config), ctypes.c_void_p, ctypes.POINTER(Stats)]),
+    "hwt_price_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(_Options), ctypes.POINTER(_Yield),
+                                        ctypes.POINTER(Config), ctypes.c_void_p, ctypes.POINTER(Stats)]),
+    "hwt_shape": (ctypes.c_int, [ctypes.POINTER(_Options), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                 ctypes.c_void_p]),
+    "hwt_active_nodes": (ctypes.c_int64, [ctypes.c_int32, ctypes.c_int32]),
+    "hwt_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(_Options), ctypes.POINTER(_Yield), ctypes.c_int,
+                                    ctypes.c_int, ctypes.POINTER(Config)]),
+    "hwt_get_config": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(Config)]),
+    "hwt_measure_peaks": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double),
+                                         ctypes.POINTER(ctypes.c_double)]),
+}
+
+
+def lib() -> ctypes.CDLL:
+    """The loaded C-ABI library; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: build the native library first "
+                              "(python diku.optionspricing_gb300/build.py)")
+        handle = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGNATURES.items():
+            fn = getattr(handle, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = handle
+    return _lib
+
+
+# ---------------------------------------------------------------------------
+# Records and text format
+# ---------------------------------------------------------------------------
+_ARRAY_RE = re.compile(r"\[([^\]]*)\]")
+
+
+def read_arrays(text: str) -> list[list[str]]:
+    """All "[..]" arrays of a text, as token lists (common/Arrays.hpp:15-32)."""
+    out = []
+    for body in _ARRAY_RE.findall(text):
+        toks = [t.strip() for t in body.split(",")]
+        out.append([t for t in toks if t])
+    return out
+
+
+def read_array(stream) -> list[str]:
+    """Reads the next "[..]" array from a text stream."""
+    buf = []
+    started = False
+    while True:
+        ch = stream.read(1)
+        if not ch:
+            break
+        if ch == "[":
+            started = True
+            continue
+        if started:
+            if ch == "]":
+                break
+            buf.append(ch)
+    return [t.strip() for t in "".join(buf).split(",") if t.strip()]
+
+
+def format_array(values, digits: int = 17) -> str:
+    """common/Arrays.hpp:34-46: '[' std::fixed values at max_digits10 ']'.
+    digits=17 for double, 9 for float, 0 for integer arrays."""
+    arr = np.asarray(values)
+    if arr.dtype.kind in "iub" or digits == 0:
+        body = ", ".join(str(int(v)) for v in arr)
+    else:
+        body = ", ".join("%.*f" % (digits, float(v)) for v in arr)
+    return "[" + body + "]\n"
+
+
+def write_array(stream, values, digits: int = 17) -> None:
+    stream.write(format_array(values, digits))
+
+
+@dataclass
+class Options:
+    """SoA option records (common/Options.hpp:48-58) with real = double."""
+    StrikePrices: np.ndarray
+    Maturities: np.ndarray
+    Lengths: np.ndarray
+    TermUnits: np.ndarray
+    TermStepCounts: np.ndarray
+    ReversionRates: np.ndarray
+    Volatilities: np.ndarray
+    Types: np.ndarray
+
+    def __post_init__(self):
+        self.StrikePrices = np.ascontiguousarray(self.StrikePrices, dtype=np.float64)
+        self.Maturities = np.ascontiguousarray(self.Maturities, dtype=np.float64)
+        self.Lengths = np.ascontiguousarray(self.Lengths, dtype=np.float64)
+        self.TermUnits = np.ascontiguousarray(self.TermUnits, dtype=np.uint16)
+        self.TermStepCounts = np.ascontiguousarray(self.TermStepCounts, dtype=np.uint16)
+        self.ReversionRates = np.ascontiguousarray(self.ReversionRates, dtype=np.float64)
+        self.Volatilities = np.ascontiguousarray(self.Volatilities, dtype=np.float64)
+        self.Types = np.ascontiguousarray(self.Types, dtype=np.int8)
+        n = len(self.StrikePrices)
+        for name in ("Maturities", "Lengths", "TermUnits", "TermStepCounts", "ReversionRates", "Volatilities",
+                     "Types"):
+            if len(getattr(self, name)) != n:
+                raise ValueError(f"option array {name} has {len(getattr(self, name))} entries, expected {n}")
+
+    @property
+    def N(self) -> int:
+        return len(self.StrikePrices)
+
+    @classmethod
+    def from_file(cls, filename: str) -> "Options":
+        """Options(const std::string&) (common/Options.hpp:73-98): eight arrays in
+        field order; a type other than 0/1 is out_of_range."""
+        if not filename:
+            raise ValueError("File not specified.")
+        if not os.path.exists(filename):
+            raise ValueError(f"File '{filename}' does not exist.")
+        with open(filename) as f:
+            arrs = read_arrays(f.read())
+        if len(arrs) < 8:
+            raise ValueError(f"File '{filename}' holds {len(arrs)} arrays, expected 8.")
+        types = np.array([int(float(t)) for t in arrs[7]], dtype=np.int64)
+        if np.any((types != 0) & (types != 1)):
+            raise IndexError("Invalid OptionType read from stream.")
+        return cls(np.array(arrs[0], dtype=np.float64), np.array(arrs[1], dtype=np.float64),
+                   np.array(arrs[2], dtype=np.float64), np.array([int(float(t)) for t in arrs[3]]),
+                   np.array([int(float(t)) for t in arrs[4]]), np.array(arrs[5], dtype=np.float64),
+                   np.array(arrs[6], dtype=np.float64), types)
+
+    @classmethod
+    def from_batch(cls, b: dict) -> "Options":
+        """From a workloads.py batch dict."""
+        return cls(b["strike"], b["bond_maturity"], b["option_maturity"], b["term_unit"], b["term_steps"], b["a"],
+                   b["sigma"], b["type"])
+
+    def to_text(self) -> str:
+        buf = io.StringIO()
+        for arr, digits in ((self.StrikePrices, 17), (self.Maturities, 17), (self.Lengths, 17),
+                            (self.TermUnits, 0), (self.TermStepCounts, 0), (self.ReversionRates, 17),
+                            (self.Volatilities, 17), (self.Types, 0)):
+            write_array(buf, arr, digits)
+        return buf.getvalue()
+
+    def write_to_file(self, filename: str) -> None:
+        """Options::writeToFile (common/Options.hpp:100-124)."""
+        with open(filename, "w") as f:
+            f.write(self.to_text())
+
+    def subset(self, idx) -> "Options":
+        return Options(*(getattr(self, f)[idx] for f in _OPTION_FIELDS))
+
+    def _c(self) -> _Options:
+        return _Options(self.N, self.StrikePrices.ctypes.data, self.Maturities.ctypes.data, self.Lengths.ctypes.data,
+                        self.TermUnits.ctypes.data, self.TermStepCounts.ctypes.data,
+                        self.ReversionRates.ctypes.data, self.Volatilities.ctypes.data, self.Types.ctypes.data)
+
+
+_OPTION_FIELDS = ("StrikePrices", "Maturities", "Lengths", "TermUnits", "TermStepCounts", "ReversionRates",
+                  "Volatilities", "Types")
+
+
+@dataclass
+class Yield:
+    """Yield curve (common/Yield.hpp:14-40): zero rates at whole-day maturities."""
+    Prices: np.ndarray
+    TimeSteps: np.ndarray
+
+    def __post_init__(self):
+        self.Prices = np.ascontiguousarray(self.Prices, dtype=np.float64)
+        self.TimeSteps = np.ascontiguousarray(self.TimeSteps, dtype=np.int32)
+        if len(self.Prices) != len(self.TimeSteps):
+            raise ValueError("yield arrays differ in length")
+
+    @property
+    def N(self) -> int:
+        return len(self.Prices)
+
+    @classmethod
+    def from_file(cls, filename: str) -> "Yield":
+        if not filename:
+            raise ValueError("File not specified.")
+        if not os.path.exists(filename):
+            raise ValueError("File does not exist.")
+        with open(filename) as f:
+            arrs = read_arrays(f.read())
+        return cls(np.array(arrs[0], dtype=np.float64), np.array([int(float(t)) for t in arrs[1]]))
+
+    def _c(self) -> _Yield:
+        return _Yield(self.N, self.Prices.ctypes.data, self.TimeSteps.ctypes.data)
+
+
+def shape(options: Options) -> dict:
+    """Tree shape per option as the reference computes it, on the host (no GPU):
+    jmax, height n, width 2*jmax+1, maturity step (common/OptionConstants.hpp:29-53)."""
+    n = options.N
+    out = {k: np.empty(n, dtype=np.int32) for k in ("jmax", "height", "width", "maturity_step")}
+    o = options._c()
+    rc = lib().hwt_shape(ctypes.byref(o), out["jmax"].ctypes.data, out["height"].ctypes.data,
+                         out["width"].ctypes.data, out["maturity_step"].ctypes.data)
+    out["status"] = rc
+    return out
+
+
+def active_nodes(height, jmax) -> np.ndarray:
+    """Active nodes of one pass: sum_{i<n} (2 min(i, jmax) + 1), the work unit."""
+    h = np.asarray(height, dtype=np.int64)
+    j = np.asarray(jmax, dtype=np.int64)
+    h = np.maximum(h, 0)
+    full = (j + 1) ** 2 + (h - j - 1) * (2 * j + 1)
+    return np.where(h <= j + 1, h * h, full)
+
+
+# ---------------------------------------------------------------------------
+# Pricer
+# ---------------------------------------------------------------------------
+class Pricer:
+    """One pricing context on one GPU (hwt_create / hwt_destroy)."""
+
+    def __init__(self, device: int = 0, tune_cache: str | None = None):
+        L = lib()
+        self._ctx = L.hwt_create(device, tune_cache.encode() if tune_cache else None)
+        if not self._ctx:
+            code = L.hwt_create_status()
+            raise HwtError(code, "no CUDA device" if code == HWT_ENODEV else "hwt_create failed")
+        self.last_stats = Stats()
+
+    def close(self):
+        if getattr(self, "_ctx", None):
+            lib().hwt_destroy(self._ctx)
+            self._ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _check(self, rc: int):
+        if rc != HWT_OK:
+            msg = lib().hwt_last_error(self._ctx)
+            msg = msg.decode() if msg else ""
+            if rc == HWT_EINVAL:
+                raise InvalidInput(rc, msg)
+            raise HwtError(rc, msg)
+
+    def config(self, mode: int, block_size: int = 0, big_threshold: int = 0, use_graph: bool = True,
+               record_busy: bool = False, sort: str = "-") -> Config:
+        return Config(mode, block_size, ord(sort), big_threshold, 1 if use_graph else 0, 1 if record_busy else 0)
+
+    def price(self, options: Options, yield_: Yield, mode: int = BATCHED_FP64, out: np.ndarray | None = None,
+              **cfg) -> np.ndarray:
+        """Prices host-memory options; returns float64 prices in input order."""
+        if out is None:
+            out = np.empty(options.N, dtype=np.float64)
+        o, y, c = options._c(), yield_._c(), self.config(mode, **cfg)
+        rc = lib().hwt_price_ex(self._ctx, ctypes.byref(o), ctypes.byref(y), ctypes.byref(c), out.ctypes.data,
+                                ctypes.byref(self.last_stats))
+        self._check(rc)
+        return out
+
+    def price_host_ptrs(self, ptrs: dict, n: int, yield_: Yield, out_ptr: int, mode: int, **cfg) -> Stats:
+        """Prices options whose arrays are given as raw host pointers (e.g. pinned
+        torch tensors), writing prices to out_ptr."""
+        o = _Options(n, *(ptrs[k] for k in ("strike", "bond_maturity", "option_maturity", "term_unit", "term_steps",
+                                            "a", "sigma", "type")))
+        y, c = yield_._c(), self.config(mode, **cfg)
+        rc = lib().hwt_price_ex(self._ctx, ctypes.byref(o), ctypes.byref(y), ctypes.byref(c), out_ptr,
+                                ctypes.byref(self.last_stats))
+        self._check(rc)
+        return self.last_stats
+
+    def price_device(self, ptrs: dict, n: int, yield_: Yield, out_ptr: int, mode: int, **cfg) -> Stats:
+        """Prices options already in device memory (raw device pointers)."""
+        o = _Options(n, *(ptrs[k] for k in ("strike", "bond_maturity", "option_maturity", "term_unit", "term_steps",
+                                            "a", "sigma", "type")))
+        y, c = yield_._c(), self.config(mode, **cfg)
+        rc = lib().hwt_price_device(self._ctx, ctypes.byref(o), ctypes.byref(y), ctypes.byref(c), out_ptr,
+                                    ctypes.byref(self.last_stats))
+        self._check(rc)
+        return self.last_stats
+
+    def autotune(self, options: Options, yield_: Yield, mode: int, repeats: int = 3) -> Config:
+        best = Config()
+        o, y = options._c(), yield_._c()
+        self._check(lib().hwt_autotune(self._ctx, ctypes.byref(o), ctypes.byref(y), mode, repeats,
+                                       ctypes.byref(best)))
+        return best
+
+    def get_config(self, mode: int) -> Config:
+        c = Config()
+        self._check(lib().hwt_get_config(self._ctx, mode, ctypes.byref(c)))
+        return c
+
+    def measure_peaks(self) -> tuple[float, float]:
+        """(FP64, FP32) FMA peaks of this GPU in TFLOP/s."""
+        a, b = ctypes.c_double(), ctypes.c_double()
+        self._check(lib().hwt_measure_peaks(self._ctx, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+
+_default_pricer = None
+
+
+def default_pricer() -> Pricer:
+    global _default_pricer
+    if _default_pricer is None:
+        _default_pricer = Pricer(0)
+    return _default_pricer
+
+
+def compute_options(options: Options, yield_: Yield, results=None, mode: int = BATCHED_FP64) -> np.ndarray:
+    """seq::computeOptions(options, yield, results) (seq/Seq.hpp:181-190) on the GPU."""
+    out = default_pricer().price(options, yield_, mode)
+    if results is not None:
+        results[:] = out
+    return out
+
+
+class KernelRun:
+    """KernelRunBase (cuda-option/Kernel.cuh:218-327): run() prices, runtime keeps stats."""
+
+    def __init__(self, mode: int = BATCHED_FP64):
+        self.mode = mode
+        self.runtime: dict = {}
+
+    def run(self, options: Options, yield_: Yield, results=None, block_size: int = -1,
+            sort_type: SortType = SortType.NONE, is_test: bool = False) -> np.ndarray:
+        p = default_pricer()
+        out = p.price(options, yield_, self.mode, block_size=max(block_size, 0), sort=SortType(sort_type).value)
+        self.runtime = p.last_stats.as_dict()
+        if results is not None:
+            results[:] = out
+        if is_test:
+            print(f"Kernel executed in {self.runtime['pricing_ms'] * 1000:.0f} microsec")
+            print(f"Total execution time {self.runtime['total_ms'] * 1000:.0f} microsec")
+        return out
+
+
+from . import workloads  # noqa: E402  (seeded synthetic batches)

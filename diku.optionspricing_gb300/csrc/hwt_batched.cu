@@ -1,0 +1,853 @@
+// Batched Hull-White trinomial-tree pricer for sm_103a.
+//
+// What it computes is the reference's per-option pricer (seq/Seq.hpp:24-179):
+// forward induction of Arrow-Debreu prices Q with an alpha fitted to the yield
+// curve at every step, then backward induction of a 100-face bond with the
+// option payoff applied at the option's maturity step.  How it computes it is
+// different, and rests on one identity: alpha_i is the same for every node of a
+// time step, so it only rescales whole rows.  Write Q_i = s_i * Qt_i.  Then
+//   r_{i+1} = G o gather(r_i),   r_0 = e_center,    G_j = exp(-(j dr) dt)
+//   Sum_i   = sum_k r_i[k]       (the reference's alpha sum is s_i * Sum_i)
+//   s_k     = P_k / Sum_{k-1}    with P_k = exp(-R(k dt) k dt), Sum_0 = 1
+// and the backward rows of the bond are  c_i = (s_n / s_i) * ct_i  with
+//   ct_i = G o P ct_{i+1},  ct_n = 100.
+// At the maturity step m the payoff max(X - (s_n/s_m) ct_m, 0) (put) or
+// max((s_n/s_m) ct_m - X, 0) (call) starts a new row v, rolled back the same
+// way; the price is s_m * v_0[center] (or s_n * ct_0[center] when m >= n).
+// So each tree is two pure stencil sweeps with no per-step reduction, log or
+// exp; the alpha fit collapses to two sums (rows m-1 and n-1) per option.
+//
+// Work layout: trees are sized, validated and binned on the device.  Trees up to
+// 256 nodes wide run on a slice of a warp (L lanes x K nodes per lane, rows in
+// registers, neighbours by shuffle); wider trees get a whole block (K nodes per
+// thread, warp edges exchanged through shared memory, one barrier per step).
+// One persistent kernel drains the block-tree queue and then the warp-task
+// queue, both ordered by descending work.
+//
+// Precision modes: FP64 runs the stencils in the gather form with G folded into
+// the coefficients (3 FMAs per node and pass, 4 while the +-jmax edge jumps are
+// live).  FP32 and MIXED run them in float in a flux form that conserves
+// probability exactly (stay = 1 - up - down is never formed), with G written as
+// 1 + g, and the bond phase of the backward sweep carried as a deviation from
+// 100.  MIXED keeps the two alpha-fit sums, the scales, the payoff and the final
+// discount in double; FP32 does those in float too.
+#include <float.h>
+#include <stdio.h>
+
+#include "hwt_internal.h"
+#include "hwt_model.cuh"
+
+namespace hwt {
+namespace {
+
+constexpr unsigned FULL = 0xffffffffu;
+
+struct ModeF64 {
+    typedef double Row;
+    typedef double Scal;
+    static constexpr bool kFlux = false;
+};
+struct ModeF32 {
+    typedef float Row;
+    typedef float Scal;
+    static constexpr bool kFlux = true;
+};
+struct ModeMix {
+    typedef float Row;
+    typedef double Scal;
+    static constexpr bool kFlux = true;
+};
+
+__device__ __forceinline__ int cls_K(int cls) { return cls / kNumL + 1; }
+
+// Barrier 1 over the first `nthreads` threads of the block (a block tree may use
+// only part of the block; the other warps wait at barrier 0 meanwhile).
+__device__ __forceinline__ void tree_barrier(int nthreads)
+{
+    asm volatile("bar.sync 1, %0;" ::"r"(nthreads) : "memory");
+}
+__device__ __forceinline__ int cls_L(int cls) { return 1 << (cls % kNumL); }
+
+// Smallest L*K >= width with K in 1..8, L in {1..32}; ties go to the larger K
+// (more trees per warp, fewer shuffles per node).
+__host__ __device__ int pick_warp_class(int width)
+{
+    int best = -1, best_slots = 1 << 30;
+    for (int K = 8; K >= 1; --K) {
+        for (int l = 0; l < kNumL; ++l) {
+            const int slots = K << l;
+            if (slots >= width && slots < best_slots) {
+                best_slots = slots;
+                best = (K - 1) * kNumL + l;
+            }
+        }
+    }
+    return best;
+}
+
+__device__ __forceinline__ int work_bucket(unsigned long long work)
+{
+    // 4 buckets per octave, descending: heavy work sorts first.
+    const double lw = log2((double)work + 1.0);
+    int b = (int)(lw * 4.0);
+    if (b > kWorkBuckets - 1) b = kWorkBuckets - 1;
+    return kWorkBuckets - 1 - b;
+}
+
+// ---------------------------------------------------------------------------
+// Sizing, validation and binning.
+// ---------------------------------------------------------------------------
+
+__global__ void size_kernel(EngineParams p)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    int key = -1;
+    unsigned long long nodes = 0;
+    if (i < p.opt.n) {
+        Shape s;
+        int st = make_shape(s, p.opt.bond_maturity[i], p.opt.option_maturity[i], p.opt.term_unit[i],
+                            p.opt.term_steps[i], p.opt.a[i], p.opt.sigma[i], p.max_width);
+        const int8_t ty = p.opt.type[i];
+        const double X = p.opt.strike[i];
+        if (st == SHAPE_OK && ty != 0 && ty != 1) st = 6;
+        if (st == SHAPE_OK && !isfinite(X)) st = SHAPE_NONFINITE;
+        if (st != SHAPE_OK) {
+            atomicAdd(&p.s.status->bad_count, 1);
+            atomicMin(&p.s.status->first_bad, ((unsigned long long)(unsigned)i << 32) | (unsigned)st);
+            p.out[i] = __longlong_as_double(0x7ff8000000000000ll);
+            p.s.keys[i] = -1;
+        } else {
+            Tree t;
+            t.dt = s.dt; t.dr = s.dr; t.M = s.M; t.X = X;
+            t.idx = i; t.jmax = s.jmax; t.n = s.n; t.m = s.m; t.jc = s.jc; t.width = s.width;
+            t.term_unit = p.opt.term_unit[i]; t.type = ty; t.edges = (int8_t)s.edges;
+            p.s.trees[i] = t;
+            nodes = (unsigned long long)s.nodes;
+            const bool warp = s.width <= p.big_threshold;
+            const int cls = warp ? pick_warp_class(s.width) : 0;
+            const unsigned long long work = (unsigned long long)s.nodes + (unsigned long long)s.width;
+            key = ((warp ? 1 : 0) * kWorkBuckets + work_bucket(work)) * 64 + cls;
+            p.s.keys[i] = key;
+            atomicMax(&p.s.status->max_width, s.width);
+            atomicMax(&p.s.status->max_height, s.n);
+        }
+    }
+    // warp-aggregated histogram and node count
+    for (int off = 16; off > 0; off >>= 1) nodes += __shfl_xor_sync(FULL, nodes, off);
+    if (lane == 0 && nodes) atomicAdd(&p.s.status->nodes, nodes);
+    const unsigned peers = __match_any_sync(FULL, key);
+    if (key >= 0 && lane == __ffs(peers) - 1) atomicAdd(&p.s.hist[key], __popc(peers));
+}
+
+// One block: exclusive scans of the key histogram into bin starts and warp-task
+// starts.  kKeyBins / blockDim bins per thread.
+__global__ void scan_kernel(EngineParams p)
+{
+    constexpr int T = 1024;
+    constexpr int PER = kKeyBins / T;
+    __shared__ int s_a[T], s_b[T];
+    const int tid = threadIdx.x;
+    int cnt[PER], tsk[PER];
+    int sa = 0, sb = 0;
+    for (int q = 0; q < PER; ++q) {
+        const int b = tid * PER + q;
+        const int c = p.s.hist[b];
+        const bool warp = b >= kWorkBuckets * 64;
+        int t = 0;
+        if (warp && c > 0) {
+            const int G = 32 / cls_L(b & 63);
+            t = (c + G - 1) / G;
+        }
+        cnt[q] = c; tsk[q] = t; sa += c; sb += t;
+    }
+    s_a[tid] = sa; s_b[tid] = sb;
+    __syncthreads();
+    for (int off = 1; off < T; off <<= 1) {
+        int va = 0, vb = 0;
+        if (tid >= off) { va = s_a[tid - off]; vb = s_b[tid - off]; }
+        __syncthreads();
+        s_a[tid] += va; s_b[tid] += vb;
+        __syncthreads();
+    }
+    int ea = s_a[tid] - sa, eb = s_b[tid] - sb;
+    for (int q = 0; q < PER; ++q) {
+        const int b = tid * PER + q;
+        p.s.bin_start[b] = ea;
+        p.s.task_start[b] = eb;
+        ea += cnt[q]; eb += tsk[q];
+    }
+    if (tid == T - 1) p.s.status->n_warp_tasks = s_b[T - 1];
+    // block trees are the bins below the first warp bin
+    if (tid == (kWorkBuckets * 64) / PER) p.s.status->n_big = s_a[tid] - sa;
+}
+
+// Places every valid option at its sorted position and emits one warp task per
+// G consecutive small trees of a bin.
+__global__ void scatter_kernel(EngineParams p)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.opt.n) return;
+    const int key = p.s.keys[i];
+    if (key < 0) return;
+    const int q = atomicAdd(&p.s.fill[key], 1);
+    const int pos = p.s.bin_start[key] + q;
+    p.s.order[pos] = i;
+    if (key >= kWorkBuckets * 64) {
+        const int cls = key & 63;
+        const int G = 32 / cls_L(cls);
+        if (q % G == 0) {
+            WarpTask t;
+            t.start = pos;
+            const int left = p.s.hist[key] - q;
+            t.count = (int16_t)(left < G ? left : G);
+            t.cls = (int16_t)cls;
+            p.s.tasks[p.s.task_start[key] + q / G] = t;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Per-thread tree slice: K consecutive nodes k0 .. k0+K-1 of one tree.
+// ---------------------------------------------------------------------------
+
+template <typename R, int K>
+struct Ext {  // e[s + 2] is node k0 + s; e[0..1] left neighbours, e[K+2..K+3] right
+    R e[K + 4];
+};
+
+template <class Mode, int K>
+struct Slice {
+    typedef typename Mode::Row R;
+    typedef typename Mode::Scal S;
+
+    R r[K];          // current row
+    R c0[K], c1[K], c2[K];  // FP64: fa/fb/fc or ba/bb/bc.  Flux: U, D, g.
+    R cl, cr;        // flux: up of node k0-1, down of node k0+K
+    R jlo, jhi;      // edge jump coefficients of this slice (0 if none)
+    unsigned mlo, mhi;       // slots receiving / sending the low and high jumps
+    unsigned mlo2, mhi2;     // flux forward: slots that send the jumps (outflow)
+
+    // Coefficients for the forward sweep of tree `t`.
+    __device__ __forceinline__ void setup_forward(const Tree &t, int k0)
+    {
+        const int W = t.width, jc = t.jc, jmax = t.jmax;
+        mlo = mhi = mlo2 = mhi2 = 0;
+        jlo = jhi = (R)0;
+        if constexpr (!Mode::kFlux) {
+#pragma unroll
+            for (int s = 0; s < K; ++s) {
+                const int k = k0 + s;
+                double a = 0.0, b = 0.0, c = 0.0;
+                if (k < W) {
+                    const int j = k - jc;
+                    const double G = column_discount(j, t.dr, t.dt);
+                    const Branch me = branch(j, jmax, t.M);
+                    b = G * me.stay;
+                    if (k >= 1) a = G * branch(j - 1, jmax, t.M).up;
+                    if (k + 1 < W) c = G * branch(j + 1, jmax, t.M).down;
+                    if (t.edges && k == 2) { jlo = G * pu_b(-jmax, t.M); mlo |= 1u << s; }
+                    if (t.edges && k == W - 3) { jhi = G * pd_c(jmax, t.M); mhi |= 1u << s; }
+                }
+                c0[s] = a; c1[s] = b; c2[s] = c;
+                r[s] = (k == jc) ? 1.0 : 0.0;
+            }
+        } else {
+            const float Mf = (float)t.M, drdt = (float)(t.dr * t.dt);
+#pragma unroll
+            for (int s = 0; s < K; ++s) {
+                const int k = k0 + s;
+                float u = 0.f, d = 0.f, g = 0.f;
+                if (k < W) {
+                    const int j = k - jc;
+                    const float x = (float)j * Mf, x2 = x * x;
+                    g = expm1f(-(float)j * drdt);
+                    if (j == -jmax) {
+                        u = -1.0f / 3.0f - x2 + 2.0f * x;   // pm_b
+                        d = 0.f;
+                    } else if (j == jmax) {
+                        u = 0.f;
+                        d = -1.0f / 3.0f - x2 - 2.0f * x;   // pm_c
+                    } else {
+                        u = 1.0f / 6.0f + (x2 + x) * 0.5f;  // pu_a
+                        d = 1.0f / 6.0f + (x2 - x) * 0.5f;  // pd_a
+                    }
+                    if (t.edges) {
+                        if (k == 0) mlo2 |= 1u << s;
+                        if (k == 2) mlo |= 1u << s;
+                        if (k == W - 1) mhi2 |= 1u << s;
+                        if (k == W - 3) mhi |= 1u << s;
+                    }
+                }
+                c0[s] = u; c1[s] = d; c2[s] = g;
+                r[s] = (k == jc) ? 1.f : 0.f;
+            }
+            // neighbours' up (node k0-1) and down (node k0+K) coefficients
+            cl = 0.f; cr = 0.f;
+            {
+                const int kl = k0 - 1, kr = k0 + K;
+                if (kl >= 0 && kl < W) {
+                    const int j = kl - jc;
+                    const float x = (float)j * Mf, x2 = x * x;
+                    cl = (j == -jmax) ? (-1.0f / 3.0f - x2 + 2.0f * x) : (j == jmax ? 0.f : 1.0f / 6.0f + (x2 + x) * 0.5f);
+                }
+                if (kr < W) {
+                    const int j = kr - jc;
+                    const float x = (float)j * Mf, x2 = x * x;
+                    cr = (j == -jmax) ? 0.f : (j == jmax ? (-1.0f / 3.0f - x2 - 2.0f * x) : 1.0f / 6.0f + (x2 - x) * 0.5f);
+                }
+            }
+            if (t.edges) {
+                const float xb = (float)(-jmax) * Mf, xt = (float)jmax * Mf;
+                jlo = 1.0f / 6.0f + (xb * xb - xb) * 0.5f;  // pu_b: bottom edge jumps up two
+                jhi = 1.0f / 6.0f + (xt * xt + xt) * 0.5f;  // pd_c: top edge jumps down two
+            }
+        }
+    }
+
+    // Coefficients for the backward sweep; rows start at the bond's face value
+    // (flux form: as the deviation 0 from 100).
+    __device__ __forceinline__ void setup_backward(const Tree &t, int k0)
+    {
+        const int W = t.width, jc = t.jc, jmax = t.jmax;
+        mlo = mhi = 0;
+        if constexpr (!Mode::kFlux) {
+            jlo = jhi = 0.0;
+#pragma unroll
+            for (int s = 0; s < K; ++s) {
+                const int k = k0 + s;
+                double a = 0.0, b = 0.0, c = 0.0;
+                if (k < W) {
+                    const int j = k - jc;
+                    const double G = column_discount(j, t.dr, t.dt);
+                    const Branch me = branch(j, jmax, t.M);
+                    a = G * me.up; b = G * me.stay; c = G * me.down;
+                    if (t.edges && k == 0) { jlo = G * me.jump; mlo |= 1u << s; }
+                    if (t.edges && k == W - 1) { jhi = G * me.jump; mhi |= 1u << s; }
+                }
+                c0[s] = a; c1[s] = b; c2[s] = c;
+                r[s] = (k < W) ? 100.0 : 0.0;
+            }
+        } else {
+            // U, D, g and jlo/jhi are the same as the forward's; only masks change.
+#pragma unroll
+            for (int s = 0; s < K; ++s) {
+                const int k = k0 + s;
+                if (t.edges && k < W) {
+                    if (k == 0) mlo |= 1u << s;
+                    if (k == W - 1) mhi |= 1u << s;
+                }
+                r[s] = (R)0;
+            }
+        }
+    }
+
+    // One forward step: r <- G o gather(r), reading neighbours from x.
+    __device__ __forceinline__ void forward_step(const Ext<R, K> &x, bool edge_live, unsigned wlo, unsigned whi)
+    {
+        if constexpr (!Mode::kFlux) {
+            R v[K];
+#pragma unroll
+            for (int s = 0; s < K; ++s) {
+                R t = c0[s] * x.e[s + 1];
+                t = fma(c1[s], x.e[s + 2], t);
+                t = fma(c2[s], x.e[s + 3], t);
+                v[s] = t;
+            }
+            if (edge_live) {
+#pragma unroll
+                for (int s = 0; s < K; ++s) {
+                    if (wlo & (1u << s)) { if (mlo & (1u << s)) v[s] = fma(jlo, x.e[s], v[s]); }
+                    if (whi & (1u << s)) { if (mhi & (1u << s)) v[s] = fma(jhi, x.e[s + 4], v[s]); }
+                }
+            }
+#pragma unroll
+            for (int s = 0; s < K; ++s) r[s] = v[s];
+        } else {
+            R f[K], h[K], v[K];
+#pragma unroll
+            for (int s = 0; s < K; ++s) { f[s] = c0[s] * r[s]; h[s] = c1[s] * r[s]; }
+            const R fl = cl * x.e[1], hr = cr * x.e[K + 2];
+#pragma unroll
+            for (int s = 0; s < K; ++s) {
+                const R fin = (s == 0) ? fl : f[s - 1];
+                const R hin = (s == K - 1) ? hr : h[s + 1];
+                v[s] = (r[s] + (fin - f[s])) + (hin - h[s]);
+            }
+            if (edge_live) {
+#pragma unroll
+                for (int s = 0; s < K; ++s) {
+                    if (wlo & (1u << s)) {
+                        if (mlo2 & (1u << s)) v[s] = fma(-jlo, r[s], v[s]);
+                        if (mlo & (1u << s)) v[s] = fma(jlo, x.e[s], v[s]);
+                    }
+                    if (whi & (1u << s)) {
+                        if (mhi2 & (1u << s)) v[s] = fma(-jhi, r[s], v[s]);
+                        if (mhi & (1u << s)) v[s] = fma(jhi, x.e[s + 4], v[s]);
+                    }
+                }
+            }
+#pragma unroll
+            for (int s = 0; s < K; ++s) r[s] = fma(c2[s], v[s], v[s]);
+        }
+    }
+
+    // One backward step: r <- G o P r (flux: on the deviation from `base`).
+    __device__ __forceinline__ void backward_step(const Ext<R, K> &x, bool edge_live, unsigned wlo, unsigned whi, R base)
+    {
+        R v[K];
+        if constexpr (!Mode::kFlux) {
+#pragma unroll
+            for (int s = 0; s < K; ++s) {
+                R t = c0[s] * x.e[s + 3];
+                t = fma(c1[s], x.e[s + 2], t);
+                t = fma(c2[s], x.e[s + 1], t);
+                v[s] = t;
+            }
+            if (edge_live) {
+#pragma unroll
+                for (int s = 0; s < K; ++s) {
+                    if (wlo & (1u << s)) { if (mlo & (1u << s)) v[s] = fma(jlo, x.e[s + 4], v[s]); }
+                    if (whi & (1u << s)) { if (mhi & (1u << s)) v[s] = fma(jhi, x.e[s], v[s]); }
+                }
+            }
+#pragma unroll
+            for (int s = 0; s < K; ++s) r[s] = v[s];
+        } else {
+#pragma unroll
+            for (int s = 0; s < K; ++s) {
+                const R d0 = x.e[s + 2];
+                const R up = x.e[s + 3] - d0, dn = x.e[s + 1] - d0;
+                v[s] = d0 + fma(c0[s], up, c1[s] * dn);
+            }
+            if (edge_live) {
+#pragma unroll
+                for (int s = 0; s < K; ++s) {
+                    if (wlo & (1u << s)) { if (mlo & (1u << s)) v[s] = fma(jlo, x.e[s + 4] - x.e[s + 2], v[s]); }
+                    if (whi & (1u << s)) { if (mhi & (1u << s)) v[s] = fma(jhi, x.e[s] - x.e[s + 2], v[s]); }
+                }
+            }
+#pragma unroll
+            for (int s = 0; s < K; ++s) r[s] = fma(c2[s], v[s] + base, v[s]);
+        }
+    }
+
+    __device__ __forceinline__ S partial_sum(int k0, int W) const
+    {
+        S acc = (S)0;
+#pragma unroll
+        for (int s = 0; s < K; ++s)
+            if (k0 + s < W) acc += (S)r[s];
+        return acc;
+    }
+
+    // Payoff at the maturity step: value = kappa * (base + row).
+    __device__ __forceinline__ void payoff(S kappa, R base, double X, int type)
+    {
+#pragma unroll
+        for (int s = 0; s < K; ++s) {
+            const S c = kappa * ((S)base + (S)r[s]);
+            const S x = (S)X;
+            const S p = (type == 1) ? (x - c) : (c - x);
+            r[s] = (R)(p < (S)0 ? (S)0 : p);
+        }
+    }
+
+    __device__ __forceinline__ R pick(int slot) const
+    {
+        R v = r[0];
+#pragma unroll
+        for (int s = 1; s < K; ++s) v = (s == slot) ? r[s] : v;
+        return v;
+    }
+};
+
+template <typename R, int K>
+__device__ __forceinline__ void fill_ext(Ext<R, K> &x, const R (&r)[K])
+{
+#pragma unroll
+    for (int s = 0; s < K; ++s) x.e[s + 2] = r[s];
+}
+
+// Neighbour values within a warp segment of L lanes holding one tree.
+template <typename R, int K>
+__device__ __forceinline__ void exchange_warp(Ext<R, K> &x, const R (&r)[K], int lis, int L)
+{
+    fill_ext(x, r);
+    if constexpr (K >= 2) {
+        const R a = __shfl_up_sync(FULL, r[K - 1], 1), b = __shfl_up_sync(FULL, r[K - 2], 1);
+        const R c = __shfl_down_sync(FULL, r[0], 1), d = __shfl_down_sync(FULL, r[1], 1);
+        const bool hl = lis > 0, hr = lis + 1 < L;
+        x.e[1] = hl ? a : (R)0; x.e[0] = hl ? b : (R)0;
+        x.e[K + 2] = hr ? c : (R)0; x.e[K + 3] = hr ? d : (R)0;
+    } else {
+        const R a = __shfl_up_sync(FULL, r[0], 1), b = __shfl_up_sync(FULL, r[0], 2);
+        const R c = __shfl_down_sync(FULL, r[0], 1), d = __shfl_down_sync(FULL, r[0], 2);
+        x.e[1] = lis >= 1 ? a : (R)0; x.e[0] = lis >= 2 ? b : (R)0;
+        x.e[3] = lis + 1 < L ? c : (R)0; x.e[4] = lis + 2 < L ? d : (R)0;
+    }
+}
+
+// Neighbour values across a whole block: shuffles inside each warp, the first and
+// last two nodes of every warp through shared memory (double buffered, so one
+// barrier per step is enough).
+template <typename R, int K>
+__device__ __forceinline__ void exchange_block(Ext<R, K> &x, const R (&r)[K], R *sh, int parity, int nthreads)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = nthreads >> 5;
+    R *buf = sh + parity * (32 * 4);
+    if constexpr (K >= 2) {
+        if (lane == 0) { buf[warp * 4 + 0] = r[0]; buf[warp * 4 + 1] = r[1]; }
+        if (lane == 31) { buf[warp * 4 + 2] = r[K - 2]; buf[warp * 4 + 3] = r[K - 1]; }
+    } else {
+        if (lane < 2) buf[warp * 4 + lane] = r[0];
+        if (lane >= 30) buf[warp * 4 + lane - 28] = r[0];
+    }
+    tree_barrier(nthreads);
+    exchange_warp<R, K>(x, r, lane, 32);
+    const bool hasl = warp > 0, hasr = warp + 1 < nw;
+    if constexpr (K >= 2) {
+        if (lane == 0) {
+            x.e[1] = hasl ? buf[(warp - 1) * 4 + 3] : (R)0;
+            x.e[0] = hasl ? buf[(warp - 1) * 4 + 2] : (R)0;
+        }
+        if (lane == 31) {
+            x.e[K + 2] = hasr ? buf[(warp + 1) * 4 + 0] : (R)0;
+            x.e[K + 3] = hasr ? buf[(warp + 1) * 4 + 1] : (R)0;
+        }
+    } else {
+        if (lane == 0) {
+            x.e[1] = hasl ? buf[(warp - 1) * 4 + 3] : (R)0;
+            x.e[0] = hasl ? buf[(warp - 1) * 4 + 2] : (R)0;
+        }
+        if (lane == 1) x.e[0] = hasl ? buf[(warp - 1) * 4 + 3] : (R)0;
+        if (lane == 31) {
+            x.e[3] = hasr ? buf[(warp + 1) * 4 + 0] : (R)0;
+            x.e[4] = hasr ? buf[(warp + 1) * 4 + 1] : (R)0;
+        }
+        if (lane == 30) x.e[4] = hasr ? buf[(warp + 1) * 4 + 0] : (R)0;
+    }
+}
+
+// Scalars of one tree after its forward sweep.
+template <typename S>
+struct Scales {
+    S kappa;  // s_n / s_m, applied at the maturity step
+    S final;  // s_m (payoff) or s_n (bond only)
+};
+
+template <typename S>
+__device__ __forceinline__ Scales<S> tree_scales(const Tree &t, S sum_m1, S sum_n1, const DevYield &yc)
+{
+    Scales<S> sc;
+    const S dt = (S)t.dt;
+    const S *rates;
+    if constexpr (sizeof(S) == 8) rates = (const S *)yc.rate; else rates = (const S *)yc.rate_f;
+    const S Pn = discount_at_step<S>(t.n, dt, t.term_unit, rates, yc.day, yc.n);
+    const S sn = Pn / sum_n1;
+    if (t.m >= 0 && t.m < t.n) {
+        S sm = (S)1;
+        if (t.m >= 1) {
+            const S Pm = discount_at_step<S>(t.m, dt, t.term_unit, rates, yc.day, yc.n);
+            sm = Pm / sum_m1;
+        }
+        sc.kappa = sn / sm;
+        sc.final = sm;
+    } else {
+        sc.kappa = (S)1;
+        sc.final = sn;
+    }
+    return sc;
+}
+
+__device__ __forceinline__ bool pays_at(const Tree &t) { return t.m >= 0 && t.m < t.n; }
+
+// ---------------------------------------------------------------------------
+// Small trees: 32/L trees per warp, L lanes x K nodes each.
+// ---------------------------------------------------------------------------
+template <class Mode, int K>
+__device__ void price_warp_task(const EngineParams &p, const WarpTask &task)
+{
+    typedef typename Mode::Row R;
+    typedef typename Mode::Scal S;
+    const int lane = threadIdx.x & 31;
+    const int L = cls_L(task.cls);
+    const int g = lane / L, lis = lane & (L - 1);
+    const bool valid = g < task.count;
+    Tree t;
+    if (valid) {
+        t = p.s.trees[p.s.order[task.start + g]];
+    } else {
+        t.n = 0; t.m = -1; t.width = 1; t.jc = 0; t.jmax = 1; t.edges = 0; t.idx = -1;
+        t.dt = 1.0; t.dr = 0.0; t.M = -0.5; t.X = 0.0; t.type = 0; t.term_unit = 365;
+    }
+    const int k0 = lis * K;
+    const int W = t.width;
+    Slice<Mode, K> sl;
+    Ext<R, K> x;
+
+    // ---- forward sweep: rows 1 .. n-1, sums of rows m-1 and n-1
+    sl.setup_forward(t, k0);
+    const unsigned wlo = __reduce_or_sync(FULL, sl.mlo | sl.mlo2), whi = __reduce_or_sync(FULL, sl.mhi | sl.mhi2);
+    S sum_m1 = (S)1, sum_n1 = (S)1;
+    const int fsteps = __reduce_max_sync(FULL, (unsigned)(t.n > 1 ? t.n - 1 : 0));
+    for (int i = 0; i < fsteps; ++i) {
+        exchange_warp<R, K>(x, sl.r, lis, L);
+        const bool live = t.edges && i >= t.jmax;
+        const bool any_live = __any_sync(FULL, live);
+        R keep[K];
+#pragma unroll
+        for (int s = 0; s < K; ++s) keep[s] = sl.r[s];
+        sl.forward_step(x, any_live, live ? wlo : 0u, live ? whi : 0u);
+        const bool run = i < t.n - 1;
+        if (!run) {
+#pragma unroll
+            for (int s = 0; s < K; ++s) sl.r[s] = keep[s];
+        }
+        const int row = i + 1;
+        const bool need = run && (row == t.m - 1 || row == t.n - 1);
+        if (__any_sync(FULL, need)) {
+            S acc = sl.partial_sum(k0, W);
+            for (int off = 1; off < L; off <<= 1) acc += __shfl_xor_sync(FULL, acc, off);
+            if (need) {
+                if (row == t.m - 1) sum_m1 = acc;
+                if (row == t.n - 1) sum_n1 = acc;
+            }
+        }
+    }
+    const Scales<S> sc = tree_scales<S>(t, sum_m1, sum_n1, p.yc);
+
+    // ---- backward sweep
+    sl.setup_backward(t, k0);
+    const unsigned blo = __reduce_or_sync(FULL, sl.mlo), bhi = __reduce_or_sync(FULL, sl.mhi);
+    R base = Mode::kFlux ? (R)100 : (R)0;
+    const int bsteps = __reduce_max_sync(FULL, (unsigned)(t.n > 0 ? t.n : 0));
+    for (int i = bsteps - 1; i >= 0; --i) {
+        exchange_warp<R, K>(x, sl.r, lis, L);
+        const bool live = t.edges && i >= t.jmax;
+        const bool any_live = __any_sync(FULL, live);
+        R keep[K];
+#pragma unroll
+        for (int s = 0; s < K; ++s) keep[s] = sl.r[s];
+        sl.backward_step(x, any_live, live ? blo : 0u, live ? bhi : 0u, base);
+        if (i >= t.n) {
+#pragma unroll
+            for (int s = 0; s < K; ++s) sl.r[s] = keep[s];
+        } else if (i == t.m) {
+            sl.payoff(sc.kappa, base, t.X, t.type);
+            base = (R)0;
+        }
+    }
+
+    // ---- price at the root node
+    const int owner = t.jc / K, slot = t.jc - owner * K;
+    const R v = sl.pick(slot);
+    if (valid && lis == owner) {
+        double price;
+        if (t.n <= 0) price = 100.0;
+        else if (pays_at(t)) price = (double)(sc.final * (S)v);
+        else price = (double)(sc.final * ((S)base + (S)v));
+        p.out[t.idx] = price;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Wide trees: one whole block per tree, K nodes per thread.
+// ---------------------------------------------------------------------------
+template <class Mode, int K>
+__device__ void price_block_tree(const EngineParams &p, const Tree &t, int nthreads, typename Mode::Row *sh_x,
+                                 typename Mode::Scal *sh_red)
+{
+    typedef typename Mode::Row R;
+    typedef typename Mode::Scal S;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = nthreads >> 5;
+    const int k0 = tid * K;
+    const int W = t.width, jc = t.jc;
+    const int wk0 = warp * 32 * K, wk1 = wk0 + 32 * K;  // this warp's node range
+    Slice<Mode, K> sl;
+    Ext<R, K> x;
+    int parity = 0;
+
+    sl.setup_forward(t, k0);
+    const unsigned wlo = __reduce_or_sync(FULL, sl.mlo | sl.mlo2), whi = __reduce_or_sync(FULL, sl.mhi | sl.mhi2);
+    S sum_m1 = (S)1, sum_n1 = (S)1;
+    const int fsteps = t.n > 1 ? t.n - 1 : 0;
+    for (int i = 0; i < fsteps; ++i) {
+        exchange_block<R, K>(x, sl.r, sh_x, parity, nthreads);
+        parity ^= 1;
+        // rows outside the cone of row i+1 stay zero: skip whole warps there
+        const int reach = (i + 1 < jc) ? i + 1 : jc;
+        const bool active = wk1 > jc - reach && wk0 <= jc + reach && wk0 < W;
+        if (active) sl.forward_step(x, t.edges && i >= t.jmax, wlo, whi);
+        const int row = i + 1;
+        if (row == t.m - 1 || row == t.n - 1) {
+            S acc = sl.partial_sum(k0, W);
+            for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(FULL, acc, off);
+            if (lane == 0) sh_red[warp] = acc;
+            tree_barrier(nthreads);
+            S tot = (S)0;
+            for (int w = 0; w < nw; ++w) tot += sh_red[w];
+            tree_barrier(nthreads);
+            if (row == t.m - 1) sum_m1 = tot;
+            if (row == t.n - 1) sum_n1 = tot;
+        }
+    }
+    const Scales<S> sc = tree_scales<S>(t, sum_m1, sum_n1, p.yc);
+
+    sl.setup_backward(t, k0);
+    const unsigned blo = __reduce_or_sync(FULL, sl.mlo), bhi = __reduce_or_sync(FULL, sl.mhi);
+    R base = Mode::kFlux ? (R)100 : (R)0;
+    for (int i = t.n - 1; i >= 0; --i) {
+        exchange_block<R, K>(x, sl.r, sh_x, parity, nthreads);
+        parity ^= 1;
+        const int reach = (i < t.jmax) ? i : t.jmax;
+        const bool active = wk1 > jc - reach && wk0 <= jc + reach && wk0 < W;
+        if (active) sl.backward_step(x, t.edges && i >= t.jmax, blo, bhi, base);
+        if (i == t.m) {
+            sl.payoff(sc.kappa, base, t.X, t.type);
+            base = (R)0;
+        }
+    }
+
+    const int owner = jc / K, slot = jc - owner * K;
+    const R v = sl.pick(slot);
+    if (tid == owner) {
+        double price;
+        if (t.n <= 0) price = 100.0;
+        else if (pays_at(t)) price = (double)(sc.final * (S)v);
+        else price = (double)(sc.final * ((S)base + (S)v));
+        p.out[t.idx] = price;
+    }
+}
+
+template <class Mode>
+__global__ void __launch_bounds__(kPricingThreads, 1) price_kernel(EngineParams p)
+{
+    typedef typename Mode::Row R;
+    typedef typename Mode::Scal S;
+    __shared__ R sh_x[2 * 32 * 4];
+    __shared__ S sh_red[32];
+    __shared__ int sh_task;
+    unsigned long long t_start = 0;
+    if (p.record_busy && threadIdx.x == 0) asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t_start));
+
+    // Phase 1: wide trees, one per block, heaviest first.
+    const int n_big = p.s.status->n_big;
+    for (;;) {
+        if (threadIdx.x == 0) sh_task = atomicAdd(&p.s.status->big_counter, 1);
+        __syncthreads();
+        const int tsk = sh_task;
+        __syncthreads();
+        if (tsk >= n_big) break;
+        const Tree t = p.s.trees[p.s.order[tsk]];
+        // threads for this tree: the configured count, at least width/8, at most the block
+        int nt = p.block_threads;
+        const int need = ((t.width + kMaxBlockK - 1) / kMaxBlockK + 31) & ~31;
+        if (nt < need) nt = need;
+        if (nt > (int)blockDim.x) nt = (int)blockDim.x;
+        const int K = (t.width + nt - 1) / nt;
+        if ((int)threadIdx.x < nt) {
+            switch (K) {
+                case 1: price_block_tree<Mode, 1>(p, t, nt, sh_x, sh_red); break;
+                case 2: price_block_tree<Mode, 2>(p, t, nt, sh_x, sh_red); break;
+                case 3: price_block_tree<Mode, 3>(p, t, nt, sh_x, sh_red); break;
+                case 4: price_block_tree<Mode, 4>(p, t, nt, sh_x, sh_red); break;
+                case 5: price_block_tree<Mode, 5>(p, t, nt, sh_x, sh_red); break;
+                case 6: price_block_tree<Mode, 6>(p, t, nt, sh_x, sh_red); break;
+                case 7: price_block_tree<Mode, 7>(p, t, nt, sh_x, sh_red); break;
+                default: price_block_tree<Mode, 8>(p, t, nt, sh_x, sh_red); break;
+            }
+        }
+        __syncthreads();  // shared buffers are reused by the next tree
+    }
+
+    // Phase 2: warp tasks, each warp on its own.
+    const int n_tasks = p.s.status->n_warp_tasks;
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        int tsk = 0;
+        if (lane == 0) tsk = atomicAdd(&p.s.status->warp_counter, 1);
+        tsk = __shfl_sync(FULL, tsk, 0);
+        if (tsk >= n_tasks) break;
+        const WarpTask wt = p.s.tasks[tsk];
+        switch (cls_K(wt.cls)) {
+            case 1: price_warp_task<Mode, 1>(p, wt); break;
+            case 2: price_warp_task<Mode, 2>(p, wt); break;
+            case 3: price_warp_task<Mode, 3>(p, wt); break;
+            case 4: price_warp_task<Mode, 4>(p, wt); break;
+            case 5: price_warp_task<Mode, 5>(p, wt); break;
+            case 6: price_warp_task<Mode, 6>(p, wt); break;
+            case 7: price_warp_task<Mode, 7>(p, wt); break;
+            default: price_warp_task<Mode, 8>(p, wt); break;
+        }
+    }
+    if (p.record_busy) {
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned long long t_end;
+            asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t_end));
+            p.s.cta_busy[blockIdx.x] = t_end - t_start;
+        }
+    }
+}
+
+}  // namespace
+
+int warp_class_of(int width, int *K, int *L)
+{
+    const int c = pick_warp_class(width);
+    if (c < 0) return -1;
+    if (K) *K = c / kNumL + 1;
+    if (L) *L = 1 << (c % kNumL);
+    return c;
+}
+
+int sizing_launches() { return 3; }
+
+cudaError_t launch_sizing(const EngineParams &p, cudaStream_t stream)
+{
+    const int n = p.opt.n;
+    cudaError_t e;
+    if ((e = cudaMemsetAsync(p.s.hist, 0, sizeof(int32_t) * kKeyBins * 2, stream)) != cudaSuccess) return e;
+    // status: zero counters, first_bad = all ones
+    if ((e = cudaMemsetAsync(p.s.status, 0, sizeof(RunStatus), stream)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(&p.s.status->first_bad, 0xff, 8, stream)) != cudaSuccess) return e;
+    if (n > 0) {
+        size_kernel<<<(n + 255) / 256, 256, 0, stream>>>(p);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    scan_kernel<<<1, 1024, 0, stream>>>(p);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if (n > 0) {
+        scatter_kernel<<<(n + 255) / 256, 256, 0, stream>>>(p);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+cudaError_t launch_pricing(const EngineParams &p, int mode, int grid, cudaStream_t stream)
+{
+    switch (mode) {
+        case MODE_BATCHED_FP64: price_kernel<ModeF64><<<grid, kPricingThreads, 0, stream>>>(p); break;
+        case MODE_BATCHED_FP32: price_kernel<ModeF32><<<grid, kPricingThreads, 0, stream>>>(p); break;
+        case MODE_BATCHED_MIXED: price_kernel<ModeMix><<<grid, kPricingThreads, 0, stream>>>(p); break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+int pricing_blocks_per_sm(int mode)
+{
+    const int block_threads = kPricingThreads;
+    int nb = 0;
+    cudaError_t e = cudaErrorInvalidValue;
+    switch (mode) {
+        case MODE_BATCHED_FP64: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, price_kernel<ModeF64>, block_threads, 0); break;
+        case MODE_BATCHED_FP32: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, price_kernel<ModeF32>, block_threads, 0); break;
+        case MODE_BATCHED_MIXED: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, price_kernel<ModeMix>, block_threads, 0); break;
+        default: break;
+    }
+    return e == cudaSuccess ? nb : 0;
+}
+
+}  // namespace hwt

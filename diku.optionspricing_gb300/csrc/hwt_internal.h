@@ -1,0 +1,115 @@
+// Internal structures shared by the batched engine, the plain kernel and the
+// C-ABI host code.  Not part of the public interface (include/hwtree.h is).
+#pragma once
+
+#include <stdint.h>
+#include <cuda_runtime.h>
+
+namespace hwt {
+
+// Precision policy of a pricing run.
+enum Mode : int {
+    MODE_PLAIN_FP64 = 0,    // one block per option, per-step alpha fit as the reference does
+    MODE_BATCHED_FP64 = 1,  // binned persistent engine, double rows
+    MODE_BATCHED_FP32 = 2,  // float rows, float sums and scales
+    MODE_BATCHED_MIXED = 3, // float rows, double sums, scales, payoff and final discount
+};
+
+// Device copy of the option records (SoA, common/Options.hpp:48-58 with real=double).
+struct DevOptions {
+    int32_t n;
+    const double *strike, *bond_maturity, *option_maturity;
+    const uint16_t *term_unit, *term_steps;
+    const double *a, *sigma;
+    const int8_t *type;
+};
+
+// Device copy of the yield curve (common/Yield.hpp:14-40): zero rates and days.
+struct DevYield {
+    int32_t n;
+    const double *rate;
+    const float *rate_f;
+    const int32_t *day;
+};
+
+// One option's tree as the sizing pass leaves it for the pricing pass.
+struct Tree {
+    double dt, dr, M, X;
+    int32_t idx;        // position in the caller's arrays
+    int32_t jmax, n, m; // edge index, height, maturity step
+    int32_t jc, width;  // half-width and width of the nodes that can carry value
+    uint16_t term_unit;
+    int8_t type;        // 0 = CALL, 1 = PUT
+    int8_t edges;       // 1 when the +-jmax edge branching is reached
+};
+
+// A group of small trees priced together by one warp: `count` trees of the same
+// warp class starting at `start` in the sorted order.
+struct WarpTask {
+    int32_t start;
+    int16_t count;
+    int16_t cls;
+};
+
+// Warp classes: L lanes per tree (power of two), K nodes per lane; L*K >= width.
+constexpr int kWarpK[] = {1, 2, 3, 4, 5, 6, 7, 8};
+constexpr int kNumK = 8;
+constexpr int kNumL = 6;                       // L = 1, 2, 4, 8, 16, 32
+constexpr int kNumWarpClasses = kNumK * kNumL; // class = (K-1) * kNumL + log2(L)
+constexpr int kMaxWarpWidth = 32 * 8;          // wider trees go to a whole block
+constexpr int kMaxBlockK = 8;                  // nodes per thread for block trees
+constexpr int kPricingThreads = 512;           // threads of every pricing block
+constexpr int kMaxTreeWidth = kMaxBlockK * kPricingThreads;  // widest tree accepted
+
+// Sort keys: small trees after big ones; both by descending work.
+constexpr int kWorkBuckets = 128;
+constexpr int kKeyBins = 2 * kWorkBuckets * 64; // [is_warp][bucket][class]
+
+// Per-run status written by the device (read back after each run).
+struct RunStatus {
+    unsigned long long first_bad; // (index << 32) | reason of the lowest rejected option; all ones if none
+    unsigned long long nodes;     // active nodes of one pass, summed over valid options
+    int32_t bad_count;            // options rejected by validation
+    int32_t n_big;                // trees priced by whole blocks
+    int32_t n_warp_tasks;         // warp tasks
+    int32_t big_counter;          // work-queue heads
+    int32_t warp_counter;
+    int32_t max_width;            // widest / tallest valid tree
+    int32_t max_height;
+    int32_t pad;
+};
+
+struct Scratch {
+    Tree *trees;            // [cap]
+    int32_t *keys;          // [cap]
+    int32_t *order;         // [cap] sorted position -> option
+    WarpTask *tasks;        // [cap]
+    int32_t *hist;          // [kKeyBins], followed in memory by fill
+    int32_t *fill;          // [kKeyBins]
+    int32_t *bin_start;     // [kKeyBins]
+    int32_t *task_start;    // [kKeyBins]
+    RunStatus *status;      // [1]
+    unsigned long long *cta_busy; // [max grid] per-CTA busy cycles (tail imbalance)
+};
+
+struct EngineParams {
+    DevOptions opt;
+    DevYield yc;
+    Scratch s;
+    double *out;
+    int32_t max_width;
+    int32_t block_threads;  // preferred threads for one block tree (raised to width/8)
+    int32_t big_threshold;  // widths above this go to whole blocks
+    int32_t record_busy;
+};
+
+// Launchers (hwt_batched.cu / hwt_plain.cu).  All enqueue on `stream`; none syncs.
+cudaError_t launch_sizing(const EngineParams &p, cudaStream_t stream);
+cudaError_t launch_pricing(const EngineParams &p, int mode, int grid, cudaStream_t stream);
+int pricing_blocks_per_sm(int mode);
+cudaError_t launch_plain(const EngineParams &p, int max_width, int max_height, cudaStream_t stream);
+size_t plain_smem_bytes(int max_width, int max_height);
+int warp_class_of(int width, int *K, int *L);
+int sizing_launches();
+
+}  // namespace hwt

@@ -1,0 +1,117 @@
+"""Seeded synthetic option batches with the shapes of the benchmark configurations.
+
+No public data set exists for these workloads; every batch is generated here from a
+fixed numpy seed so the GPU path, the oracle and the CPU baseline see identical
+inputs.  Records use the reference's SoA option fields (common/Options.hpp:48-58):
+strike, bond maturity (Maturities), option maturity (Lengths), term unit, term steps
+per year, mean reversion a, volatility sigma, type (0 = CALL, 1 = PUT).
+
+The yield curve is 11 nodes at 0.25/0.5/1/2/3/5/7/10/15/20/30 years, held as whole
+days (common/Yield.hpp:17-18 stores int32 days), with continuously compounded zero
+rates rising linearly in maturity from 1.0% to 4.0%.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+CURVE_YEARS = (0.25, 0.5, 1.0, 2.0, 3.0, 5.0, 7.0, 10.0, 15.0, 20.0, 30.0)
+
+
+def yield_curve():
+    """(rates float64[11], days int32[11]) of the synthetic curve."""
+    years = np.array(CURVE_YEARS)
+    days = np.array([int(y * 365 + 0.5) for y in CURVE_YEARS], dtype=np.int32)
+    rates = 0.01 + 0.03 * (years - years[0]) / (years[-1] - years[0])
+    return rates.astype(np.float64), days
+
+
+def _curve_rate(t_years, rates, days, term_unit=365):
+    """Zero rate at t the way common/Domain.hpp:11-46 interpolates it (whole days)."""
+    t_days = np.floor(np.asarray(t_years, dtype=np.float64) * term_unit + 0.5).astype(np.int64)
+    out = np.empty(t_days.shape, dtype=np.float64)
+    for idx, td in np.ndenumerate(t_days):
+        if td <= days[0]:
+            out[idx] = rates[0]
+        elif td > days[-1]:
+            out[idx] = rates[-1]
+        else:
+            s = int(np.searchsorted(days, td, side="left"))
+            f = s - 1
+            out[idx] = rates[f] + (td - days[f]) / float(days[s] - days[f]) * (rates[s] - rates[f])
+    return out
+
+
+def forward_bond_price(option_maturity, bond_maturity, rates=None, days=None):
+    """100 * P(0,T) / P(0,t) from the curve's zero rates."""
+    if rates is None:
+        rates, days = yield_curve()
+    t = np.asarray(option_maturity, dtype=np.float64)
+    T = np.asarray(bond_maturity, dtype=np.float64)
+    pt = np.exp(-_curve_rate(t, rates, days) * t)
+    pT = np.exp(-_curve_rate(T, rates, days) * T)
+    return 100.0 * pT / pt
+
+
+def _batch(strike, T, t, steps, a, sigma, typ):
+    n = len(strike)
+    return dict(
+        strike=np.asarray(strike, dtype=np.float64),
+        bond_maturity=np.asarray(T, dtype=np.float64),
+        option_maturity=np.asarray(t, dtype=np.float64),
+        term_unit=np.full(n, 365, dtype=np.uint16),
+        term_steps=np.asarray(steps, dtype=np.uint16),
+        a=np.asarray(a, dtype=np.float64),
+        sigma=np.asarray(sigma, dtype=np.float64),
+        type=np.asarray(typ, dtype=np.int8),
+    )
+
+
+def uniform_book(n=1000, seed=0):
+    """1,000 options: t=5y, T=10y, 12 steps/year (jmax 23, width 47, height 120),
+    a=0.10, sigma=0.01, strike U[75,95], call/put 50/50."""
+    rng = np.random.default_rng(seed)
+    return _batch(rng.uniform(75.0, 95.0, n), np.full(n, 10.0), np.full(n, 5.0), np.full(n, 12),
+                  np.full(n, 0.10), np.full(n, 0.01), rng.integers(0, 2, n))
+
+
+def uneven_batch(n=30000, seed=1):
+    """30,000 uneven options: t U{1..10}, T = t + U{1..10}, steps/year U{6..48},
+    a U[0.02,0.20], sigma U[0.005,0.02], strike = forward bond price x U[0.9,1.1]."""
+    rng = np.random.default_rng(seed)
+    t = rng.integers(1, 11, n).astype(np.float64)
+    T = t + rng.integers(1, 11, n)
+    steps = rng.integers(6, 49, n)
+    a = rng.uniform(0.02, 0.20, n)
+    sigma = rng.uniform(0.005, 0.02, n)
+    strike = forward_bond_price(t, T) * rng.uniform(0.9, 1.1, n)
+    return _batch(strike, T, t, steps, a, sigma, rng.integers(0, 2, n))
+
+
+def skewed_batch(n=100000, seed=2, heavy_fraction=0.01):
+    """100,000 options, 1% heavy.  Light: a U[0.10,0.20], 12 steps/year, t U{1..5},
+    T U{t+1..10}.  Heavy: a U[0.01,0.02], steps/year U{48..96}, t U{10..20},
+    T U{t+1..30}.  sigma=0.01, strike U[75,95], call/put 50/50 for both."""
+    rng = np.random.default_rng(seed)
+    heavy = np.zeros(n, dtype=bool)
+    heavy[rng.permutation(n)[: int(round(n * heavy_fraction))]] = True
+    t = np.where(heavy, rng.integers(10, 21, n), rng.integers(1, 6, n)).astype(np.float64)
+    span = np.where(heavy, 30.0 - t, 10.0 - t)
+    T = t + 1.0 + np.floor(rng.uniform(0.0, 1.0, n) * span)
+    steps = np.where(heavy, rng.integers(48, 97, n), 12)
+    a = np.where(heavy, rng.uniform(0.01, 0.02, n), rng.uniform(0.10, 0.20, n))
+    return _batch(rng.uniform(75.0, 95.0, n), T, t, steps, a, np.full(n, 0.01), rng.integers(0, 2, n))
+
+
+def book_batch(count=100):
+    """The reference's 'Book options' unit-test batch (test/TestCuda.cu:20-31):
+    t=3, T=9, strike 63, term unit 365, steps 1..count, a=0.1, sigma=0.01, PUT."""
+    k = np.arange(1, count + 1)
+    return _batch(np.full(count, 63.0), np.full(count, 9.0), np.full(count, 3.0), k,
+                  np.full(count, 0.1), np.full(count, 0.01), np.ones(count))
+
+
+WORKLOADS = {
+    "uniform_1k": uniform_book,
+    "uneven_30k": uneven_batch,
+    "skewed_100k": skewed_batch,
+}

@@ -1,0 +1,184 @@
+/*
+ * hwtree.h - C ABI of the GB300 Hull-White trinomial-tree batch pricer.
+ *
+ * Drop-in boundary for the batch pricing path of the reference project
+ * (MartinMetaksov/diku.OptionsPricing).  The reference has no FFI; its pricing
+ * entry points are C++ calls:
+ *   seq::computeOptions(const Options&, const Yield&, std::vector<real>&)
+ *       seq/Seq.hpp:181-190
+ *   cuda::option::KernelRunBase::run(const Options&, const Yield&,
+ *       std::vector<real>&, int blockSize, SortType, bool isTest)
+ *       cuda-option/Kernel.cuh:303-314
+ *   cuda::multi::KernelRunBase::run(...)  cuda-multi/Kernel.cuh:375-404
+ * Each is replaced by hwt_price() below; the records are the reference's SoA
+ * option and yield arrays (common/Options.hpp:48-58, common/Yield.hpp:14-18)
+ * with real = double.  include/hwtree.hpp wraps this ABI in the reference's own
+ * C++ record and call shapes.
+ *
+ * Plain C types only; no exceptions or process exits cross this boundary.  All
+ * functions return HWT_OK (0) or a negative HWT_E* code; hwt_last_error() gives
+ * the message.  One context per host thread; calls on one context are
+ * serialised by the caller.
+ */
+#ifndef HWTREE_H
+#define HWTREE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HWT_ABI_VERSION 1
+
+/* Status codes. */
+#define HWT_OK 0
+#define HWT_EINVAL (-1)      /* bad argument or option record (a <= 0, zero steps, bad type, too wide) */
+#define HWT_ECUDA (-2)       /* CUDA runtime error */
+#define HWT_ENOMEM (-3)      /* device or pinned host allocation failed */
+#define HWT_EUNSUPPORTED (-4)/* mode not available for these inputs */
+#define HWT_ENODEV (-5)      /* no CUDA device */
+
+/* Pricing modes.  The reference selects precision at compile time
+ * (common/Real.hpp:9-21); here it is a run-time argument. */
+#define HWT_PLAIN_FP64 0     /* one block per option, reference step structure, double */
+#define HWT_BATCHED_FP64 1   /* binned persistent engine, double */
+#define HWT_BATCHED_FP32 2   /* binned persistent engine, float throughout */
+#define HWT_BATCHED_MIXED 3  /* float rows, double alpha-fit sums, scales, payoff, discount */
+
+/* Sort orders accepted for compatibility with the reference's -s flag
+ * (common/Options.hpp:15-22).  Results never depend on them; the engine always
+ * bins by width x height and orders work heaviest first. */
+#define HWT_SORT_NONE '-'
+#define HWT_SORT_WIDTH_DESC 'W'
+#define HWT_SORT_WIDTH_ASC 'w'
+#define HWT_SORT_HEIGHT_DESC 'H'
+#define HWT_SORT_HEIGHT_ASC 'h'
+
+/* Option records, SoA, one entry per option (common/Options.hpp:48-58).
+ * strike = StrikePrices, bond_maturity = Maturities [years], option_maturity =
+ * Lengths [years], term_unit = TermUnits [days], term_steps = TermStepCounts
+ * [steps per term unit year], a = ReversionRates, sigma = Volatilities,
+ * type = Types (0 = CALL, 1 = PUT). */
+typedef struct hwt_options {
+    int32_t n;
+    const double *strike;
+    const double *bond_maturity;
+    const double *option_maturity;
+    const uint16_t *term_unit;
+    const uint16_t *term_steps;
+    const double *a;
+    const double *sigma;
+    const int8_t *type;
+} hwt_options;
+
+/* Yield curve (common/Yield.hpp:14-18): continuously compounded zero rates
+ * (Prices) at whole-day maturities (TimeSteps), ascending days. */
+typedef struct hwt_yield {
+    int32_t n;
+    const double *rate;
+    const int32_t *day;
+} hwt_yield;
+
+/* Tuning knobs; zero fields take the context's (tuned or default) values.
+ * block_size plays the part of the reference's -b flag (common/Args.hpp:43). */
+typedef struct hwt_config {
+    int32_t mode;          /* HWT_* mode */
+    int32_t block_size;    /* threads that price one wide tree, multiple of 32 in 32..512; raised
+                              to width/8 for wider trees (8 nodes per thread at most) */
+    int32_t sort;          /* HWT_SORT_*, accepted and ignored */
+    int32_t big_threshold; /* widths above this get a whole block (<= 256) */
+    int32_t use_graph;     /* 1 = replay a captured CUDA graph (default), 0 = direct launches */
+    int32_t record_busy;   /* 1 = record per-block busy time for the tail-imbalance stat */
+} hwt_config;
+
+/* Run statistics, filled when a non-NULL pointer is passed.  Times are CUDA-event
+ * times on the context's stream. */
+typedef struct hwt_stats {
+    double total_ms;        /* whole call on the stream: copies + sizing + pricing */
+    double pricing_ms;      /* pricing kernel only */
+    double sizing_ms;       /* sizing / validation / binning kernels */
+    int64_t nodes;          /* active tree nodes of one pass, summed over options */
+    int64_t h2d_bytes;      /* bytes copied host -> device by this call */
+    int64_t d2h_bytes;      /* bytes copied device -> host by this call */
+    int64_t device_bytes;   /* device memory held by the context */
+    int32_t kernel_launches;/* kernels of this library launched by this call */
+    int32_t n_block_trees;  /* trees priced by a whole block */
+    int32_t n_warp_tasks;   /* warp tasks (groups of small trees) */
+    int32_t grid;           /* pricing blocks launched */
+    int32_t block_size;     /* threads per pricing block (512) */
+    int32_t max_width;      /* widest tree in the batch */
+    int32_t max_height;     /* tallest tree in the batch */
+    int32_t graph_replayed; /* 1 if the kernels ran from a captured graph */
+    double busy_max_ms;     /* per-block busy time: max (record_busy only) */
+    double busy_mean_ms;    /* per-block busy time: mean (record_busy only) */
+} hwt_stats;
+
+typedef struct hwt_ctx hwt_ctx;
+
+/* Library ABI version (HWT_ABI_VERSION). */
+int hwt_abi_version(void);
+
+/* Creates a context on CUDA device `device`: stream, events, and buffers that
+ * grow with the largest batch seen.  tune_cache: path of the autotuner's cache
+ * file (read now, written by hwt_autotune), or NULL.  Returns NULL on failure;
+ * hwt_create_status() then says why.  Replaces the reference's per-call Thrust
+ * allocations (cuda/CudaDomain.cuh:114-130) and cudaSetDevice
+ * (cuda-option/CudaOptionMain.cu:104-105). */
+hwt_ctx *hwt_create(int device, const char *tune_cache);
+int hwt_create_status(void);
+void hwt_destroy(hwt_ctx *ctx);
+const char *hwt_last_error(const hwt_ctx *ctx);
+
+/* Prices n options held in HOST memory; out_prices (n doubles, host) receives
+ * the prices in input order.  Replaces seq::computeOptions (seq/Seq.hpp:181)
+ * and KernelRunBase::run (cuda-option/Kernel.cuh:303-314,
+ * cuda-multi/Kernel.cuh:375-404).  n == 0 is a no-op.  A rejected option makes
+ * the call return HWT_EINVAL; its price is NaN and the message names the first
+ * rejected index. */
+int hwt_price(hwt_ctx *ctx, const hwt_options *opts, const hwt_yield *yield, int mode,
+              double *out_prices, hwt_stats *stats);
+
+/* As hwt_price with explicit configuration (the reference's blockSize and
+ * SortType arguments, cuda-option/Kernel.cuh:303-305). */
+int hwt_price_ex(hwt_ctx *ctx, const hwt_options *opts, const hwt_yield *yield,
+                 const hwt_config *cfg, double *out_prices, hwt_stats *stats);
+
+/* Prices options whose arrays are already in DEVICE memory of the context's
+ * device; out_prices is a device pointer.  The yield curve is host memory.
+ * Runs on the context's stream and waits for it, so device inputs may be reused
+ * on return.  No host<->device copies of option data. */
+int hwt_price_device(hwt_ctx *ctx, const hwt_options *dev_opts, const hwt_yield *yield,
+                     const hwt_config *cfg, double *dev_out_prices, hwt_stats *stats);
+
+/* Tree shape of each option as the reference computes it
+ * (common/OptionConstants.hpp:29-53, seq/Seq.hpp:125), on the host, no GPU:
+ * jmax, height n, width 2*jmax+1 and maturity step (int)(t/dt).  Any output
+ * pointer may be NULL.  Returns HWT_EINVAL if an option is invalid (its entries
+ * are then -1). */
+int hwt_shape(const hwt_options *opts, int32_t *jmax, int32_t *height, int32_t *width,
+              int32_t *maturity_step);
+
+/* Active nodes of one pass of one option's tree, sum_{i<n} (2 min(i,jmax) + 1):
+ * the work unit of the roofline accounting. */
+int64_t hwt_active_nodes(int32_t height, int32_t jmax);
+
+/* Autotuner: prices the batch with each candidate configuration (block size,
+ * block-tree threshold), keeps the fastest for `mode` in the context, writes it
+ * to the context's tune cache (if any) and returns it in *best. */
+int hwt_autotune(hwt_ctx *ctx, const hwt_options *opts, const hwt_yield *yield, int mode,
+                 int repeats, hwt_config *best);
+
+/* Current default configuration of the context for `mode`. */
+int hwt_get_config(const hwt_ctx *ctx, int mode, hwt_config *cfg);
+
+/* Measured FP64 and FP32 fused-multiply-add peaks of the context's GPU in
+ * TFLOP/s (2 flops per FMA), from dependent-chain microbenchmarks timed with
+ * CUDA events.  The roofline denominators of the tree kernels. */
+int hwt_measure_peaks(hwt_ctx *ctx, double *fp64_tflops, double *fp32_tflops);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HWTREE_H */

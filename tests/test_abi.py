@@ -1,0 +1,60 @@
+"""The C-ABI library loads, exports every entry point include/hwtree.h declares,
+and its host-only functions behave (no GPU compute here)."""
+import os
+import re
+
+import numpy as np
+
+from conftest import ROOT, REF_SETS, SYN_SETS, load_set
+
+HEADER = os.path.join(ROOT, "include", "hwtree.h")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(hwt_[a-z_0-9]+)\s*\(", text)))
+
+
+def test_every_declared_symbol_is_exported(pkg):
+    lib = pkg.lib()
+    names = declared_functions()
+    assert len(names) >= 10
+    for n in names:
+        assert hasattr(lib, n), n
+
+
+def test_python_binding_covers_header(pkg):
+    assert set(declared_functions()) == set(pkg._SIGNATURES)
+
+
+def test_abi_version(pkg):
+    assert pkg.lib().hwt_abi_version() == 1
+
+
+def test_active_nodes_formula(pkg):
+    for n, j in ((0, 5), (1, 5), (5, 5), (6, 5), (7, 5), (120, 23), (2880, 1767), (10, 100)):
+        brute = sum(2 * min(i, j) + 1 for i in range(n))
+        assert pkg.lib().hwt_active_nodes(n, j) == brute
+        assert pkg.active_nodes(n, j) == brute
+
+
+def test_shape_of_uniform_book(pkg):
+    opts, _, _, _ = load_set(pkg, "uniform_1k")
+    s = pkg.shape(opts)
+    assert s["status"] == 0
+    assert np.all(s["jmax"] == 23) and np.all(s["width"] == 47) and np.all(s["height"] == 120)
+    assert np.all(s["maturity_step"] == 60)
+
+
+def test_shape_rejects_bad_records(pkg):
+    opts, _, _, _ = load_set(pkg, "book")
+    opts.ReversionRates[2] = 0.0
+    opts.TermStepCounts[3] = 0
+    s = pkg.shape(opts)
+    assert s["status"] == pkg.HWT_EINVAL
+    assert s["jmax"][2] == -1 and s["jmax"][3] == -1 and s["jmax"][0] > 0
+
+
+def test_null_context_is_einval(pkg):
+    assert pkg.lib().hwt_price(None, None, None, 1, None, None) == pkg.HWT_EINVAL
