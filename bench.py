@@ -249,7 +249,7 @@ def run_ours(args, rank, world, local):
 
     # per-mode survey (prices + errors + device time), untimed by the contract
     modes = {}
-    for m in (pkg.BATCHED_MIXED, pkg.BATCHED_FP32, pkg.BATCHED_FP64, pkg.PLAIN_FP64):
+    for m in (() if args.skip_survey else (pkg.BATCHED_MIXED, pkg.BATCHED_FP32, pkg.BATCHED_FP64, pkg.PLAIN_FP64)):
         name = pkg.MODE_NAMES[m]
         k = args.steps if m != pkg.PLAIN_FP64 else max(1, min(args.steps, 3))
         t, _, st = device_steps(m, k, 1)
@@ -261,11 +261,12 @@ def run_ours(args, rank, world, local):
             entry.update({"max_abs_err": float(np.max(err)), "p99_abs_err": float(np.percentile(err, 99)),
                           "max_rel_err": float(np.max(err / np.maximum(np.abs(ref_prices), 1e-300)))})
         modes[name] = entry
-    fp64_rate = modes["batched_fp64"]["options_per_s"]
-    plain_rate = modes["plain_fp64"]["options_per_s"]
-    for e in modes.values():
-        e["x_batched_fp64"] = e["options_per_s"] / fp64_rate
-        e["x_plain_fp64"] = e["options_per_s"] / plain_rate
+    if modes:
+        fp64_rate = modes["batched_fp64"]["options_per_s"]
+        plain_rate = modes["plain_fp64"]["options_per_s"]
+        for e in modes.values():
+            e["x_batched_fp64"] = e["options_per_s"] / fp64_rate
+            e["x_plain_fp64"] = e["options_per_s"] / plain_rate
 
     # ---- timed region: K device-resident steps of the headline mode
     if dist is not None:
@@ -350,6 +351,7 @@ def main():
     ap.add_argument("--ref-sample", type=int, default=6000)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--tune", action="store_true")
+    ap.add_argument("--skip-survey", action="store_true", help="time only the headline mode (profiling runs)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_env()

@@ -25,7 +25,7 @@ using namespace hwt;
 namespace {
 
 constexpr int kMaxYield = 4096;
-constexpr int kDefaultBlock = 256;
+constexpr int kDefaultBlock = 128;
 constexpr int kDefaultBig = 256;
 
 thread_local int g_create_status = HWT_OK;
@@ -299,7 +299,7 @@ int run_batch(hwt_ctx *c, const DevOptions &dopt, double *dev_out, const hwt_con
     p.s.bin_start = c->d_bin_start; p.s.task_start = c->d_task_start;
     p.s.status = c->d_status;
     p.out = dev_out;
-    p.block_threads = cfg.block_size;
+    p.group_threads = cfg.block_size;
     p.big_threshold = std::min(cfg.big_threshold, kMaxWarpWidth);
     p.max_width = kMaxTreeWidth;
     p.record_busy = cfg.record_busy ? 1 : 0;
@@ -365,7 +365,7 @@ int finish(hwt_ctx *c, const hwt_config &cfg, hwt_stats *stats, int launches, in
         stats->d2h_bytes = d2h;
         stats->device_bytes = c->device_bytes;
         stats->kernel_launches = launches;
-        stats->n_block_trees = st.n_big;
+        stats->n_block_trees = st.n_cta + st.n_group;
         stats->n_warp_tasks = st.n_warp_tasks;
         stats->block_size = cfg.mode == HWT_PLAIN_FP64 ? 128 : kPricingThreads;
         stats->grid = grid_hint;
@@ -457,7 +457,7 @@ hwt_ctx *hwt_create(int device, const char *tune_cache)
             int mode = -1, block = 0, big = 0;
             if (!std::getline(ls, name, '|')) continue;
             if (!(ls >> mode >> block >> big)) continue;
-            if (name == c->gpu_name && mode >= 0 && mode < 4 && block >= 32 && block <= 512 && block % 32 == 0 &&
+            if (name == c->gpu_name && mode >= 0 && mode < 4 && (block == 64 || block == 128 || block == 256 || block == 512) &&
                 big >= 1 && big <= kMaxWarpWidth) {
                 c->tuned[mode].block_size = block;
                 c->tuned[mode].big_threshold = big;
@@ -506,8 +506,8 @@ int hwt_price_ex(hwt_ctx *c, const hwt_options *o, const hwt_yield *y, const hwt
     if (o->n == 0) return HWT_OK;
     if ((r = ensure_capacity(c, o->n))) return r;
     const hwt_config cfg = resolve(c, cfg_in, mode);
-    if (cfg.block_size < 32 || cfg.block_size > 512 || cfg.block_size % 32)
-        return fail(c, HWT_EINVAL, "block_size must be a multiple of 32 in [32, 512]");
+    if (cfg.block_size != 64 && cfg.block_size != 128 && cfg.block_size != 256 && cfg.block_size != 512)
+        return fail(c, HWT_EINVAL, "block_size must be 64, 128, 256 or 512");
 
     const int64_t n = o->n;
     const Packing pk = packing(c->cap);
@@ -583,8 +583,8 @@ int hwt_price_device(hwt_ctx *c, const hwt_options *o, const hwt_yield *y, const
     if (o->n == 0) return HWT_OK;
     if ((r = ensure_capacity(c, o->n))) return r;
     const hwt_config cfg = resolve(c, cfg_in, mode);
-    if (cfg.block_size < 32 || cfg.block_size > 512 || cfg.block_size % 32)
-        return fail(c, HWT_EINVAL, "block_size must be a multiple of 32 in [32, 512]");
+    if (cfg.block_size != 64 && cfg.block_size != 128 && cfg.block_size != 256 && cfg.block_size != 512)
+        return fail(c, HWT_EINVAL, "block_size must be 64, 128, 256 or 512");
     DevOptions dopt;
     dopt.n = o->n;
     dopt.strike = o->strike; dopt.bond_maturity = o->bond_maturity; dopt.option_maturity = o->option_maturity;
@@ -636,8 +636,8 @@ int hwt_autotune(hwt_ctx *c, const hwt_options *o, const hwt_yield *y, int mode,
     if (r) return r;
     if (o->n == 0) return fail(c, HWT_EINVAL, "autotune needs a non-empty batch");
     std::vector<double> out(o->n);
-    const int blocks[] = {128, 256, 384, 512};
-    const int bigs[] = {96, 128, 192, 256};
+    const int blocks[] = {64, 128, 256, 512};
+    const int bigs[] = {64, 128, 192, 256};
     double best_ms = 1e300;
     hwt_config best_cfg = c->tuned[mode];
     for (int b : blocks) {

@@ -60,20 +60,29 @@ struct ModeMix {
 
 __device__ __forceinline__ int cls_K(int cls) { return cls / kNumL + 1; }
 
-// Barrier 1 over the first `nthreads` threads of the block (a block tree may use
-// only part of the block; the other warps wait at barrier 0 meanwhile).
-__device__ __forceinline__ void tree_barrier(int nthreads)
+// Named barrier `id` over the `nthreads` threads of one tree's warp group (id 0
+// with the whole block is __syncthreads).
+__device__ __forceinline__ void tree_barrier(int id, int nthreads)
 {
-    asm volatile("bar.sync 1, %0;" ::"r"(nthreads) : "memory");
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
 }
+
+// Warps that price one tree together: `nthreads` threads from `base`, synchronised
+// by named barrier `bar`.
+struct Group {
+    int base, nthreads, bar;
+};
 __device__ __forceinline__ int cls_L(int cls) { return 1 << (cls % kNumL); }
 
-// Smallest L*K >= width with K in 1..8, L in {1..32}; ties go to the larger K
-// (more trees per warp, fewer shuffles per node).
+// Smallest L*K >= width with K in {1,2,3,4,6,8}, L in {1..32}; ties go to the
+// larger K (more trees per warp, fewer shuffles per node).  K = 5 and 7 are left
+// out to keep the kernel's code (and its instruction-cache footprint) small.
 __host__ __device__ int pick_warp_class(int width)
 {
+    const int ks[6] = {8, 6, 4, 3, 2, 1};
     int best = -1, best_slots = 1 << 30;
-    for (int K = 8; K >= 1; --K) {
+    for (int q = 0; q < 6; ++q) {
+        const int K = ks[q];
         for (int l = 0; l < kNumL; ++l) {
             const int slots = K << l;
             if (slots >= width && slots < best_slots) {
@@ -124,10 +133,10 @@ __global__ void size_kernel(EngineParams p)
             t.term_unit = p.opt.term_unit[i]; t.type = ty; t.edges = (int8_t)s.edges;
             p.s.trees[i] = t;
             nodes = (unsigned long long)s.nodes;
-            const bool warp = s.width <= p.big_threshold;
-            const int cls = warp ? pick_warp_class(s.width) : 0;
+            const int tier = s.width <= p.big_threshold ? 2 : (s.width <= kMaxBlockK * p.group_threads ? 1 : 0);
+            const int cls = tier == 2 ? pick_warp_class(s.width) : 0;
             const unsigned long long work = (unsigned long long)s.nodes + (unsigned long long)s.width;
-            key = ((warp ? 1 : 0) * kWorkBuckets + work_bucket(work)) * 64 + cls;
+            key = (tier * kWorkBuckets + work_bucket(work)) * 64 + cls;
             p.s.keys[i] = key;
             atomicMax(&p.s.status->max_width, s.width);
             atomicMax(&p.s.status->max_height, s.n);
@@ -146,6 +155,7 @@ __global__ void scan_kernel(EngineParams p)
 {
     constexpr int T = 1024;
     constexpr int PER = kKeyBins / T;
+    static_assert(PER * T == kKeyBins, "bins must split evenly over the scan threads");
     __shared__ int s_a[T], s_b[T];
     const int tid = threadIdx.x;
     int cnt[PER], tsk[PER];
@@ -153,7 +163,7 @@ __global__ void scan_kernel(EngineParams p)
     for (int q = 0; q < PER; ++q) {
         const int b = tid * PER + q;
         const int c = p.s.hist[b];
-        const bool warp = b >= kWorkBuckets * 64;
+        const bool warp = b >= 2 * kTierBins;
         int t = 0;
         if (warp && c > 0) {
             const int G = 32 / cls_L(b & 63);
@@ -178,8 +188,14 @@ __global__ void scan_kernel(EngineParams p)
         ea += cnt[q]; eb += tsk[q];
     }
     if (tid == T - 1) p.s.status->n_warp_tasks = s_b[T - 1];
-    // block trees are the bins below the first warp bin
-    if (tid == (kWorkBuckets * 64) / PER) p.s.status->n_big = s_a[tid] - sa;
+    // tier boundaries: options before the first tier-1 and tier-2 bins (global
+    // writes of the block are visible to it after the barrier)
+    __syncthreads();
+    if (tid == 0) {
+        const int t1 = p.s.bin_start[kTierBins], t2 = p.s.bin_start[2 * kTierBins];
+        p.s.status->n_cta = t1;
+        p.s.status->n_group = t2 - t1;
+    }
 }
 
 // Places every valid option at its sorted position and emits one warp task per
@@ -193,7 +209,7 @@ __global__ void scatter_kernel(EngineParams p)
     const int q = atomicAdd(&p.s.fill[key], 1);
     const int pos = p.s.bin_start[key] + q;
     p.s.order[pos] = i;
-    if (key >= kWorkBuckets * 64) {
+    if (key >= 2 * kTierBins) {
         const int cls = key & 63;
         const int G = 32 / cls_L(cls);
         if (q % G == 0) {
@@ -469,22 +485,25 @@ __device__ __forceinline__ void fill_ext(Ext<R, K> &x, const R (&r)[K])
     for (int s = 0; s < K; ++s) x.e[s + 2] = r[s];
 }
 
-// Neighbour values within a warp segment of L lanes holding one tree.
+// Neighbour values within a warp segment of L lanes holding one tree.  The
+// shuffles use width L, so a lane never reads another tree: at the segment ends
+// it gets its own values back, which only ever meet a zero coefficient (the
+// tree's outer nodes branch nowhere outward) or feed nodes outside the active
+// cone.
 template <typename R, int K>
-__device__ __forceinline__ void exchange_warp(Ext<R, K> &x, const R (&r)[K], int lis, int L)
+__device__ __forceinline__ void exchange_warp(Ext<R, K> &x, const R (&r)[K], int L)
 {
     fill_ext(x, r);
     if constexpr (K >= 2) {
-        const R a = __shfl_up_sync(FULL, r[K - 1], 1), b = __shfl_up_sync(FULL, r[K - 2], 1);
-        const R c = __shfl_down_sync(FULL, r[0], 1), d = __shfl_down_sync(FULL, r[1], 1);
-        const bool hl = lis > 0, hr = lis + 1 < L;
-        x.e[1] = hl ? a : (R)0; x.e[0] = hl ? b : (R)0;
-        x.e[K + 2] = hr ? c : (R)0; x.e[K + 3] = hr ? d : (R)0;
+        x.e[1] = __shfl_up_sync(FULL, r[K - 1], 1, L);
+        x.e[0] = __shfl_up_sync(FULL, r[K - 2], 1, L);
+        x.e[K + 2] = __shfl_down_sync(FULL, r[0], 1, L);
+        x.e[K + 3] = __shfl_down_sync(FULL, r[1], 1, L);
     } else {
-        const R a = __shfl_up_sync(FULL, r[0], 1), b = __shfl_up_sync(FULL, r[0], 2);
-        const R c = __shfl_down_sync(FULL, r[0], 1), d = __shfl_down_sync(FULL, r[0], 2);
-        x.e[1] = lis >= 1 ? a : (R)0; x.e[0] = lis >= 2 ? b : (R)0;
-        x.e[3] = lis + 1 < L ? c : (R)0; x.e[4] = lis + 2 < L ? d : (R)0;
+        x.e[1] = __shfl_up_sync(FULL, r[0], 1, L);
+        x.e[0] = __shfl_up_sync(FULL, r[0], 2, L);
+        x.e[3] = __shfl_down_sync(FULL, r[0], 1, L);
+        x.e[4] = __shfl_down_sync(FULL, r[0], 2, L);
     }
 }
 
@@ -492,9 +511,12 @@ __device__ __forceinline__ void exchange_warp(Ext<R, K> &x, const R (&r)[K], int
 // last two nodes of every warp through shared memory (double buffered, so one
 // barrier per step is enough).
 template <typename R, int K>
-__device__ __forceinline__ void exchange_block(Ext<R, K> &x, const R (&r)[K], R *sh, int parity, int nthreads)
+__device__ __forceinline__ void exchange_block(Ext<R, K> &x, const R (&r)[K], R *sh, int parity, const Group &gr)
 {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = nthreads >> 5;
+    // shared slots are indexed by the warp's index in the block; neighbours are
+    // the adjacent warps of the same group
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int w0 = gr.base >> 5, w1 = w0 + (gr.nthreads >> 5);
     R *buf = sh + parity * (32 * 4);
     if constexpr (K >= 2) {
         if (lane == 0) { buf[warp * 4 + 0] = r[0]; buf[warp * 4 + 1] = r[1]; }
@@ -503,9 +525,9 @@ __device__ __forceinline__ void exchange_block(Ext<R, K> &x, const R (&r)[K], R 
         if (lane < 2) buf[warp * 4 + lane] = r[0];
         if (lane >= 30) buf[warp * 4 + lane - 28] = r[0];
     }
-    tree_barrier(nthreads);
-    exchange_warp<R, K>(x, r, lane, 32);
-    const bool hasl = warp > 0, hasr = warp + 1 < nw;
+    tree_barrier(gr.bar, gr.nthreads);
+    exchange_warp<R, K>(x, r, 32);
+    const bool hasl = warp > w0, hasr = warp + 1 < w1;
     if constexpr (K >= 2) {
         if (lane == 0) {
             x.e[1] = hasl ? buf[(warp - 1) * 4 + 3] : (R)0;
@@ -570,6 +592,7 @@ __device__ void price_warp_task(const EngineParams &p, const WarpTask &task)
 {
     typedef typename Mode::Row R;
     typedef typename Mode::Scal S;
+    constexpr unsigned NONE = 0x7fffffffu;
     const int lane = threadIdx.x & 31;
     const int L = cls_L(task.cls);
     const int g = lane / L, lis = lane & (L - 1);
@@ -586,56 +609,62 @@ __device__ void price_warp_task(const EngineParams &p, const WarpTask &task)
     Slice<Mode, K> sl;
     Ext<R, K> x;
 
-    // ---- forward sweep: rows 1 .. n-1, sums of rows m-1 and n-1
+    // ---- forward sweep: rows 1 .. n-1; the sums of rows m-1 and n-1 are kept.
+    // Rows of trees that are done keep being updated (their segment is isolated by
+    // the width-L shuffles), so the step loop carries no per-tree predicates.
     sl.setup_forward(t, k0);
     const unsigned wlo = __reduce_or_sync(FULL, sl.mlo | sl.mlo2), whi = __reduce_or_sync(FULL, sl.mhi | sl.mhi2);
+    const int e_f = (int)__reduce_min_sync(FULL, (valid && t.edges) ? (unsigned)t.jmax : NONE);
+    const int rm = (t.m >= 2 && t.m < t.n) ? t.m - 1 : -1;  // row m-1 (row 0 sums to 1)
+    const int rn = (t.n >= 2) ? t.n - 1 : -1;               // row n-1
     S sum_m1 = (S)1, sum_n1 = (S)1;
-    const int fsteps = __reduce_max_sync(FULL, (unsigned)(t.n > 1 ? t.n - 1 : 0));
-    for (int i = 0; i < fsteps; ++i) {
-        exchange_warp<R, K>(x, sl.r, lis, L);
-        const bool live = t.edges && i >= t.jmax;
-        const bool any_live = __any_sync(FULL, live);
-        R keep[K];
-#pragma unroll
-        for (int s = 0; s < K; ++s) keep[s] = sl.r[s];
-        sl.forward_step(x, any_live, live ? wlo : 0u, live ? whi : 0u);
-        const bool run = i < t.n - 1;
-        if (!run) {
-#pragma unroll
-            for (int s = 0; s < K; ++s) sl.r[s] = keep[s];
+    const int fsteps = (int)__reduce_max_sync(FULL, (unsigned)(t.n > 1 ? t.n - 1 : 0));
+    int i = 0;
+    while (i < fsteps) {
+        unsigned mine = NONE;
+        if (rm > i) mine = (unsigned)rm;
+        if (rn > i && (unsigned)rn < mine) mine = (unsigned)rn;
+        const int ev = (int)__reduce_min_sync(FULL, mine);  // next row whose sum someone needs
+        const int stop = ev < fsteps ? ev : fsteps;          // steps i .. stop-1 produce rows .. stop
+        for (; i < stop; ++i) {
+            exchange_warp<R, K>(x, sl.r, L);
+            sl.forward_step(x, i >= e_f, wlo, whi);
         }
-        const int row = i + 1;
-        const bool need = run && (row == t.m - 1 || row == t.n - 1);
-        if (__any_sync(FULL, need)) {
+        if (ev <= fsteps) {
             S acc = sl.partial_sum(k0, W);
             for (int off = 1; off < L; off <<= 1) acc += __shfl_xor_sync(FULL, acc, off);
-            if (need) {
-                if (row == t.m - 1) sum_m1 = acc;
-                if (row == t.n - 1) sum_n1 = acc;
-            }
+            if (rm == ev) sum_m1 = acc;
+            if (rn == ev) sum_n1 = acc;
         }
     }
     const Scales<S> sc = tree_scales<S>(t, sum_m1, sum_n1, p.yc);
 
-    // ---- backward sweep
+    // ---- backward sweep from each tree's own height; rows of trees that have not
+    // started yet are put back to the face value after every step.
     sl.setup_backward(t, k0);
     const unsigned blo = __reduce_or_sync(FULL, sl.mlo), bhi = __reduce_or_sync(FULL, sl.mhi);
+    const int e_b = (int)__reduce_min_sync(FULL, (valid && t.edges) ? (unsigned)t.jmax : NONE);
+    const int bsteps = (int)__reduce_max_sync(FULL, (unsigned)(t.n > 0 ? t.n : 0));
+    const int n_min = (int)__reduce_min_sync(FULL, valid ? (unsigned)t.n : (unsigned)bsteps);
+    const R face = Mode::kFlux ? (R)0 : (R)100;
     R base = Mode::kFlux ? (R)100 : (R)0;
-    const int bsteps = __reduce_max_sync(FULL, (unsigned)(t.n > 0 ? t.n : 0));
-    for (int i = bsteps - 1; i >= 0; --i) {
-        exchange_warp<R, K>(x, sl.r, lis, L);
-        const bool live = t.edges && i >= t.jmax;
-        const bool any_live = __any_sync(FULL, live);
-        R keep[K];
+    const bool pays = valid && pays_at(t);
+    i = bsteps - 1;
+    while (i >= 0) {
+        // next maturity step at or below i (one per tree), -1 if none left
+        const int pm = (int)__reduce_max_sync(FULL, (pays && t.m <= i) ? (unsigned)(t.m + 1) : 0u) - 1;
+        const int lo = pm > 0 ? pm : 0;
+        for (; i >= lo; --i) {
+            exchange_warp<R, K>(x, sl.r, L);
+            sl.backward_step(x, i >= e_b, blo, bhi, base);
+            if (i >= n_min && i >= t.n) {
 #pragma unroll
-        for (int s = 0; s < K; ++s) keep[s] = sl.r[s];
-        sl.backward_step(x, any_live, live ? blo : 0u, live ? bhi : 0u, base);
-        if (i >= t.n) {
-#pragma unroll
-            for (int s = 0; s < K; ++s) sl.r[s] = keep[s];
-        } else if (i == t.m) {
-            sl.payoff(sc.kappa, base, t.X, t.type);
-            base = (R)0;
+                for (int s = 0; s < K; ++s) sl.r[s] = (k0 + s < W) ? face : (R)0;
+            }
+            if (i == pm && pays && t.m == i) {
+                sl.payoff(sc.kappa, base, t.X, t.type);
+                base = (R)0;
+            }
         }
     }
 
@@ -655,12 +684,13 @@ __device__ void price_warp_task(const EngineParams &p, const WarpTask &task)
 // Wide trees: one whole block per tree, K nodes per thread.
 // ---------------------------------------------------------------------------
 template <class Mode, int K>
-__device__ void price_block_tree(const EngineParams &p, const Tree &t, int nthreads, typename Mode::Row *sh_x,
+__device__ void price_block_tree(const EngineParams &p, const Tree &t, const Group &gr, typename Mode::Row *sh_x,
                                  typename Mode::Scal *sh_red)
 {
     typedef typename Mode::Row R;
     typedef typename Mode::Scal S;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = nthreads >> 5;
+    const int tid = threadIdx.x - gr.base, lane = tid & 31, warp = tid >> 5, nw = gr.nthreads >> 5;
+    const int aw0 = gr.base >> 5;  // first warp of the group in the block
     const int k0 = tid * K;
     const int W = t.width, jc = t.jc;
     const int wk0 = warp * 32 * K, wk1 = wk0 + 32 * K;  // this warp's node range
@@ -673,7 +703,7 @@ __device__ void price_block_tree(const EngineParams &p, const Tree &t, int nthre
     S sum_m1 = (S)1, sum_n1 = (S)1;
     const int fsteps = t.n > 1 ? t.n - 1 : 0;
     for (int i = 0; i < fsteps; ++i) {
-        exchange_block<R, K>(x, sl.r, sh_x, parity, nthreads);
+        exchange_block<R, K>(x, sl.r, sh_x, parity, gr);
         parity ^= 1;
         // rows outside the cone of row i+1 stay zero: skip whole warps there
         const int reach = (i + 1 < jc) ? i + 1 : jc;
@@ -683,11 +713,11 @@ __device__ void price_block_tree(const EngineParams &p, const Tree &t, int nthre
         if (row == t.m - 1 || row == t.n - 1) {
             S acc = sl.partial_sum(k0, W);
             for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(FULL, acc, off);
-            if (lane == 0) sh_red[warp] = acc;
-            tree_barrier(nthreads);
+            if (lane == 0) sh_red[aw0 + warp] = acc;
+            tree_barrier(gr.bar, gr.nthreads);
             S tot = (S)0;
-            for (int w = 0; w < nw; ++w) tot += sh_red[w];
-            tree_barrier(nthreads);
+            for (int w = 0; w < nw; ++w) tot += sh_red[aw0 + w];
+            tree_barrier(gr.bar, gr.nthreads);
             if (row == t.m - 1) sum_m1 = tot;
             if (row == t.n - 1) sum_n1 = tot;
         }
@@ -698,7 +728,7 @@ __device__ void price_block_tree(const EngineParams &p, const Tree &t, int nthre
     const unsigned blo = __reduce_or_sync(FULL, sl.mlo), bhi = __reduce_or_sync(FULL, sl.mhi);
     R base = Mode::kFlux ? (R)100 : (R)0;
     for (int i = t.n - 1; i >= 0; --i) {
-        exchange_block<R, K>(x, sl.r, sh_x, parity, nthreads);
+        exchange_block<R, K>(x, sl.r, sh_x, parity, gr);
         parity ^= 1;
         const int reach = (i < t.jmax) ? i : t.jmax;
         const bool active = wk1 > jc - reach && wk0 <= jc + reach && wk0 < W;
@@ -720,6 +750,19 @@ __device__ void price_block_tree(const EngineParams &p, const Tree &t, int nthre
     }
 }
 
+// K = nodes per thread for a tree on group `gr` (width <= 8 * gr.nthreads).
+template <class Mode>
+__device__ __forceinline__ void dispatch_block_tree(const EngineParams &p, const Tree &t, const Group &gr,
+                                                    typename Mode::Row *sh_x, typename Mode::Scal *sh_red)
+{
+    // K rounded up to 1, 2, 4 or 8 (warps left past the width skip their steps)
+    const int K = (t.width + gr.nthreads - 1) / gr.nthreads;
+    if (K <= 1) price_block_tree<Mode, 1>(p, t, gr, sh_x, sh_red);
+    else if (K <= 2) price_block_tree<Mode, 2>(p, t, gr, sh_x, sh_red);
+    else if (K <= 4) price_block_tree<Mode, 4>(p, t, gr, sh_x, sh_red);
+    else price_block_tree<Mode, 8>(p, t, gr, sh_x, sh_red);
+}
+
 template <class Mode>
 __global__ void __launch_bounds__(kPricingThreads, 1) price_kernel(EngineParams p)
 {
@@ -727,38 +770,40 @@ __global__ void __launch_bounds__(kPricingThreads, 1) price_kernel(EngineParams 
     typedef typename Mode::Scal S;
     __shared__ R sh_x[2 * 32 * 4];
     __shared__ S sh_red[32];
-    __shared__ int sh_task;
+    __shared__ int sh_task[1 + 16];
     unsigned long long t_start = 0;
     if (p.record_busy && threadIdx.x == 0) asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t_start));
 
-    // Phase 1: wide trees, one per block, heaviest first.
-    const int n_big = p.s.status->n_big;
+    // Tier 0: trees wider than a group holds, one per block, heaviest first.
+    const int n_cta = p.s.status->n_cta;
     for (;;) {
-        if (threadIdx.x == 0) sh_task = atomicAdd(&p.s.status->big_counter, 1);
+        if (threadIdx.x == 0) sh_task[0] = atomicAdd(&p.s.status->cta_counter, 1);
         __syncthreads();
-        const int tsk = sh_task;
+        const int tsk = sh_task[0];
         __syncthreads();
-        if (tsk >= n_big) break;
+        if (tsk >= n_cta) break;
         const Tree t = p.s.trees[p.s.order[tsk]];
-        // threads for this tree: the configured count, at least width/8, at most the block
-        int nt = p.block_threads;
-        const int need = ((t.width + kMaxBlockK - 1) / kMaxBlockK + 31) & ~31;
-        if (nt < need) nt = need;
-        if (nt > (int)blockDim.x) nt = (int)blockDim.x;
-        const int K = (t.width + nt - 1) / nt;
-        if ((int)threadIdx.x < nt) {
-            switch (K) {
-                case 1: price_block_tree<Mode, 1>(p, t, nt, sh_x, sh_red); break;
-                case 2: price_block_tree<Mode, 2>(p, t, nt, sh_x, sh_red); break;
-                case 3: price_block_tree<Mode, 3>(p, t, nt, sh_x, sh_red); break;
-                case 4: price_block_tree<Mode, 4>(p, t, nt, sh_x, sh_red); break;
-                case 5: price_block_tree<Mode, 5>(p, t, nt, sh_x, sh_red); break;
-                case 6: price_block_tree<Mode, 6>(p, t, nt, sh_x, sh_red); break;
-                case 7: price_block_tree<Mode, 7>(p, t, nt, sh_x, sh_red); break;
-                default: price_block_tree<Mode, 8>(p, t, nt, sh_x, sh_red); break;
-            }
-        }
+        const Group gr{0, (int)blockDim.x, 0};
+        dispatch_block_tree<Mode>(p, t, gr, sh_x, sh_red);
         __syncthreads();  // shared buffers are reused by the next tree
+    }
+
+    // Tier 1: each group of group_threads threads prices its own trees.
+    {
+        const int n_group = p.s.status->n_group;
+        const int gsize = p.group_threads;
+        const int g = (int)threadIdx.x / gsize;
+        const Group gr{g * gsize, gsize, 1 + g};
+        for (;;) {
+            if ((int)threadIdx.x == gr.base) sh_task[1 + g] = atomicAdd(&p.s.status->group_counter, 1);
+            tree_barrier(gr.bar, gr.nthreads);
+            const int tsk = sh_task[1 + g];
+            tree_barrier(gr.bar, gr.nthreads);
+            if (tsk >= n_group) break;
+            const Tree t = p.s.trees[p.s.order[n_cta + tsk]];
+            dispatch_block_tree<Mode>(p, t, gr, sh_x, sh_red);
+            tree_barrier(gr.bar, gr.nthreads);
+        }
     }
 
     // Phase 2: warp tasks, each warp on its own.
@@ -775,9 +820,7 @@ __global__ void __launch_bounds__(kPricingThreads, 1) price_kernel(EngineParams 
             case 2: price_warp_task<Mode, 2>(p, wt); break;
             case 3: price_warp_task<Mode, 3>(p, wt); break;
             case 4: price_warp_task<Mode, 4>(p, wt); break;
-            case 5: price_warp_task<Mode, 5>(p, wt); break;
             case 6: price_warp_task<Mode, 6>(p, wt); break;
-            case 7: price_warp_task<Mode, 7>(p, wt); break;
             default: price_warp_task<Mode, 8>(p, wt); break;
         }
     }

@@ -61,22 +61,27 @@ constexpr int kMaxBlockK = 8;                  // nodes per thread for block tre
 constexpr int kPricingThreads = 512;           // threads of every pricing block
 constexpr int kMaxTreeWidth = kMaxBlockK * kPricingThreads;  // widest tree accepted
 
-// Sort keys: small trees after big ones; both by descending work.
+// Sort keys: [tier][work bucket][warp class].  Tier 0: trees wider than a group
+// can hold, priced by the whole block; tier 1: priced by a group of warps;
+// tier 2: small trees packed into warp tasks.  Descending work inside each tier.
 constexpr int kWorkBuckets = 128;
-constexpr int kKeyBins = 2 * kWorkBuckets * 64; // [is_warp][bucket][class]
+constexpr int kTiers = 3;
+constexpr int kKeyBins = kTiers * kWorkBuckets * 64;
+constexpr int kTierBins = kWorkBuckets * 64;
 
 // Per-run status written by the device (read back after each run).
 struct RunStatus {
     unsigned long long first_bad; // (index << 32) | reason of the lowest rejected option; all ones if none
     unsigned long long nodes;     // active nodes of one pass, summed over valid options
     int32_t bad_count;            // options rejected by validation
-    int32_t n_big;                // trees priced by whole blocks
-    int32_t n_warp_tasks;         // warp tasks
-    int32_t big_counter;          // work-queue heads
+    int32_t n_cta;                // tier 0: trees priced by whole blocks
+    int32_t n_group;              // tier 1: trees priced by warp groups
+    int32_t n_warp_tasks;         // tier 2: warp tasks
+    int32_t cta_counter;          // work-queue heads
+    int32_t group_counter;
     int32_t warp_counter;
     int32_t max_width;            // widest / tallest valid tree
     int32_t max_height;
-    int32_t pad;
 };
 
 struct Scratch {
@@ -98,7 +103,7 @@ struct EngineParams {
     Scratch s;
     double *out;
     int32_t max_width;
-    int32_t block_threads;  // preferred threads for one block tree (raised to width/8)
+    int32_t group_threads;  // threads of the warp group that prices one tier-1 tree
     int32_t big_threshold;  // widths above this go to whole blocks
     int32_t record_busy;
 };
