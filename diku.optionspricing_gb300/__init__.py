@@ -119,6 +119,8 @@ _SIGNATURES = {
     "hwt_get_config": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(Config)]),
     "hwt_measure_peaks": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double),
                                          ctypes.POINTER(ctypes.c_double)]),
+    "hwt_price_device_noalloc": (ctypes.c_int, [ctypes.POINTER(_Options), ctypes.POINTER(_Yield), ctypes.c_int,
+                                                ctypes.c_void_p, ctypes.c_void_p]),
 }
 
 

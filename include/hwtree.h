@@ -151,6 +151,22 @@ int hwt_price_ex(hwt_ctx *ctx, const hwt_options *opts, const hwt_yield *yield,
 int hwt_price_device(hwt_ctx *ctx, const hwt_options *dev_opts, const hwt_yield *yield,
                      const hwt_config *cfg, double *dev_out_prices, hwt_stats *stats);
 
+/* Allocation-free variant of hwt_price_device, with no counterpart in the
+ * reference.  For callers that cannot call cudaMalloc (device memory owned by
+ * another allocator; latency-bound paths where cudaMalloc/cudaFree, which may
+ * synchronise the device, are not allowed): no context, no allocation of any
+ * kind; the scratch the pricing kernels need lives in a static device array of
+ * the library (about 3.2 MB on every GPU that loads it, until exit).
+ *   dev_opts, dev_yield, dev_out_prices: DEVICE pointers of the current device
+ *   mode: HWT_BATCHED_FP64, HWT_BATCHED_FP32 or HWT_BATCHED_MIXED
+ *   stream: cudaStream_t to run on (NULL: the default stream); the call waits for it
+ * At most 32768 options and 1024 curve nodes per call, else HWT_EINVAL.  The
+ * first call on a device looks up the array's device address (make it before
+ * any stream capture).  Calls share the array: calls that overlap on the GPU
+ * race.  Returns HWT_EINVAL if an option is invalid (its price is NaN). */
+int hwt_price_device_noalloc(const hwt_options *dev_opts, const hwt_yield *dev_yield, int mode,
+                             double *dev_out_prices, void *stream);
+
 /* Tree shape of each option as the reference computes it
  * (common/OptionConstants.hpp:29-53, seq/Seq.hpp:125), on the host, no GPU:
  * jmax, height n, width 2*jmax+1 and maturity step (int)(t/dt).  Any output
