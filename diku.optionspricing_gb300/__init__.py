@@ -454,4 +454,151 @@ class KernelRun:
         return out
 
 
+# ---------------------------------------------------------------------------
+# Learned surrogate (hwt_surrogate_*)
+# ---------------------------------------------------------------------------
+class Box(ctypes.Structure):
+    """hwt_box: the surrogate's training box."""
+    _fields_ = [("t_min", ctypes.c_double), ("t_max", ctypes.c_double), ("span_min", ctypes.c_double),
+                ("span_max", ctypes.c_double), ("moneyness_min", ctypes.c_double),
+                ("moneyness_max", ctypes.c_double), ("a_min", ctypes.c_double), ("a_max", ctypes.c_double),
+                ("sigma_min", ctypes.c_double), ("sigma_max", ctypes.c_double), ("steps_min", ctypes.c_int32),
+                ("steps_max", ctypes.c_int32), ("term_unit", ctypes.c_int32)]
+
+
+class TrainConfig(ctypes.Structure):
+    _fields_ = [("epochs", ctypes.c_int32), ("batch", ctypes.c_int32), ("lr", ctypes.c_double),
+                ("lr_min", ctypes.c_double), ("seed", ctypes.c_uint64)]
+
+
+class TrainStats(ctypes.Structure):
+    _fields_ = [("final_loss", ctypes.c_double), ("train_ms", ctypes.c_double), ("label_ms", ctypes.c_double),
+                ("steps", ctypes.c_int64), ("samples", ctypes.c_int64), ("samples_per_s", ctypes.c_double),
+                ("y_mean", ctypes.c_double), ("y_std", ctypes.c_double)]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+class SurrogateStats(ctypes.Structure):
+    _fields_ = [("n_in_box", ctypes.c_int64), ("n_routed", ctypes.c_int64), ("n_judged", ctypes.c_int64),
+                ("judge_max_abs", ctypes.c_double), ("judge_p99_abs", ctypes.c_double),
+                ("judge_mean_abs", ctypes.c_double), ("network_ms", ctypes.c_double), ("tree_ms", ctypes.c_double),
+                ("route_ms", ctypes.c_double), ("total_ms", ctypes.c_double)]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+_SIGNATURES.update({
+    "hwt_surrogate_create": (ctypes.c_void_p, [ctypes.c_void_p, ctypes.POINTER(Box), ctypes.c_uint64]),
+    "hwt_surrogate_destroy": (None, [ctypes.c_void_p]),
+    "hwt_surrogate_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
+    "hwt_surrogate_train": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(_Options), ctypes.POINTER(_Yield),
+                                           ctypes.POINTER(TrainConfig), ctypes.POINTER(TrainStats)]),
+    "hwt_surrogate_price": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(_Options), ctypes.POINTER(_Yield),
+                                           ctypes.c_double, ctypes.c_uint64, ctypes.c_int, ctypes.c_void_p,
+                                           ctypes.POINTER(SurrogateStats)]),
+    "hwt_surrogate_save": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p]),
+    "hwt_surrogate_load": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p]),
+    "hwt_surrogate_param_count": (ctypes.c_int64, [ctypes.c_void_p]),
+    "hwt_surrogate_params": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int]),
+    "hwt_surrogate_forward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
+    "hwt_surrogate_loss_grads": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                                ctypes.POINTER(ctypes.c_double), ctypes.c_void_p]),
+})
+
+SURROGATE_DIMS = (8, 256, 256, 256, 256, 1)  # first fan-in: 7 features + 1 zero pad row
+
+
+class Surrogate:
+    """MLP surrogate with the tree as fallback (outside the box) and judge."""
+
+    def __init__(self, pricer: Pricer, box: dict | None = None, seed: int = 1):
+        from .workloads import SURROGATE_BOX
+        b = dict(SURROGATE_BOX if box is None else box)
+        self.box = Box(**b)
+        self.pricer = pricer
+        self._s = lib().hwt_surrogate_create(pricer._ctx, ctypes.byref(self.box), seed)
+        if not self._s:
+            raise HwtError(HWT_ECUDA, "hwt_surrogate_create failed")
+        self.train_stats = TrainStats()
+        self.stats = SurrogateStats()
+
+    def close(self):
+        if getattr(self, "_s", None):
+            lib().hwt_surrogate_destroy(self._s)
+            self._s = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc != HWT_OK:
+            msg = lib().hwt_surrogate_last_error(self._s)
+            raise (InvalidInput if rc == HWT_EINVAL else HwtError)(rc, msg.decode() if msg else "")
+
+    def train(self, samples: Options, yield_: Yield, epochs: int = 1, batch: int = 8192, lr: float = 1e-3,
+              lr_min: float = 0.0, seed: int = 7) -> dict:
+        cfg = TrainConfig(epochs, batch, lr, lr_min, seed)
+        o, y = samples._c(), yield_._c()
+        self._check(lib().hwt_surrogate_train(self._s, ctypes.byref(o), ctypes.byref(y), ctypes.byref(cfg),
+                                              ctypes.byref(self.train_stats)))
+        return self.train_stats.as_dict()
+
+    def price(self, options: Options, yield_: Yield, judge_fraction: float = 0.01, seed: int = 11,
+              tree_mode: int = BATCHED_MIXED) -> np.ndarray:
+        out = np.empty(options.N, dtype=np.float64)
+        o, y = options._c(), yield_._c()
+        self._check(lib().hwt_surrogate_price(self._s, ctypes.byref(o), ctypes.byref(y), judge_fraction, seed,
+                                              tree_mode, out.ctypes.data, ctypes.byref(self.stats)))
+        return out
+
+    def save(self, path: str):
+        self._check(lib().hwt_surrogate_save(self._s, path.encode()))
+
+    def load(self, path: str):
+        self._check(lib().hwt_surrogate_load(self._s, path.encode()))
+
+    def params(self) -> list[tuple[np.ndarray, np.ndarray]]:
+        n = lib().hwt_surrogate_param_count(self._s)
+        flat = np.empty(n, dtype=np.float32)
+        self._check(lib().hwt_surrogate_params(self._s, flat.ctypes.data, n, 0))
+        out, off = [], 0
+        for fi, fo in zip(SURROGATE_DIMS[:-1], SURROGATE_DIMS[1:]):
+            W = flat[off:off + fi * fo].reshape(fi, fo).copy(); off += fi * fo
+            b = flat[off:off + fo].copy(); off += fo
+            out.append((W, b))
+        return out
+
+    def set_params(self, params):
+        flat = np.concatenate([np.concatenate([np.asarray(W, np.float32).ravel(), np.asarray(b, np.float32)])
+                               for W, b in params]).astype(np.float32)
+        self._check(lib().hwt_surrogate_params(self._s, flat.ctypes.data, len(flat), 1))
+
+    def forward(self, x: np.ndarray) -> np.ndarray:
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        out = np.empty(len(x), dtype=np.float32)
+        self._check(lib().hwt_surrogate_forward(self._s, x.ctypes.data, len(x), out.ctypes.data))
+        return out
+
+    def loss_grads(self, x: np.ndarray, y: np.ndarray):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        y = np.ascontiguousarray(y, dtype=np.float32)
+        n = lib().hwt_surrogate_param_count(self._s)
+        g = np.empty(n, dtype=np.float32)
+        loss = ctypes.c_double()
+        self._check(lib().hwt_surrogate_loss_grads(self._s, x.ctypes.data, y.ctypes.data, len(x), ctypes.byref(loss),
+                                                   g.ctypes.data))
+        grads, off = [], 0
+        for fi, fo in zip(SURROGATE_DIMS[:-1], SURROGATE_DIMS[1:]):
+            gW = g[off:off + fi * fo].reshape(fi, fo).copy(); off += fi * fo
+            gb = g[off:off + fo].copy(); off += fo
+            grads.append((gW, gb))
+        return loss.value, grads
+
+
 from . import workloads  # noqa: E402  (seeded synthetic batches)

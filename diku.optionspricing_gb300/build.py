@@ -25,7 +25,7 @@ INCLUDE = os.path.join(ROOT, "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "--expt-relaxed-constexpr", "-I" + INCLUDE, "-I" + CSRC]
-CU_SOURCES = ["hwt_batched.cu", "hwt_plain.cu", "hwt_api.cu", "hwt_noalloc.cu"]
+CU_SOURCES = ["hwt_batched.cu", "hwt_plain.cu", "hwt_api.cu", "hwt_noalloc.cu", "hwt_surrogate.cu"]
 TOOLS = {"hwt-price": "tools/price_main.cpp", "hwt-compare": "tools/compare_main.cpp"}
 
 

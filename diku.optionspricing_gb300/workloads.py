@@ -115,3 +115,45 @@ WORKLOADS = {
     "uneven_30k": uneven_batch,
     "skewed_100k": skewed_batch,
 }
+
+
+# ---------------------------------------------------------------------------
+# Surrogate: training box and query batches
+# ---------------------------------------------------------------------------
+# The network's box is the uneven batch's own parameter box (the batch it must
+# price): t in [1, 10], T - t in [1, 10], strike / forward bond price in
+# [0.9, 1.1], a in [0.02, 0.20], sigma in [0.005, 0.02], 6..48 steps per year,
+# term unit 365.
+SURROGATE_BOX = dict(t_min=1.0, t_max=10.0, span_min=1.0, span_max=10.0, moneyness_min=0.9, moneyness_max=1.1,
+                     a_min=0.02, a_max=0.20, sigma_min=0.005, sigma_max=0.02, steps_min=6, steps_max=48,
+                     term_unit=365)
+
+
+def surrogate_training_batch(n=4_000_000, seed=3):
+    """Training samples: the uneven batch's distribution (seed 3)."""
+    return uneven_batch(n, seed)
+
+
+def surrogate_query_batch(n=1_000_000, seed=4, outside_fraction=0.10):
+    """Queries: 90% drawn like the uneven batch, 10% outside the box (longer
+    option or bond maturities, faster mean reversion, finer time steps or
+    strikes further from the forward), in random order."""
+    rng = np.random.default_rng(seed)
+    b = uneven_batch(n, seed)
+    out = rng.permutation(n)[: int(round(n * outside_fraction))]
+    kind = rng.integers(0, 4, len(out))
+    t, T, steps, a, strike = (b["option_maturity"], b["bond_maturity"], b["term_steps"], b["a"], b["strike"])
+    for k, idx in ((0, out[kind == 0]), (1, out[kind == 1]), (2, out[kind == 2]), (3, out[kind == 3])):
+        if k == 0:    # option maturity 11-15 y
+            t[idx] = rng.integers(11, 16, len(idx))
+            T[idx] = t[idx] + rng.integers(1, 11, len(idx))
+        elif k == 1:  # a above the box
+            a[idx] = rng.uniform(0.21, 0.30, len(idx))
+        elif k == 2:  # 49-64 steps per year
+            steps[idx] = rng.integers(49, 65, len(idx))
+        else:         # strike 12-20% away from the forward
+            sign = np.where(rng.integers(0, 2, len(idx)) == 0, -1.0, 1.0)
+            strike[idx] = forward_bond_price(t[idx], T[idx]) * (1.0 + sign * rng.uniform(0.12, 0.20, len(idx)))
+    b["outside"] = np.zeros(n, dtype=bool)
+    b["outside"][out] = True
+    return b

@@ -193,6 +193,71 @@ int hwt_get_config(const hwt_ctx *ctx, int mode, hwt_config *cfg);
  * CUDA events.  The roofline denominators of the tree kernels. */
 int hwt_measure_peaks(hwt_ctx *ctx, double *fp64_tflops, double *fp32_tflops);
 
+/* ---- Learned surrogate -------------------------------------------------------
+ * A 7 -> 4 x 256 (SiLU) -> 1 MLP mapping standardised (option maturity, bond
+ * maturity, strike / forward bond price, a, sigma, steps per year, call/put) to
+ * price / forward bond price, bf16 weights with fp32 accumulation on the tensor
+ * cores.  Trained on prices from the batched FP64 tree; options outside its
+ * training box go to the tree, and a random sample of every batch is repriced by
+ * the tree as its judge.  The reference has no learned part (row a10 of the
+ * build's scope); these entry points have no reference counterpart. */
+typedef struct hwt_box {
+    double t_min, t_max;             /* option maturity [years] */
+    double span_min, span_max;       /* bond maturity - option maturity [years] */
+    double moneyness_min, moneyness_max; /* strike / forward bond price */
+    double a_min, a_max, sigma_min, sigma_max;
+    int32_t steps_min, steps_max;    /* steps per year */
+    int32_t term_unit;               /* the only term unit inside the box */
+} hwt_box;
+
+typedef struct hwt_train_config {
+    int32_t epochs;                  /* passes over the samples (default 1) */
+    int32_t batch;                   /* samples per Adam step (default 8192) */
+    double lr, lr_min;               /* cosine decay from lr to lr_min over all steps */
+    uint64_t seed;                   /* shuffling */
+} hwt_train_config;
+
+typedef struct hwt_train_stats {
+    double final_loss;               /* mean 0.5 (y - f(x))^2 of the last epoch, standardised units */
+    double train_ms, label_ms;       /* training time; time the tree took to price the labels */
+    int64_t steps, samples;          /* Adam steps; in-box samples used */
+    double samples_per_s;
+    double y_mean, y_std;            /* target standardisation */
+} hwt_train_stats;
+
+typedef struct hwt_surrogate_stats {
+    int64_t n_in_box, n_routed, n_judged;
+    double judge_max_abs, judge_p99_abs, judge_mean_abs; /* |network - tree| on the judged sample */
+    double network_ms, tree_ms, route_ms, total_ms;
+} hwt_surrogate_stats;
+
+typedef struct hwt_surrogate hwt_surrogate;
+
+hwt_surrogate *hwt_surrogate_create(hwt_ctx *ctx, const hwt_box *box, uint64_t seed);
+void hwt_surrogate_destroy(hwt_surrogate *s);
+const char *hwt_surrogate_last_error(const hwt_surrogate *s);
+/* Prices the (host) samples with the batched FP64 tree and trains on them. */
+int hwt_surrogate_train(hwt_surrogate *s, const hwt_options *samples, const hwt_yield *yield,
+                        const hwt_train_config *cfg, hwt_train_stats *stats);
+/* Prices host options: network inside the box, tree (tree_mode: a batched mode)
+ * outside it and for the judge's sample (fraction judge_fraction, drawn from
+ * `seed`), whose options get the tree price. */
+int hwt_surrogate_price(hwt_surrogate *s, const hwt_options *opts, const hwt_yield *yield, double judge_fraction,
+                        uint64_t seed, int tree_mode, double *out_prices, hwt_surrogate_stats *stats);
+/* Checkpoint: box, target scaling, weights and Adam state (resume training). */
+int hwt_surrogate_save(const hwt_surrogate *s, const char *path);
+int hwt_surrogate_load(hwt_surrogate *s, const char *path);
+/* Parameters: layer l has W_l [fan_in][fan_out] then b_l [fan_out], fan_in 8
+ * (7 features + a zero pad row) for the first layer; get (set = 0) or set them. */
+int64_t hwt_surrogate_param_count(const hwt_surrogate *s);
+int hwt_surrogate_params(hwt_surrogate *s, float *params, int64_t count, int set);
+/* Forward pass and loss/gradients on host buffers of standardised features
+ * x [n][7] and standardised targets y [n] (no update): the hooks the gradient
+ * check against the CPU oracle uses. */
+int hwt_surrogate_forward(hwt_surrogate *s, const float *x, int n, float *out);
+int hwt_surrogate_loss_grads(hwt_surrogate *s, const float *x, const float *y, int n, double *loss,
+                             float *grads);
+
 #ifdef __cplusplus
 }
 #endif
