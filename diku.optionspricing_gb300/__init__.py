@@ -463,7 +463,7 @@ class Box(ctypes.Structure):
                 ("span_max", ctypes.c_double), ("moneyness_min", ctypes.c_double),
                 ("moneyness_max", ctypes.c_double), ("a_min", ctypes.c_double), ("a_max", ctypes.c_double),
                 ("sigma_min", ctypes.c_double), ("sigma_max", ctypes.c_double), ("steps_min", ctypes.c_int32),
-                ("steps_max", ctypes.c_int32), ("term_unit", ctypes.c_int32)]
+                ("steps_max", ctypes.c_int32), ("term_unit", ctypes.c_int32), ("residual", ctypes.c_int32)]
 
 
 class TrainConfig(ctypes.Structure):
@@ -482,7 +482,7 @@ class TrainStats(ctypes.Structure):
 
 class SurrogateStats(ctypes.Structure):
     _fields_ = [("n_in_box", ctypes.c_int64), ("n_routed", ctypes.c_int64), ("n_judged", ctypes.c_int64),
-                ("judge_max_abs", ctypes.c_double), ("judge_p99_abs", ctypes.c_double),
+                ("fell_back", ctypes.c_int32), ("pad", ctypes.c_int32), ("judge_max_abs", ctypes.c_double), ("judge_p99_abs", ctypes.c_double),
                 ("judge_mean_abs", ctypes.c_double), ("network_ms", ctypes.c_double), ("tree_ms", ctypes.c_double),
                 ("route_ms", ctypes.c_double), ("total_ms", ctypes.c_double)]
 
@@ -497,8 +497,8 @@ _SIGNATURES.update({
     "hwt_surrogate_train": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(_Options), ctypes.POINTER(_Yield),
                                            ctypes.POINTER(TrainConfig), ctypes.POINTER(TrainStats)]),
     "hwt_surrogate_price": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(_Options), ctypes.POINTER(_Yield),
-                                           ctypes.c_double, ctypes.c_uint64, ctypes.c_int, ctypes.c_void_p,
-                                           ctypes.POINTER(SurrogateStats)]),
+                                           ctypes.c_double, ctypes.c_uint64, ctypes.c_int, ctypes.c_double,
+                                           ctypes.c_void_p, ctypes.POINTER(SurrogateStats)]),
     "hwt_surrogate_save": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p]),
     "hwt_surrogate_load": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p]),
     "hwt_surrogate_param_count": (ctypes.c_int64, [ctypes.c_void_p]),
@@ -514,9 +514,10 @@ SURROGATE_DIMS = (8, 256, 256, 256, 256, 1)  # first fan-in: 7 features + 1 zero
 class Surrogate:
     """MLP surrogate with the tree as fallback (outside the box) and judge."""
 
-    def __init__(self, pricer: Pricer, box: dict | None = None, seed: int = 1):
+    def __init__(self, pricer: Pricer, box: dict | None = None, seed: int = 1, residual: bool = True):
         from .workloads import SURROGATE_BOX
         b = dict(SURROGATE_BOX if box is None else box)
+        b.setdefault("residual", 1 if residual else 0)
         self.box = Box(**b)
         self.pricer = pricer
         self._s = lib().hwt_surrogate_create(pricer._ctx, ctypes.byref(self.box), seed)
@@ -550,11 +551,13 @@ class Surrogate:
         return self.train_stats.as_dict()
 
     def price(self, options: Options, yield_: Yield, judge_fraction: float = 0.01, seed: int = 11,
-              tree_mode: int = BATCHED_MIXED) -> np.ndarray:
+              tree_mode: int = BATCHED_MIXED, judge_tolerance: float = 0.0) -> np.ndarray:
+        """Network inside the box, tree outside it and on the judged sample; with
+        judge_tolerance > 0 a batch whose judged error exceeds it is priced by the tree."""
         out = np.empty(options.N, dtype=np.float64)
         o, y = options._c(), yield_._c()
         self._check(lib().hwt_surrogate_price(self._s, ctypes.byref(o), ctypes.byref(y), judge_fraction, seed,
-                                              tree_mode, out.ctypes.data, ctypes.byref(self.stats)))
+                                              tree_mode, judge_tolerance, out.ctypes.data, ctypes.byref(self.stats)))
         return out
 
     def save(self, path: str):

@@ -96,9 +96,9 @@ __host__ __device__ int pick_warp_class(int width)
 
 __device__ __forceinline__ int work_bucket(unsigned long long work)
 {
-    // 4 buckets per octave, descending: heavy work sorts first.
+    // 2 buckets per octave, descending: heavy work sorts first.
     const double lw = log2((double)work + 1.0);
-    int b = (int)(lw * 4.0);
+    int b = (int)(lw * 2.0);
     if (b > kWorkBuckets - 1) b = kWorkBuckets - 1;
     return kWorkBuckets - 1 - b;
 }
@@ -134,9 +134,14 @@ __global__ void size_kernel(EngineParams p)
             p.s.trees[i] = t;
             nodes = (unsigned long long)s.nodes;
             const int tier = s.width <= p.big_threshold ? 2 : (s.width <= kMaxBlockK * p.group_threads ? 1 : 0);
-            const int cls = tier == 2 ? pick_warp_class(s.width) : 0;
+            int cls = 0;
+            if (tier == 2) {
+                cls = pick_warp_class(s.width);
+                const int top = s.edges ? (s.width - 1) % cls_K(cls) : 0;  // slot of node W-1
+                cls |= top << 6;
+            }
             const unsigned long long work = (unsigned long long)s.nodes + (unsigned long long)s.width;
-            key = (tier * kWorkBuckets + work_bucket(work)) * 64 + cls;
+            key = (tier * kWorkBuckets + work_bucket(work)) * kClassSlots + cls;
             p.s.keys[i] = key;
             atomicMax(&p.s.status->max_width, s.width);
             atomicMax(&p.s.status->max_height, s.n);
@@ -166,7 +171,7 @@ __global__ void scan_kernel(EngineParams p)
         const bool warp = b >= 2 * kTierBins;
         int t = 0;
         if (warp && c > 0) {
-            const int G = 32 / cls_L(b & 63);
+            const int G = 32 / cls_L((b % kClassSlots) & 63);  // low 6 bits of the class: K and L
             t = (c + G - 1) / G;
         }
         cnt[q] = c; tsk[q] = t; sa += c; sb += t;
@@ -210,8 +215,8 @@ __global__ void scatter_kernel(EngineParams p)
     const int pos = p.s.bin_start[key] + q;
     p.s.order[pos] = i;
     if (key >= 2 * kTierBins) {
-        const int cls = key & 63;
-        const int G = 32 / cls_L(cls);
+        const int cls = key % kClassSlots;
+        const int G = 32 / cls_L(cls & 63);
         if (q % G == 0) {
             WarpTask t;
             t.start = pos;
@@ -237,18 +242,33 @@ struct Slice {
     typedef typename Mode::Row R;
     typedef typename Mode::Scal S;
 
-    R r[K];          // current row
-    R c0[K], c1[K], c2[K];  // FP64: fa/fb/fc or ba/bb/bc.  Flux: U, D, g.
-    R cl, cr;        // flux: up of node k0-1, down of node k0+K
-    R jlo, jhi;      // edge jump coefficients of this slice (0 if none)
-    unsigned mlo, mhi;       // slots receiving / sending the low and high jumps
-    unsigned mlo2, mhi2;     // flux forward: slots that send the jumps (outflow)
+    R r[K];                 // current row
+    R c0[K], c1[K], c2[K];  // FP64: fa/fb/fc or ba/bb/bc.  Flux: up, down, g.
+    R cl, cr;               // flux: up of node k0-1, down of node k0+K
+    // Edge jumps (+-jmax branch two nodes away).  Nodes 0 and 2 sit at compile-time
+    // slots (0 and 2 % K); node W-1 sits at slot ts = (W-1) % K, which is the same
+    // for every tree a warp prices (it is part of the warp class), so the top
+    // edge is handled by one uniform switch per step instead of a test per slot.
+    R jlo, jhi;             // FP64: jump coefficient times the receiving node's G; flux: pu_b, pd_c
+    bool n0, n2, nw1, nw3;  // this thread owns node 0 / 2 / W-1 / W-3 of an edged tree
+    int ts;
+
+    __device__ __forceinline__ void setup_owners(const Tree &t, int k0)
+    {
+        const int W = t.width;
+        const bool e = t.edges != 0;
+        n0 = e && k0 == 0;
+        n2 = e && k0 <= 2 && 2 < k0 + K;
+        nw1 = e && k0 <= W - 1 && W - 1 < k0 + K;
+        nw3 = e && k0 <= W - 3 && W - 3 < k0 + K;
+        ts = (W - 1) % K;
+    }
 
     // Coefficients for the forward sweep of tree `t`.
     __device__ __forceinline__ void setup_forward(const Tree &t, int k0)
     {
         const int W = t.width, jc = t.jc, jmax = t.jmax;
-        mlo = mhi = mlo2 = mhi2 = 0;
+        setup_owners(t, k0);
         jlo = jhi = (R)0;
         if constexpr (!Mode::kFlux) {
 #pragma unroll
@@ -262,8 +282,8 @@ struct Slice {
                     b = G * me.stay;
                     if (k >= 1) a = G * branch(j - 1, jmax, t.M).up;
                     if (k + 1 < W) c = G * branch(j + 1, jmax, t.M).down;
-                    if (t.edges && k == 2) { jlo = G * pu_b(-jmax, t.M); mlo |= 1u << s; }
-                    if (t.edges && k == W - 3) { jhi = G * pd_c(jmax, t.M); mhi |= 1u << s; }
+                    if (t.edges && k == 2) jlo = G * pu_b(-jmax, t.M);
+                    if (t.edges && k == W - 3) jhi = G * pd_c(jmax, t.M);
                 }
                 c0[s] = a; c1[s] = b; c2[s] = c;
                 r[s] = (k == jc) ? 1.0 : 0.0;
@@ -287,12 +307,6 @@ struct Slice {
                     } else {
                         u = 1.0f / 6.0f + (x2 + x) * 0.5f;  // pu_a
                         d = 1.0f / 6.0f + (x2 - x) * 0.5f;  // pd_a
-                    }
-                    if (t.edges) {
-                        if (k == 0) mlo2 |= 1u << s;
-                        if (k == 2) mlo |= 1u << s;
-                        if (k == W - 1) mhi2 |= 1u << s;
-                        if (k == W - 3) mhi |= 1u << s;
                     }
                 }
                 c0[s] = u; c1[s] = d; c2[s] = g;
@@ -326,7 +340,6 @@ struct Slice {
     __device__ __forceinline__ void setup_backward(const Tree &t, int k0)
     {
         const int W = t.width, jc = t.jc, jmax = t.jmax;
-        mlo = mhi = 0;
         if constexpr (!Mode::kFlux) {
             jlo = jhi = 0.0;
 #pragma unroll
@@ -338,31 +351,87 @@ struct Slice {
                     const double G = column_discount(j, t.dr, t.dt);
                     const Branch me = branch(j, jmax, t.M);
                     a = G * me.up; b = G * me.stay; c = G * me.down;
-                    if (t.edges && k == 0) { jlo = G * me.jump; mlo |= 1u << s; }
-                    if (t.edges && k == W - 1) { jhi = G * me.jump; mhi |= 1u << s; }
+                    if (t.edges && k == 0) jlo = G * me.jump;
+                    if (t.edges && k == W - 1) jhi = G * me.jump;
                 }
                 c0[s] = a; c1[s] = b; c2[s] = c;
                 r[s] = (k < W) ? 100.0 : 0.0;
             }
         } else {
-            // U, D, g and jlo/jhi are the same as the forward's; only masks change.
+            // up, down, g and the jump probabilities are the forward's
 #pragma unroll
-            for (int s = 0; s < K; ++s) {
-                const int k = k0 + s;
-                if (t.edges && k < W) {
-                    if (k == 0) mlo |= 1u << s;
-                    if (k == W - 1) mhi |= 1u << s;
-                }
-                r[s] = (R)0;
+            for (int s = 0; s < K; ++s) r[s] = (R)0;
+        }
+    }
+
+    // Top-edge terms with the slot of node W-1 known at compile time.
+    template <int TS>
+    __device__ __forceinline__ void top_forward(R (&v)[K], const Ext<R, K> &x) const
+    {
+        if constexpr (TS < K) {
+            constexpr int S3 = (TS + 2 * K - 2) % K;  // slot of node W-3
+            if constexpr (Mode::kFlux) {
+                if (nw1) v[TS] = fma(-jhi, r[TS], v[TS]);
+            }
+            if (nw3) v[S3] = fma(jhi, x.e[S3 + 4], v[S3]);
+        }
+    }
+
+    template <int TS>
+    __device__ __forceinline__ void top_backward(R (&v)[K], const Ext<R, K> &x) const
+    {
+        if constexpr (TS < K) {
+            if constexpr (Mode::kFlux) {
+                if (nw1) v[TS] = fma(jhi, x.e[TS] - x.e[TS + 2], v[TS]);
+            } else {
+                if (nw1) v[TS] = fma(jhi, x.e[TS], v[TS]);
             }
         }
     }
 
-    // One forward step: r <- G o gather(r), reading neighbours from x.
-    __device__ __forceinline__ void forward_step(const Ext<R, K> &x, bool edge_live, unsigned wlo, unsigned whi)
+    __device__ __forceinline__ void edges_forward(R (&v)[K], const Ext<R, K> &x) const
     {
+        constexpr int S2 = 2 % K;  // slot of node 2
+        if constexpr (Mode::kFlux) {
+            if (n0) v[0] = fma(-jlo, r[0], v[0]);
+        }
+        if (n2) v[S2] = fma(jlo, x.e[S2], v[S2]);
+        switch (ts) {
+            case 0: top_forward<0>(v, x); break;
+            case 1: top_forward<1>(v, x); break;
+            case 2: top_forward<2>(v, x); break;
+            case 3: top_forward<3>(v, x); break;
+            case 4: top_forward<4>(v, x); break;
+            case 5: top_forward<5>(v, x); break;
+            case 6: top_forward<6>(v, x); break;
+            default: top_forward<7>(v, x); break;
+        }
+    }
+
+    __device__ __forceinline__ void edges_backward(R (&v)[K], const Ext<R, K> &x) const
+    {
+        if constexpr (Mode::kFlux) {
+            if (n0) v[0] = fma(jlo, x.e[4] - x.e[2], v[0]);
+        } else {
+            if (n0) v[0] = fma(jlo, x.e[4], v[0]);
+        }
+        switch (ts) {
+            case 0: top_backward<0>(v, x); break;
+            case 1: top_backward<1>(v, x); break;
+            case 2: top_backward<2>(v, x); break;
+            case 3: top_backward<3>(v, x); break;
+            case 4: top_backward<4>(v, x); break;
+            case 5: top_backward<5>(v, x); break;
+            case 6: top_backward<6>(v, x); break;
+            default: top_backward<7>(v, x); break;
+        }
+    }
+
+    // One forward step: r <- G o gather(r), reading neighbours from x.
+    __device__ __forceinline__ void forward_step(const Ext<R, K> &x, bool edge_live)
+    {
+        R v[K];
         if constexpr (!Mode::kFlux) {
-            R v[K];
 #pragma unroll
             for (int s = 0; s < K; ++s) {
                 R t = c0[s] * x.e[s + 1];
@@ -370,17 +439,11 @@ struct Slice {
                 t = fma(c2[s], x.e[s + 3], t);
                 v[s] = t;
             }
-            if (edge_live) {
-#pragma unroll
-                for (int s = 0; s < K; ++s) {
-                    if (wlo & (1u << s)) { if (mlo & (1u << s)) v[s] = fma(jlo, x.e[s], v[s]); }
-                    if (whi & (1u << s)) { if (mhi & (1u << s)) v[s] = fma(jhi, x.e[s + 4], v[s]); }
-                }
-            }
+            if (edge_live) edges_forward(v, x);
 #pragma unroll
             for (int s = 0; s < K; ++s) r[s] = v[s];
         } else {
-            R f[K], h[K], v[K];
+            R f[K], h[K];
 #pragma unroll
             for (int s = 0; s < K; ++s) { f[s] = c0[s] * r[s]; h[s] = c1[s] * r[s]; }
             const R fl = cl * x.e[1], hr = cr * x.e[K + 2];
@@ -390,26 +453,14 @@ struct Slice {
                 const R hin = (s == K - 1) ? hr : h[s + 1];
                 v[s] = (r[s] + (fin - f[s])) + (hin - h[s]);
             }
-            if (edge_live) {
-#pragma unroll
-                for (int s = 0; s < K; ++s) {
-                    if (wlo & (1u << s)) {
-                        if (mlo2 & (1u << s)) v[s] = fma(-jlo, r[s], v[s]);
-                        if (mlo & (1u << s)) v[s] = fma(jlo, x.e[s], v[s]);
-                    }
-                    if (whi & (1u << s)) {
-                        if (mhi2 & (1u << s)) v[s] = fma(-jhi, r[s], v[s]);
-                        if (mhi & (1u << s)) v[s] = fma(jhi, x.e[s + 4], v[s]);
-                    }
-                }
-            }
+            if (edge_live) edges_forward(v, x);
 #pragma unroll
             for (int s = 0; s < K; ++s) r[s] = fma(c2[s], v[s], v[s]);
         }
     }
 
     // One backward step: r <- G o P r (flux: on the deviation from `base`).
-    __device__ __forceinline__ void backward_step(const Ext<R, K> &x, bool edge_live, unsigned wlo, unsigned whi, R base)
+    __device__ __forceinline__ void backward_step(const Ext<R, K> &x, bool edge_live, R base)
     {
         R v[K];
         if constexpr (!Mode::kFlux) {
@@ -420,13 +471,7 @@ struct Slice {
                 t = fma(c2[s], x.e[s + 1], t);
                 v[s] = t;
             }
-            if (edge_live) {
-#pragma unroll
-                for (int s = 0; s < K; ++s) {
-                    if (wlo & (1u << s)) { if (mlo & (1u << s)) v[s] = fma(jlo, x.e[s + 4], v[s]); }
-                    if (whi & (1u << s)) { if (mhi & (1u << s)) v[s] = fma(jhi, x.e[s], v[s]); }
-                }
-            }
+            if (edge_live) edges_backward(v, x);
 #pragma unroll
             for (int s = 0; s < K; ++s) r[s] = v[s];
         } else {
@@ -436,13 +481,7 @@ struct Slice {
                 const R up = x.e[s + 3] - d0, dn = x.e[s + 1] - d0;
                 v[s] = d0 + fma(c0[s], up, c1[s] * dn);
             }
-            if (edge_live) {
-#pragma unroll
-                for (int s = 0; s < K; ++s) {
-                    if (wlo & (1u << s)) { if (mlo & (1u << s)) v[s] = fma(jlo, x.e[s + 4] - x.e[s + 2], v[s]); }
-                    if (whi & (1u << s)) { if (mhi & (1u << s)) v[s] = fma(jhi, x.e[s] - x.e[s + 2], v[s]); }
-                }
-            }
+            if (edge_live) edges_backward(v, x);
 #pragma unroll
             for (int s = 0; s < K; ++s) r[s] = fma(c2[s], v[s] + base, v[s]);
         }
@@ -594,7 +633,7 @@ __device__ void price_warp_task(const EngineParams &p, const WarpTask &task)
     typedef typename Mode::Scal S;
     constexpr unsigned NONE = 0x7fffffffu;
     const int lane = threadIdx.x & 31;
-    const int L = cls_L(task.cls);
+    const int L = cls_L(task.cls & 63);
     const int g = lane / L, lis = lane & (L - 1);
     const bool valid = g < task.count;
     Tree t;
@@ -613,7 +652,7 @@ __device__ void price_warp_task(const EngineParams &p, const WarpTask &task)
     // Rows of trees that are done keep being updated (their segment is isolated by
     // the width-L shuffles), so the step loop carries no per-tree predicates.
     sl.setup_forward(t, k0);
-    const unsigned wlo = __reduce_or_sync(FULL, sl.mlo | sl.mlo2), whi = __reduce_or_sync(FULL, sl.mhi | sl.mhi2);
+    sl.ts = (task.cls >> 6) & 7;  // the warp's common top-edge slot
     const int e_f = (int)__reduce_min_sync(FULL, (valid && t.edges) ? (unsigned)t.jmax : NONE);
     const int rm = (t.m >= 2 && t.m < t.n) ? t.m - 1 : -1;  // row m-1 (row 0 sums to 1)
     const int rn = (t.n >= 2) ? t.n - 1 : -1;               // row n-1
@@ -628,7 +667,7 @@ __device__ void price_warp_task(const EngineParams &p, const WarpTask &task)
         const int stop = ev < fsteps ? ev : fsteps;          // steps i .. stop-1 produce rows .. stop
         for (; i < stop; ++i) {
             exchange_warp<R, K>(x, sl.r, L);
-            sl.forward_step(x, i >= e_f, wlo, whi);
+            sl.forward_step(x, i >= e_f);
         }
         if (ev <= fsteps) {
             S acc = sl.partial_sum(k0, W);
@@ -642,7 +681,6 @@ __device__ void price_warp_task(const EngineParams &p, const WarpTask &task)
     // ---- backward sweep from each tree's own height; rows of trees that have not
     // started yet are put back to the face value after every step.
     sl.setup_backward(t, k0);
-    const unsigned blo = __reduce_or_sync(FULL, sl.mlo), bhi = __reduce_or_sync(FULL, sl.mhi);
     const int e_b = (int)__reduce_min_sync(FULL, (valid && t.edges) ? (unsigned)t.jmax : NONE);
     const int bsteps = (int)__reduce_max_sync(FULL, (unsigned)(t.n > 0 ? t.n : 0));
     const int n_min = (int)__reduce_min_sync(FULL, valid ? (unsigned)t.n : (unsigned)bsteps);
@@ -656,7 +694,7 @@ __device__ void price_warp_task(const EngineParams &p, const WarpTask &task)
         const int lo = pm > 0 ? pm : 0;
         for (; i >= lo; --i) {
             exchange_warp<R, K>(x, sl.r, L);
-            sl.backward_step(x, i >= e_b, blo, bhi, base);
+            sl.backward_step(x, i >= e_b, base);
             if (i >= n_min && i >= t.n) {
 #pragma unroll
                 for (int s = 0; s < K; ++s) sl.r[s] = (k0 + s < W) ? face : (R)0;
@@ -699,7 +737,6 @@ __device__ void price_block_tree(const EngineParams &p, const Tree &t, const Gro
     int parity = 0;
 
     sl.setup_forward(t, k0);
-    const unsigned wlo = __reduce_or_sync(FULL, sl.mlo | sl.mlo2), whi = __reduce_or_sync(FULL, sl.mhi | sl.mhi2);
     S sum_m1 = (S)1, sum_n1 = (S)1;
     const int fsteps = t.n > 1 ? t.n - 1 : 0;
     for (int i = 0; i < fsteps; ++i) {
@@ -708,7 +745,7 @@ __device__ void price_block_tree(const EngineParams &p, const Tree &t, const Gro
         // rows outside the cone of row i+1 stay zero: skip whole warps there
         const int reach = (i + 1 < jc) ? i + 1 : jc;
         const bool active = wk1 > jc - reach && wk0 <= jc + reach && wk0 < W;
-        if (active) sl.forward_step(x, t.edges && i >= t.jmax, wlo, whi);
+        if (active) sl.forward_step(x, t.edges && i >= t.jmax);
         const int row = i + 1;
         if (row == t.m - 1 || row == t.n - 1) {
             S acc = sl.partial_sum(k0, W);
@@ -725,14 +762,13 @@ __device__ void price_block_tree(const EngineParams &p, const Tree &t, const Gro
     const Scales<S> sc = tree_scales<S>(t, sum_m1, sum_n1, p.yc);
 
     sl.setup_backward(t, k0);
-    const unsigned blo = __reduce_or_sync(FULL, sl.mlo), bhi = __reduce_or_sync(FULL, sl.mhi);
     R base = Mode::kFlux ? (R)100 : (R)0;
     for (int i = t.n - 1; i >= 0; --i) {
         exchange_block<R, K>(x, sl.r, sh_x, parity, gr);
         parity ^= 1;
         const int reach = (i < t.jmax) ? i : t.jmax;
         const bool active = wk1 > jc - reach && wk0 <= jc + reach && wk0 < W;
-        if (active) sl.backward_step(x, t.edges && i >= t.jmax, blo, bhi, base);
+        if (active) sl.backward_step(x, t.edges && i >= t.jmax, base);
         if (i == t.m) {
             sl.payoff(sc.kappa, base, t.X, t.type);
             base = (R)0;
@@ -815,7 +851,7 @@ __global__ void __launch_bounds__(kPricingThreads, 1) price_kernel(EngineParams 
         tsk = __shfl_sync(FULL, tsk, 0);
         if (tsk >= n_tasks) break;
         const WarpTask wt = p.s.tasks[tsk];
-        switch (cls_K(wt.cls)) {
+        switch (cls_K(wt.cls & 63)) {
             case 1: price_warp_task<Mode, 1>(p, wt); break;
             case 2: price_warp_task<Mode, 2>(p, wt); break;
             case 3: price_warp_task<Mode, 3>(p, wt); break;

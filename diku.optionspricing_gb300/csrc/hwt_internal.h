@@ -64,10 +64,12 @@ constexpr int kMaxTreeWidth = kMaxBlockK * kPricingThreads;  // widest tree acce
 // Sort keys: [tier][work bucket][warp class].  Tier 0: trees wider than a group
 // can hold, priced by the whole block; tier 1: priced by a group of warps;
 // tier 2: small trees packed into warp tasks.  Descending work inside each tier.
-constexpr int kWorkBuckets = 128;
+// A warp class is K and L (6 bits) and the slot of the top edge node (3 bits).
+constexpr int kWorkBuckets = 64;
 constexpr int kTiers = 3;
-constexpr int kKeyBins = kTiers * kWorkBuckets * 64;
-constexpr int kTierBins = kWorkBuckets * 64;
+constexpr int kClassSlots = 512;
+constexpr int kKeyBins = kTiers * kWorkBuckets * kClassSlots;
+constexpr int kTierBins = kWorkBuckets * kClassSlots;
 
 // Per-run status written by the device (read back after each run).
 struct RunStatus {

@@ -11,7 +11,7 @@
 // caller passes device pointers for the options, the yield curve and the prices.
 //
 // The array is a __device__ variable: every GPU that loads the library holds it
-// (about 3.2 MB) until the process exits.  In host code its name is only a
+// (about 4 MB) until the process exits.  In host code its name is only a
 // host-side stand-in, so its device address is looked up once per device with
 // cudaGetSymbolAddress, on the first call made with that device current; make
 // that first call before any stream capture.  All calls share the array and it

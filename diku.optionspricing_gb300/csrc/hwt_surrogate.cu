@@ -40,9 +40,21 @@ struct FeatureNorm {
 // device kernels
 // ---------------------------------------------------------------------------
 
-// Features, forward bond price and in-box flag of each option.
+// Hull-White closed-form price of a European option on a zero-coupon bond
+// (Jamshidian 1989) with face 100: the control variate of the residual network.
+__device__ double hw_closed_form(double t, double T, double X, double a, double sigma, double Pt, double PT, int type)
+{
+    const double B = -expm1(-a * (T - t)) / a;
+    const double sp = sigma * B * sqrt(-expm1(-2.0 * a * t) / (2.0 * a));
+    const double bond = 100.0 * PT, strike = X * Pt;
+    if (!(sp > 1e-12)) return type == 1 ? fmax(strike - bond, 0.0) : fmax(bond - strike, 0.0);
+    const double h = log(bond / strike) / sp + 0.5 * sp;
+    return type == 1 ? strike * normcdf(-h + sp) - bond * normcdf(-h) : bond * normcdf(h) - strike * normcdf(h - sp);
+}
+
+// Features, forward bond price, control-variate price and in-box flag of each option.
 __global__ void features_kernel(DevOptions o, DevYield yc, hwt_box box, FeatureNorm fn, __nv_bfloat16 *X,
-                                double *F, uint8_t *inbox)
+                                double *F, double *base, uint8_t *inbox)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= o.n) return;
@@ -59,6 +71,7 @@ __global__ void features_kernel(DevOptions o, DevYield yc, hwt_box box, FeatureN
     for (int q = 0; q < kIn; ++q) X[(size_t)i * kInPad + q] = __float2bfloat16(((float)v[q] - fn.mean[q]) * fn.inv_std[q]);
     X[(size_t)i * kInPad + kIn] = __float2bfloat16(0.f);
     F[i] = fwd;
+    base[i] = box.residual ? hw_closed_form(t, T, o.strike[i], a, sg, Pt, PT, o.type[i]) : 0.0;
     const double span = T - t;
     const bool in = t >= box.t_min && t <= box.t_max && span >= box.span_min && span <= box.span_max &&
                     mny >= box.moneyness_min && mny <= box.moneyness_max && a >= box.a_min && a <= box.a_max &&
@@ -135,18 +148,19 @@ __global__ void gather_rows_kernel(const __nv_bfloat16 *X, const float *y, const
     yo[i] = y[s];
 }
 
-__global__ void targets_kernel(const double *price, const double *F, int n, double ymean, double yinv, float *y)
+__global__ void targets_kernel(const double *price, const double *F, const double *base, int n, double ymean,
+                               double yinv, float *y)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) y[i] = (float)((price[i] / F[i] - ymean) * yinv);
+    if (i < n) y[i] = (float)(((price[i] - base[i]) / F[i] - ymean) * yinv);
 }
 
 // Price from the network output for in-box options.
-__global__ void decode_kernel(const float *out, const double *F, const uint8_t *inbox, int n, double ymean, double ystd,
-                              double *price)
+__global__ void decode_kernel(const float *out, const double *F, const double *base, const uint8_t *inbox, int n,
+                              double ymean, double ystd, double *price)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n && inbox[i]) price[i] = F[i] * ((double)out[i] * ystd + ymean);
+    if (i < n && inbox[i]) price[i] = base[i] + F[i] * ((double)out[i] * ystd + ymean);
 }
 
 __device__ __forceinline__ unsigned long long mix64(unsigned long long x)
@@ -624,23 +638,25 @@ int hwt_surrogate_train(hwt_surrogate *s, const hwt_options *samples, const hwt_
     Scoped guard;
     if ((r = upload_curve(s, cv, y))) { free_batch(b); return r; }
     __nv_bfloat16 *X = nullptr, *Xs = nullptr;
-    double *F = nullptr, *dprice = nullptr;
+    double *F = nullptr, *dprice = nullptr, *base = nullptr;
     uint8_t *inbox = nullptr;
     float *yv = nullptr, *ys = nullptr;
     int32_t *perm = nullptr;
     bool ok = cudaMalloc(&X, 2ull * n * kInPad) == cudaSuccess && cudaMalloc(&Xs, 2ull * n * kInPad) == cudaSuccess &&
               cudaMalloc(&F, 8ull * n) == cudaSuccess && cudaMalloc(&dprice, 8ull * n) == cudaSuccess &&
+              cudaMalloc(&base, 8ull * n) == cudaSuccess &&
               cudaMalloc(&inbox, n) == cudaSuccess && cudaMalloc(&yv, 4ull * n) == cudaSuccess &&
               cudaMalloc(&ys, 4ull * n) == cudaSuccess && cudaMalloc(&perm, 4ull * n) == cudaSuccess;
-    guard.ptrs = {X, Xs, F, dprice, inbox, yv, ys, perm};
+    guard.ptrs = {X, Xs, F, dprice, base, inbox, yv, ys, perm};
     if (!ok) { free_batch(b); free_curve(cv); return sfail(s, HWT_ENOMEM, "training buffers"); }
     if (upload_batch(b, samples, s->stream) != cudaSuccess) { free_batch(b); free_curve(cv); return sfail(s, HWT_ECUDA, "samples H2D"); }
     DevYield yc;
     yc.n = cv.n; yc.rate = cv.rate; yc.rate_f = cv.rate_f; yc.day = cv.day;
-    features_kernel<<<(n + 255) / 256, 256, 0, s->stream>>>(dev_view(b, n), yc, s->box, s->fn, X, F, inbox);
-    std::vector<double> Fh(n);
+    features_kernel<<<(n + 255) / 256, 256, 0, s->stream>>>(dev_view(b, n), yc, s->box, s->fn, X, F, base, inbox);
+    std::vector<double> Fh(n), bh(n);
     std::vector<uint8_t> ib(n);
     cudaMemcpyAsync(Fh.data(), F, 8ull * n, cudaMemcpyDeviceToHost, s->stream);
+    cudaMemcpyAsync(bh.data(), base, 8ull * n, cudaMemcpyDeviceToHost, s->stream);
     cudaMemcpyAsync(ib.data(), inbox, n, cudaMemcpyDeviceToHost, s->stream);
     cudaError_t ce = cudaStreamSynchronize(s->stream);
     free_batch(b);
@@ -650,14 +666,14 @@ int hwt_surrogate_train(hwt_surrogate *s, const hwt_options *samples, const hwt_
     int64_t nin = 0;
     for (int i = 0; i < n; ++i) {
         if (!ib[i]) continue;
-        const double v = price[i] / Fh[i];
+        const double v = (price[i] - bh[i]) / Fh[i];
         sum += v; sum2 += v * v; ++nin;
     }
     if (nin < batch) return sfail(s, HWT_EINVAL, "fewer in-box samples than one batch");
     s->ymean = sum / nin;
     s->ystd = std::max(sqrt(std::max(sum2 / nin - s->ymean * s->ymean, 0.0)), 1e-12);
     SCUDA(s, cudaMemcpyAsync(dprice, price.data(), 8ull * n, cudaMemcpyHostToDevice, s->stream), "prices H2D");
-    targets_kernel<<<(n + 255) / 256, 256, 0, s->stream>>>(dprice, F, n, s->ymean, 1.0 / s->ystd, yv);
+    targets_kernel<<<(n + 255) / 256, 256, 0, s->stream>>>(dprice, F, base, n, s->ymean, 1.0 / s->ystd, yv);
     SCUDA(s, cudaGetLastError(), "targets");
     if ((r = ensure_act(s, batch))) return r;
 
@@ -723,7 +739,7 @@ int hwt_surrogate_train(hwt_surrogate *s, const hwt_options *samples, const hwt_
 }
 
 int hwt_surrogate_price(hwt_surrogate *s, const hwt_options *o, const hwt_yield *y, double judge_fraction,
-                        uint64_t seed, int tree_mode, double *out, hwt_surrogate_stats *stats)
+                        uint64_t seed, int tree_mode, double judge_tolerance, double *out, hwt_surrogate_stats *stats)
 {
     if (!s || !o || !y || (o->n > 0 && !out)) return HWT_EINVAL;
     if (!s->trained) return sfail(s, HWT_EINVAL, "the surrogate has not been trained or loaded");
@@ -741,26 +757,27 @@ int hwt_surrogate_price(hwt_surrogate *s, const hwt_options *o, const hwt_yield 
     if (!alloc_batch(b, n)) { free_batch(b); return sfail(s, HWT_ENOMEM, "option buffers"); }
     if ((r = upload_curve(s, cv, y))) { free_batch(b); return r; }
     __nv_bfloat16 *X = nullptr;
-    double *F = nullptr, *dout = nullptr, *tree_out = nullptr;
+    double *F = nullptr, *dout = nullptr, *tree_out = nullptr, *base = nullptr;
     uint8_t *inbox = nullptr, *kind = nullptr;
     int32_t *list = nullptr, *count = nullptr;
     bool ok = cudaMalloc(&X, 2ull * n * kInPad) == cudaSuccess && cudaMalloc(&F, 8ull * n) == cudaSuccess &&
+              cudaMalloc(&base, 8ull * n) == cudaSuccess &&
               cudaMalloc(&dout, 8ull * n) == cudaSuccess && cudaMalloc(&tree_out, 8ull * n) == cudaSuccess &&
               cudaMalloc(&inbox, n) == cudaSuccess && cudaMalloc(&kind, n) == cudaSuccess &&
               cudaMalloc(&list, 4ull * n) == cudaSuccess && cudaMalloc(&count, 4) == cudaSuccess;
-    guard.ptrs = {X, F, dout, tree_out, inbox, kind, list, count};
+    guard.ptrs = {X, F, dout, tree_out, base, inbox, kind, list, count};
     if (!ok) { free_batch(b); free_curve(cv); return sfail(s, HWT_ENOMEM, "pricing buffers"); }
     if (upload_batch(b, o, s->stream) != cudaSuccess) { free_batch(b); free_curve(cv); return sfail(s, HWT_ECUDA, "options H2D"); }
     DevYield yc;
     yc.n = cv.n; yc.rate = cv.rate; yc.rate_f = cv.rate_f; yc.day = cv.day;
-    features_kernel<<<(n + 255) / 256, 256, 0, s->stream>>>(dev_view(b, n), yc, s->box, s->fn, X, F, inbox);
+    features_kernel<<<(n + 255) / 256, 256, 0, s->stream>>>(dev_view(b, n), yc, s->box, s->fn, X, F, base, inbox);
     // network on every option (out-of-box rows are overwritten by the tree)
     if ((r = ensure_act(s, std::min(n, kChunk)))) { free_batch(b); free_curve(cv); return r; }
     for (int c0 = 0; c0 < n; c0 += kChunk) {
         const int rows = std::min(kChunk, n - c0);
         if ((r = forward_from(s, X + (size_t)c0 * kInPad, rows))) { free_batch(b); free_curve(cv); return r; }
-        decode_kernel<<<(rows + 255) / 256, 256, 0, s->stream>>>(s->d_z[kLayers - 1], F + c0, inbox + c0, rows, s->ymean,
-                                                               s->ystd, dout + c0);
+        decode_kernel<<<(rows + 255) / 256, 256, 0, s->stream>>>(s->d_z[kLayers - 1], F + c0, base + c0, inbox + c0, rows,
+                                                               s->ymean, s->ystd, dout + c0);
     }
     cudaEventRecord(ev[1], s->stream);
     // route out-of-box options and the judge's sample to the tree
@@ -805,11 +822,31 @@ int hwt_surrogate_price(hwt_surrogate *s, const hwt_options *o, const hwt_yield 
     std::vector<double> errs;
     errs.reserve(m);
     int64_t routed = 0;
+    double worst = 0.0;
     for (int j = 0; j < m; ++j) {
         const int i = hl[j];
-        if (kh[i] == 2) errs.push_back(fabs(out[i] - tree_px[j]));
-        else ++routed;
+        if (kh[i] == 2) {
+            const double e = fabs(out[i] - tree_px[j]);
+            errs.push_back(e);
+            worst = std::max(worst, e != e ? INFINITY : e);
+        } else {
+            ++routed;
+        }
         out[i] = tree_px[j];
+    }
+    int fell_back = 0;
+    double fallback_ms = 0;
+    if (judge_tolerance > 0 && worst > judge_tolerance) {
+        // the network failed its judge on this batch: the tree prices all of it
+        hwt_config tc;
+        memset(&tc, 0, sizeof(tc));
+        tc.mode = tree_mode;
+        tc.use_graph = 1;
+        hwt_stats ts;
+        r = hwt_price_ex(s->ctx, o, y, &tc, out, &ts);
+        if (r) return sfail(s, r, hwt_last_error(s->ctx));
+        fell_back = 1;
+        fallback_ms = ts.total_ms;
     }
     if (stats) {
         float t0 = 0, t1 = 0, t2 = 0;
@@ -828,10 +865,11 @@ int hwt_surrogate_price(hwt_surrogate *s, const hwt_options *o, const hwt_yield 
             stats->judge_p99_abs = e[std::min(e.size() - 1, (size_t)floor(0.99 * (e.size() - 1)))];
             stats->judge_mean_abs = sm / e.size();
         }
+        stats->fell_back = fell_back;
         stats->network_ms = t0;
-        stats->tree_ms = tree_ms;
+        stats->tree_ms = tree_ms + fallback_ms;
         stats->route_ms = t2;
-        stats->total_ms = t1;
+        stats->total_ms = t1 + fallback_ms;
     }
     for (auto &e : ev) cudaEventDestroy(e);
     return HWT_OK;

@@ -28,17 +28,12 @@ def yield_curve():
 def _curve_rate(t_years, rates, days, term_unit=365):
     """Zero rate at t the way common/Domain.hpp:11-46 interpolates it (whole days)."""
     t_days = np.floor(np.asarray(t_years, dtype=np.float64) * term_unit + 0.5).astype(np.int64)
-    out = np.empty(t_days.shape, dtype=np.float64)
-    for idx, td in np.ndenumerate(t_days):
-        if td <= days[0]:
-            out[idx] = rates[0]
-        elif td > days[-1]:
-            out[idx] = rates[-1]
-        else:
-            s = int(np.searchsorted(days, td, side="left"))
-            f = s - 1
-            out[idx] = rates[f] + (td - days[f]) / float(days[s] - days[f]) * (rates[s] - rates[f])
-    return out
+    days = np.asarray(days, dtype=np.int64)
+    rates = np.asarray(rates, dtype=np.float64)
+    s = np.clip(np.searchsorted(days, t_days, side="left"), 1, len(days) - 1)
+    f = s - 1
+    inner = rates[f] + (t_days - days[f]) / (days[s] - days[f]).astype(np.float64) * (rates[s] - rates[f])
+    return np.where(t_days <= days[0], rates[0], np.where(t_days > days[-1], rates[-1], inner))
 
 
 def forward_bond_price(option_maturity, bond_maturity, rates=None, days=None):

@@ -156,7 +156,7 @@ int hwt_price_device(hwt_ctx *ctx, const hwt_options *dev_opts, const hwt_yield 
  * another allocator; latency-bound paths where cudaMalloc/cudaFree, which may
  * synchronise the device, are not allowed): no context, no allocation of any
  * kind; the scratch the pricing kernels need lives in a static device array of
- * the library (about 3.2 MB on every GPU that loads it, until exit).
+ * the library (about 4 MB on every GPU that loads it, until exit).
  *   dev_opts, dev_yield, dev_out_prices: DEVICE pointers of the current device
  *   mode: HWT_BATCHED_FP64, HWT_BATCHED_FP32 or HWT_BATCHED_MIXED
  *   stream: cudaStream_t to run on (NULL: the default stream); the call waits for it
@@ -208,6 +208,9 @@ typedef struct hwt_box {
     double a_min, a_max, sigma_min, sigma_max;
     int32_t steps_min, steps_max;    /* steps per year */
     int32_t term_unit;               /* the only term unit inside the box */
+    int32_t residual;                /* 1: the network learns (tree price - Hull-White closed-form
+                                        price) / forward bond price, a control variate; 0: price /
+                                        forward bond price */
 } hwt_box;
 
 typedef struct hwt_train_config {
@@ -227,6 +230,9 @@ typedef struct hwt_train_stats {
 
 typedef struct hwt_surrogate_stats {
     int64_t n_in_box, n_routed, n_judged;
+    int32_t fell_back;               /* 1: the judge saw an error above the tolerance and the tree
+                                        priced the whole batch */
+    int32_t pad;
     double judge_max_abs, judge_p99_abs, judge_mean_abs; /* |network - tree| on the judged sample */
     double network_ms, tree_ms, route_ms, total_ms;
 } hwt_surrogate_stats;
@@ -241,9 +247,13 @@ int hwt_surrogate_train(hwt_surrogate *s, const hwt_options *samples, const hwt_
                         const hwt_train_config *cfg, hwt_train_stats *stats);
 /* Prices host options: network inside the box, tree (tree_mode: a batched mode)
  * outside it and for the judge's sample (fraction judge_fraction, drawn from
- * `seed`), whose options get the tree price. */
+ * `seed`), whose options get the tree price.  If judge_tolerance > 0 and the
+ * judge's largest |network - tree| exceeds it, the tree prices the whole batch
+ * (stats->fell_back = 1), so the answer is never worse than the tolerance on
+ * the judged sample. */
 int hwt_surrogate_price(hwt_surrogate *s, const hwt_options *opts, const hwt_yield *yield, double judge_fraction,
-                        uint64_t seed, int tree_mode, double *out_prices, hwt_surrogate_stats *stats);
+                        uint64_t seed, int tree_mode, double judge_tolerance, double *out_prices,
+                        hwt_surrogate_stats *stats);
 /* Checkpoint: box, target scaling, weights and Adam state (resume training). */
 int hwt_surrogate_save(const hwt_surrogate *s, const char *path);
 int hwt_surrogate_load(hwt_surrogate *s, const char *path);

@@ -83,6 +83,10 @@ def test_train_route_judge_and_checkpoint(pkg, pricer, orc, tmp_path):
     inb = ~out
     fwd = wl.forward_bond_price(q["option_maturity"], q["bond_maturity"])
     assert np.mean(np.abs(got[inb] - ref[inb]) / fwd[inb]) < 5e-2
+    # a judge tolerance the short-trained network cannot meet sends the batch to the tree
+    fb = s.price(opts, y, judge_fraction=0.05, seed=9, tree_mode=pkg.BATCHED_FP64, judge_tolerance=1e-9)
+    assert s.stats.as_dict()["fell_back"] == 1
+    assert np.max(np.abs(fb - ref)) <= 1e-10 * np.max(np.abs(ref)) + 1e-12
     # checkpoint round trip: same network output after loading into a fresh model
     path = str(tmp_path / "sur.bin")
     s.save(path)
