@@ -226,13 +226,15 @@ def run_ours(args, rank, world, local):
     def device_steps(m, steps, warm):
         for _ in range(warm):
             pricer.price_device(dev_ptr, n, y, dev_out.data_ptr(), m)
-        times, launches, stats = [], 0, None
+        times, launches, stats, kernel = [], 0, None, []
         for _ in range(steps):
             flush_l2()
             st = pricer.price_device(dev_ptr, n, y, dev_out.data_ptr(), m)
             times.append(st.total_ms)
+            kernel.append(st.pricing_ms)  # CUDA events around the pricing kernel, on its stream
             launches += st.kernel_launches
             stats = pkg.Stats.from_buffer_copy(st)
+        stats.pricing_ms = sum(kernel) / len(kernel)
         return times, launches, stats
 
     # CPU baseline first (rank 0, N=1): also gives the FP64 reference prices
@@ -398,7 +400,7 @@ def run_ours(args, rank, world, local):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="uneven_30k", choices=["uniform_1k", "uneven_30k", "skewed_100k"])

@@ -300,7 +300,8 @@ int run_batch(hwt_ctx *c, const DevOptions &dopt, double *dev_out, const hwt_con
     p.s.status = c->d_status;
     p.out = dev_out;
     p.group_threads = cfg.block_size;
-    p.big_threshold = std::min(cfg.big_threshold, kMaxWarpWidth);
+    p.max_warp_k = cfg.mode == HWT_BATCHED_FP64 ? 8 : 16;
+    p.big_threshold = std::min(cfg.big_threshold, 32 * p.max_warp_k);
     p.max_width = kMaxTreeWidth;
     p.record_busy = cfg.record_busy ? 1 : 0;
 
@@ -444,7 +445,7 @@ hwt_ctx *hwt_create(int device, const char *tune_cache)
         memset(&t, 0, sizeof(t));
         t.mode = m;
         t.block_size = kDefaultBlock;
-        t.big_threshold = kDefaultBig;
+        t.big_threshold = m == HWT_BATCHED_FP64 ? kDefaultBig : kMaxWarpWidth;  // float rows fit 512 per warp
         t.use_graph = 1;
     }
     if (tune_cache && *tune_cache) {
@@ -637,7 +638,7 @@ int hwt_autotune(hwt_ctx *c, const hwt_options *o, const hwt_yield *y, int mode,
     if (o->n == 0) return fail(c, HWT_EINVAL, "autotune needs a non-empty batch");
     std::vector<double> out(o->n);
     const int blocks[] = {64, 128, 256, 512};
-    const int bigs[] = {64, 128, 192, 256};
+    const int bigs[] = {128, 256, 384, 512};
     double best_ms = 1e300;
     hwt_config best_cfg = c->tuned[mode];
     for (int b : blocks) {

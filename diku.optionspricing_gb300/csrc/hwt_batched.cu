@@ -58,7 +58,11 @@ struct ModeMix {
     static constexpr bool kFlux = true;
 };
 
-__device__ __forceinline__ int cls_K(int cls) { return cls / kNumL + 1; }
+__device__ __forceinline__ int cls_K(int cls)
+{
+    const int k = cls / kNumL;
+    return k < 6 ? (k < 4 ? k + 1 : (k == 4 ? 6 : 8)) : (k == 6 ? 12 : 16);
+}
 
 // Named barrier `id` over the `nthreads` threads of one tree's warp group (id 0
 // with the whole block is __syncthreads).
@@ -74,33 +78,56 @@ struct Group {
 };
 __device__ __forceinline__ int cls_L(int cls) { return 1 << (cls % kNumL); }
 
-// Smallest L*K >= width with K in {1,2,3,4,6,8}, L in {1..32}; ties go to the
-// larger K (more trees per warp, fewer shuffles per node).  K = 5 and 7 are left
-// out to keep the kernel's code (and its instruction-cache footprint) small.
-__host__ __device__ int pick_warp_class(int width)
+// A warp task's class word: K index q and L index l as q * kNumL + l (bits 0-5),
+// top-edge slot ts (bits 6-9).  Its sort-key slot packs the same triple densely:
+// kNumL * (sum of the K values before K_q) + ts * kNumL + l, so slot % kNumL = l.
+__device__ __forceinline__ int class_slot_base(int q)
 {
-    const int ks[6] = {8, 6, 4, 3, 2, 1};
+    // kNumL x prefix sums of {1, 2, 3, 4, 6, 8, 12, 16}
+    return kNumL * (q < 4 ? q * (q + 1) / 2 : (q == 4 ? 10 : (q == 5 ? 16 : (q == 6 ? 24 : 36))));
+}
+__device__ __forceinline__ int class_slot(int cls)
+{
+    const int q = (cls & 63) / kNumL, l = (cls & 63) % kNumL, ts = (cls >> 6) & 15;
+    return class_slot_base(q) + ts * kNumL + l;
+}
+__device__ __forceinline__ int slot_class(int slot)
+{
+    int q = 0;
+#pragma unroll
+    for (int t = 1; t < kNumK; ++t) q += slot >= class_slot_base(t);
+    const int rest = slot - class_slot_base(q);
+    return (q * kNumL + rest % kNumL) | ((rest / kNumL) << 6);
+}
+
+// Smallest L*K >= width with K in {1,2,3,4,6,8,12,16} (up to max_k), L in
+// {1..32}; ties go to the larger K (more trees per warp, fewer shuffles per
+// node).  K = 5, 7, ... are left out to keep the kernel's code (and its
+// instruction-cache footprint) small.
+__host__ __device__ int pick_warp_class(int width, int max_k)
+{
+    const int ks[kNumK] = {1, 2, 3, 4, 6, 8, 12, 16};  // the K values of kWarpK
     int best = -1, best_slots = 1 << 30;
-    for (int q = 0; q < 6; ++q) {
+    for (int q = kNumK - 1; q >= 0; --q) {
         const int K = ks[q];
+        if (K > max_k) continue;
         for (int l = 0; l < kNumL; ++l) {
             const int slots = K << l;
             if (slots >= width && slots < best_slots) {
                 best_slots = slots;
-                best = (K - 1) * kNumL + l;
+                best = q * kNumL + l;
             }
         }
     }
     return best;
 }
 
-__device__ __forceinline__ int work_bucket(unsigned long long work)
+// Descending log buckets, `per` per octave: heavy work (tall trees) sorts first.
+__device__ __forceinline__ int desc_bucket(double v, int per)
 {
-    // 2 buckets per octave, descending: heavy work sorts first.
-    const double lw = log2((double)work + 1.0);
-    int b = (int)(lw * 2.0);
-    if (b > kWorkBuckets - 1) b = kWorkBuckets - 1;
-    return kWorkBuckets - 1 - b;
+    int b = (int)(log2(v + 1.0) * per);
+    if (b > kBuckets - 1) b = kBuckets - 1;
+    return kBuckets - 1 - b;
 }
 
 // ---------------------------------------------------------------------------
@@ -133,15 +160,18 @@ __global__ void size_kernel(EngineParams p)
             t.term_unit = p.opt.term_unit[i]; t.type = ty; t.edges = (int8_t)s.edges;
             p.s.trees[i] = t;
             nodes = (unsigned long long)s.nodes;
-            const int tier = s.width <= p.big_threshold ? 2 : (s.width <= kMaxBlockK * p.group_threads ? 1 : 0);
+            const int warp_max = p.big_threshold < 32 * p.max_warp_k ? p.big_threshold : 32 * p.max_warp_k;
+            const int tier = s.width <= warp_max ? 2 : (s.width <= kMaxBlockK * p.group_threads ? 1 : 0);
             int cls = 0;
             if (tier == 2) {
-                cls = pick_warp_class(s.width);
+                cls = pick_warp_class(s.width, p.max_warp_k);
                 const int top = s.edges ? (s.width - 1) % cls_K(cls) : 0;  // slot of node W-1
                 cls |= top << 6;
             }
-            const unsigned long long work = (unsigned long long)s.nodes + (unsigned long long)s.width;
-            key = (tier * kWorkBuckets + work_bucket(work)) * kClassSlots + cls;
+            // tiers 0 and 1: one tree per task, by work (4 buckets per octave); tier 2:
+            // trees of one class in lockstep, by height (8 per octave, <= 9% apart)
+            if (tier == 2) key = 2 * kBuckets + desc_bucket((double)s.n, 8) * kClassSlots + class_slot(cls);
+            else key = tier * kBuckets + desc_bucket((double)s.nodes + (double)s.width, 4);
             p.s.keys[i] = key;
             atomicMax(&p.s.status->max_width, s.width);
             atomicMax(&p.s.status->max_height, s.n);
@@ -155,49 +185,71 @@ __global__ void size_kernel(EngineParams p)
 }
 
 // One block: exclusive scans of the key histogram into bin starts and warp-task
-// starts.  kKeyBins / blockDim bins per thread.
-__global__ void scan_kernel(EngineParams p)
+// starts, and the tier sizes.
+__device__ __forceinline__ int bin_tasks(int b, int c)
 {
-    constexpr int T = 1024;
-    constexpr int PER = kKeyBins / T;
-    static_assert(PER * T == kKeyBins, "bins must split evenly over the scan threads");
-    __shared__ int s_a[T], s_b[T];
-    const int tid = threadIdx.x;
-    int cnt[PER], tsk[PER];
+    if (b < 2 * kBuckets || c == 0) return 0;  // tiers 0 and 1: no warp tasks
+    const int G = 32 / cls_L((b - 2 * kBuckets) % kClassSlots);  // slot % kNumL is the L index
+    return (c + G - 1) / G;
+}
+
+__device__ __forceinline__ int warp_inclusive_scan(int v, int lane)
+{
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const int u = __shfl_up_sync(FULL, v, off);
+        if (lane >= off) v += u;
+    }
+    return v;
+}
+
+// Each warp owns a contiguous run of bins and reads it 32 bins at a time
+// (coalesced): pass 1 sums the run, warp 0 scans the 32 run sums, pass 2 scans
+// each 32-bin tile with shuffles and writes the starts.
+__global__ void __launch_bounds__(1024) scan_kernel(EngineParams p)
+{
+    constexpr int T = 1024, NW = T / 32;
+    constexpr int SEG = (kKeyBins + NW - 1) / NW;
+    __shared__ int s_a[NW], s_b[NW];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int b0 = warp * SEG, b1 = min(kKeyBins, b0 + SEG);
     int sa = 0, sb = 0;
-    for (int q = 0; q < PER; ++q) {
-        const int b = tid * PER + q;
+    for (int b = b0 + lane; b < b1; b += 32) {
         const int c = p.s.hist[b];
-        const bool warp = b >= 2 * kTierBins;
-        int t = 0;
-        if (warp && c > 0) {
-            const int G = 32 / cls_L((b % kClassSlots) & 63);  // low 6 bits of the class: K and L
-            t = (c + G - 1) / G;
+        sa += c;
+        sb += bin_tasks(b, c);
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        sa += __shfl_xor_sync(FULL, sa, off);
+        sb += __shfl_xor_sync(FULL, sb, off);
+    }
+    if (lane == 0) { s_a[warp] = sa; s_b[warp] = sb; }
+    __syncthreads();
+    if (warp == 0) {
+        const int a = s_a[lane], t = s_b[lane];
+        const int ia = warp_inclusive_scan(a, lane), it = warp_inclusive_scan(t, lane);
+        s_a[lane] = ia - a;
+        s_b[lane] = it - t;
+        if (lane == 31) p.s.status->n_warp_tasks = it;
+    }
+    __syncthreads();
+    int ea = s_a[warp], eb = s_b[warp];
+    for (int base = b0; base < b1; base += 32) {
+        const int b = base + lane;
+        const int c = b < b1 ? p.s.hist[b] : 0;
+        const int t = b < b1 ? bin_tasks(b, c) : 0;
+        const int ic = warp_inclusive_scan(c, lane), it = warp_inclusive_scan(t, lane);
+        if (b < b1) {
+            p.s.bin_start[b] = ea + ic - c;
+            p.s.task_start[b] = eb + it - t;
         }
-        cnt[q] = c; tsk[q] = t; sa += c; sb += t;
+        ea += __shfl_sync(FULL, ic, 31);
+        eb += __shfl_sync(FULL, it, 31);
     }
-    s_a[tid] = sa; s_b[tid] = sb;
+    // tier boundaries (global writes of the block are visible to it after the barrier)
     __syncthreads();
-    for (int off = 1; off < T; off <<= 1) {
-        int va = 0, vb = 0;
-        if (tid >= off) { va = s_a[tid - off]; vb = s_b[tid - off]; }
-        __syncthreads();
-        s_a[tid] += va; s_b[tid] += vb;
-        __syncthreads();
-    }
-    int ea = s_a[tid] - sa, eb = s_b[tid] - sb;
-    for (int q = 0; q < PER; ++q) {
-        const int b = tid * PER + q;
-        p.s.bin_start[b] = ea;
-        p.s.task_start[b] = eb;
-        ea += cnt[q]; eb += tsk[q];
-    }
-    if (tid == T - 1) p.s.status->n_warp_tasks = s_b[T - 1];
-    // tier boundaries: options before the first tier-1 and tier-2 bins (global
-    // writes of the block are visible to it after the barrier)
-    __syncthreads();
-    if (tid == 0) {
-        const int t1 = p.s.bin_start[kTierBins], t2 = p.s.bin_start[2 * kTierBins];
+    if (threadIdx.x == 0) {
+        const int t1 = p.s.bin_start[kBuckets], t2 = p.s.bin_start[2 * kBuckets];
         p.s.status->n_cta = t1;
         p.s.status->n_group = t2 - t1;
     }
@@ -214,8 +266,8 @@ __global__ void scatter_kernel(EngineParams p)
     const int q = atomicAdd(&p.s.fill[key], 1);
     const int pos = p.s.bin_start[key] + q;
     p.s.order[pos] = i;
-    if (key >= 2 * kTierBins) {
-        const int cls = key % kClassSlots;
+    if (key >= 2 * kBuckets) {
+        const int cls = slot_class((key - 2 * kBuckets) % kClassSlots);
         const int G = 32 / cls_L(cls & 63);
         if (q % G == 0) {
             WarpTask t;
@@ -232,9 +284,11 @@ __global__ void scatter_kernel(EngineParams p)
 // Per-thread tree slice: K consecutive nodes k0 .. k0+K-1 of one tree.
 // ---------------------------------------------------------------------------
 
-template <typename R, int K>
-struct Ext {  // e[s + 2] is node k0 + s; e[0..1] left neighbours, e[K+2..K+3] right
-    R e[K + 4];
+// Values of the two nodes left of a thread's slice (l1 = k0-1, l2 = k0-2) and the
+// two right of it (r1 = k0+K, r2 = k0+K+1), all from the current row.
+template <typename R>
+struct Halo {
+    R l1, l2, r1, r2;
 };
 
 template <class Mode, int K>
@@ -242,13 +296,15 @@ struct Slice {
     typedef typename Mode::Row R;
     typedef typename Mode::Scal S;
 
-    R r[K];                 // current row
-    R c0[K], c1[K], c2[K];  // FP64: fa/fb/fc or ba/bb/bc.  Flux: up, down, g.
-    R cl, cr;               // flux: up of node k0-1, down of node k0+K
+    R r[K];                 // current row, nodes k0 .. k0+K-1
+    R c0[K], c1[K], c2[K];  // FP64: fa/fb/fc or ba/bb/bc.  Flux: up, -down of the next node, g.
+    R cl, cd0;              // flux: up of node k0-1, -down of node k0
     // Edge jumps (+-jmax branch two nodes away).  Nodes 0 and 2 sit at compile-time
-    // slots (0 and 2 % K); node W-1 sits at slot ts = (W-1) % K, which is the same
-    // for every tree a warp prices (it is part of the warp class), so the top
-    // edge is handled by one uniform switch per step instead of a test per slot.
+    // slots (0 and 2 % K) and their terms are part of the step loop; node W-1 sits
+    // at slot ts = (W-1) % K, known only at run time, so the top-edge terms are
+    // applied after the in-place step from old values saved before it, through a
+    // switch on ts.  Warp tasks group trees by ts (it is part of the warp class),
+    // which keeps the switch uniform across the warp.
     R jlo, jhi;             // FP64: jump coefficient times the receiving node's G; flux: pu_b, pd_c
     bool n0, n2, nw1, nw3;  // this thread owns node 0 / 2 / W-1 / W-3 of an edged tree
     int ts;
@@ -290,6 +346,7 @@ struct Slice {
             }
         } else {
             const float Mf = (float)t.M, drdt = (float)(t.dr * t.dt);
+            float dn[K];  // down coefficient of node k0+s
 #pragma unroll
             for (int s = 0; s < K; ++s) {
                 const int k = k0 + s;
@@ -309,11 +366,12 @@ struct Slice {
                         d = 1.0f / 6.0f + (x2 - x) * 0.5f;  // pd_a
                     }
                 }
-                c0[s] = u; c1[s] = d; c2[s] = g;
+                c0[s] = u; dn[s] = d; c2[s] = g;
                 r[s] = (k == jc) ? 1.f : 0.f;
             }
             // neighbours' up (node k0-1) and down (node k0+K) coefficients
-            cl = 0.f; cr = 0.f;
+            float cr = 0.f;
+            cl = 0.f;
             {
                 const int kl = k0 - 1, kr = k0 + K;
                 if (kl >= 0 && kl < W) {
@@ -327,6 +385,11 @@ struct Slice {
                     cr = (j == -jmax) ? 0.f : (j == jmax ? (-1.0f / 3.0f - x2 - 2.0f * x) : 1.0f / 6.0f + (x2 - x) * 0.5f);
                 }
             }
+            // c1 holds the next node's down coefficient, negated: the net flux from
+            // node k to node k+1 is then fma(c0, r_k, c1 r_{k+1})
+            cd0 = -dn[0];
+#pragma unroll
+            for (int s = 0; s < K; ++s) c1[s] = -((s < K - 1) ? dn[s + 1] : cr);
             if (t.edges) {
                 const float xb = (float)(-jmax) * Mf, xt = (float)jmax * Mf;
                 jlo = 1.0f / 6.0f + (xb * xb - xb) * 0.5f;  // pu_b: bottom edge jumps up two
@@ -364,127 +427,186 @@ struct Slice {
         }
     }
 
-    // Top-edge terms with the slot of node W-1 known at compile time.
+    // Old value of the node `d` nodes away from slot S (d in -2..2), from the row
+    // or the halo.
+    template <int S, int D>
+    __device__ __forceinline__ R old_at(const Halo<R> &h) const
+    {
+        constexpr int q = S + D;
+        if constexpr (q >= 0 && q < K) return r[q];
+        else if constexpr (q == -1) return h.l1;
+        else if constexpr (q == -2) return h.l2;
+        else if constexpr (q == K) return h.r1;
+        else return h.r2;
+    }
+
+    // Old values the top-edge terms need, per compile-time slot TS of node W-1.
+    // Seen from the thread owning node W-1: w1 = node W-1, w3 = node W-3.  Seen
+    // from the thread owning node W-3 (possibly the previous thread): w1b = node W-1.
     template <int TS>
-    __device__ __forceinline__ void top_forward(R (&v)[K], const Ext<R, K> &x) const
+    __device__ __forceinline__ void save_top(const Halo<R> &h, R &w1, R &w3, R &w1b) const
     {
         if constexpr (TS < K) {
             constexpr int S3 = (TS + 2 * K - 2) % K;  // slot of node W-3
-            if constexpr (Mode::kFlux) {
-                if (nw1) v[TS] = fma(-jhi, r[TS], v[TS]);
-            }
-            if (nw3) v[S3] = fma(jhi, x.e[S3 + 4], v[S3]);
+            w1 = r[TS];
+            w3 = old_at<TS, -2>(h);
+            w1b = old_at<S3, 2>(h);
         }
     }
 
-    template <int TS>
-    __device__ __forceinline__ void top_backward(R (&v)[K], const Ext<R, K> &x) const
+    __device__ __forceinline__ void top_values(const Halo<R> &h, R &w1, R &w3, R &w1b) const
+    {
+        switch (ts) {
+            case 0: save_top<0>(h, w1, w3, w1b); break;
+            case 1: save_top<1>(h, w1, w3, w1b); break;
+            case 2: save_top<2>(h, w1, w3, w1b); break;
+            case 3: save_top<3>(h, w1, w3, w1b); break;
+            case 4: save_top<4>(h, w1, w3, w1b); break;
+            case 5: save_top<5>(h, w1, w3, w1b); break;
+            case 6: save_top<6>(h, w1, w3, w1b); break;
+            case 7: save_top<7>(h, w1, w3, w1b); break;
+            case 8: save_top<8>(h, w1, w3, w1b); break;
+            case 9: save_top<9>(h, w1, w3, w1b); break;
+            case 10: save_top<10>(h, w1, w3, w1b); break;
+            case 11: save_top<11>(h, w1, w3, w1b); break;
+            case 12: save_top<12>(h, w1, w3, w1b); break;
+            case 13: save_top<13>(h, w1, w3, w1b); break;
+            case 14: save_top<14>(h, w1, w3, w1b); break;
+            default: save_top<15>(h, w1, w3, w1b); break;
+        }
+    }
+
+    // Adds c to the step's pre-discount value at slot S: the row holds
+    // (1+g) v (flux) or the finished value (FP64, c already carries G).
+    template <int S>
+    __device__ __forceinline__ void add_at(R c)
+    {
+        if constexpr (Mode::kFlux) r[S] += fma(c2[S], c, c);
+        else r[S] += c;
+    }
+
+    template <int TS, bool FWD>
+    __device__ __forceinline__ void top_fix(R w1, R w3, R w1b)
     {
         if constexpr (TS < K) {
-            if constexpr (Mode::kFlux) {
-                if (nw1) v[TS] = fma(jhi, x.e[TS] - x.e[TS + 2], v[TS]);
+            constexpr int S3 = (TS + 2 * K - 2) % K;
+            if constexpr (FWD) {
+                if constexpr (Mode::kFlux) {
+                    if (nw1) add_at<TS>(-jhi * w1);
+                }
+                if (nw3) add_at<S3>(jhi * w1b);
             } else {
-                if (nw1) v[TS] = fma(jhi, x.e[TS], v[TS]);
+                if constexpr (Mode::kFlux) {
+                    if (nw1) add_at<TS>(jhi * (w3 - w1));
+                } else {
+                    if (nw1) add_at<TS>(jhi * w3);
+                }
             }
         }
     }
 
-    __device__ __forceinline__ void edges_forward(R (&v)[K], const Ext<R, K> &x) const
+    template <bool FWD>
+    __device__ __forceinline__ void top_fixes(R w1, R w3, R w1b)
+    {
+        switch (ts) {
+            case 0: top_fix<0, FWD>(w1, w3, w1b); break;
+            case 1: top_fix<1, FWD>(w1, w3, w1b); break;
+            case 2: top_fix<2, FWD>(w1, w3, w1b); break;
+            case 3: top_fix<3, FWD>(w1, w3, w1b); break;
+            case 4: top_fix<4, FWD>(w1, w3, w1b); break;
+            case 5: top_fix<5, FWD>(w1, w3, w1b); break;
+            case 6: top_fix<6, FWD>(w1, w3, w1b); break;
+            case 7: top_fix<7, FWD>(w1, w3, w1b); break;
+            case 8: top_fix<8, FWD>(w1, w3, w1b); break;
+            case 9: top_fix<9, FWD>(w1, w3, w1b); break;
+            case 10: top_fix<10, FWD>(w1, w3, w1b); break;
+            case 11: top_fix<11, FWD>(w1, w3, w1b); break;
+            case 12: top_fix<12, FWD>(w1, w3, w1b); break;
+            case 13: top_fix<13, FWD>(w1, w3, w1b); break;
+            case 14: top_fix<14, FWD>(w1, w3, w1b); break;
+            default: top_fix<15, FWD>(w1, w3, w1b); break;
+        }
+    }
+
+    // One forward step, in place: r <- G o gather(r).
+    __device__ __forceinline__ void forward_step(const Halo<R> &h, bool edge_live)
     {
         constexpr int S2 = 2 % K;  // slot of node 2
-        if constexpr (Mode::kFlux) {
-            if (n0) v[0] = fma(-jlo, r[0], v[0]);
-        }
-        if (n2) v[S2] = fma(jlo, x.e[S2], v[S2]);
-        switch (ts) {
-            case 0: top_forward<0>(v, x); break;
-            case 1: top_forward<1>(v, x); break;
-            case 2: top_forward<2>(v, x); break;
-            case 3: top_forward<3>(v, x); break;
-            case 4: top_forward<4>(v, x); break;
-            case 5: top_forward<5>(v, x); break;
-            case 6: top_forward<6>(v, x); break;
-            default: top_forward<7>(v, x); break;
-        }
-    }
-
-    __device__ __forceinline__ void edges_backward(R (&v)[K], const Ext<R, K> &x) const
-    {
-        if constexpr (Mode::kFlux) {
-            if (n0) v[0] = fma(jlo, x.e[4] - x.e[2], v[0]);
+        R w1 = (R)0, w3 = (R)0, w1b = (R)0;
+        // bottom-edge jump weights of this thread's nodes 0 and 2 (zero elsewhere)
+        const R jout = (edge_live && n0) ? jlo : (R)0;
+        const R jin = (edge_live && n2) ? jlo : (R)0;
+        const R src2 = old_at<S2, -2>(h);  // node 0 seen from node 2 (read before the update)
+        if (edge_live) top_values(h, w1, w3, w1b);
+        if constexpr (!Mode::kFlux) {
+            R prev = h.l1;
+#pragma unroll
+            for (int s = 0; s < K; ++s) {
+                const R cur = r[s];
+                const R nxt = (s < K - 1) ? r[s + 1] : h.r1;
+                R v = c0[s] * prev;
+                v = fma(c1[s], cur, v);
+                v = fma(c2[s], nxt, v);
+                if (s == S2) v = fma(jin, src2, v);
+                r[s] = v;
+                prev = cur;
+            }
         } else {
-            if (n0) v[0] = fma(jlo, x.e[4], v[0]);
+            // net flux e_k = up_k r_k - down_{k+1} r_{k+1} across each link, computed
+            // once and used by both ends (the row's sum is kept exactly)
+            R eprev = fma(cl, h.l1, cd0 * r[0]);
+#pragma unroll
+            for (int s = 0; s < K; ++s) {
+                const R cur = r[s];
+                const R nxt = (s < K - 1) ? r[s + 1] : h.r1;
+                const R e = fma(c0[s], cur, c1[s] * nxt);
+                R v = cur + (eprev - e);
+                if (s == 0) v = fma(-jout, cur, v);
+                if (s == S2) v = fma(jin, src2, v);
+                r[s] = fma(c2[s], v, v);
+                eprev = e;
+            }
         }
-        switch (ts) {
-            case 0: top_backward<0>(v, x); break;
-            case 1: top_backward<1>(v, x); break;
-            case 2: top_backward<2>(v, x); break;
-            case 3: top_backward<3>(v, x); break;
-            case 4: top_backward<4>(v, x); break;
-            case 5: top_backward<5>(v, x); break;
-            case 6: top_backward<6>(v, x); break;
-            default: top_backward<7>(v, x); break;
-        }
+        if (edge_live) top_fixes<true>(w1, w3, w1b);
     }
 
-    // One forward step: r <- G o gather(r), reading neighbours from x.
-    __device__ __forceinline__ void forward_step(const Ext<R, K> &x, bool edge_live)
+    // One backward step, in place: r <- G o P r (flux: on the deviation from `base`).
+    __device__ __forceinline__ void backward_step(const Halo<R> &h, bool edge_live, R base)
     {
-        R v[K];
+        R w1 = (R)0, w3 = (R)0, w1b = (R)0;
+        const R j0 = (edge_live && n0) ? jlo : (R)0;  // bottom-edge jump weight of node 0
+        const R o2 = old_at<0, 2>(h);                 // node 2 seen from node 0 (read before the update)
+        if (edge_live) top_values(h, w1, w3, w1b);
+        R prev = h.l1;
         if constexpr (!Mode::kFlux) {
 #pragma unroll
             for (int s = 0; s < K; ++s) {
-                R t = c0[s] * x.e[s + 1];
-                t = fma(c1[s], x.e[s + 2], t);
-                t = fma(c2[s], x.e[s + 3], t);
-                v[s] = t;
+                const R cur = r[s];
+                const R nxt = (s < K - 1) ? r[s + 1] : h.r1;
+                R v = c0[s] * nxt;
+                v = fma(c1[s], cur, v);
+                v = fma(c2[s], prev, v);
+                if (s == 0) v = fma(j0, o2, v);
+                r[s] = v;
+                prev = cur;
             }
-            if (edge_live) edges_forward(v, x);
-#pragma unroll
-            for (int s = 0; s < K; ++s) r[s] = v[s];
         } else {
-            R f[K], h[K];
-#pragma unroll
-            for (int s = 0; s < K; ++s) { f[s] = c0[s] * r[s]; h[s] = c1[s] * r[s]; }
-            const R fl = cl * x.e[1], hr = cr * x.e[K + 2];
+            // differences D_k = r_{k+1} - r_k, each computed once:
+            // v_k = r_k + up_k D_k - down_k D_{k-1}
+            R dprev = r[0] - prev;
 #pragma unroll
             for (int s = 0; s < K; ++s) {
-                const R fin = (s == 0) ? fl : f[s - 1];
-                const R hin = (s == K - 1) ? hr : h[s + 1];
-                v[s] = (r[s] + (fin - f[s])) + (hin - h[s]);
+                const R cur = r[s];
+                const R nxt = (s < K - 1) ? r[s + 1] : h.r1;
+                const R d = nxt - cur;
+                const R ndown = (s == 0) ? cd0 : c1[s - 1];  // -down of this node
+                R v = cur + fma(c0[s], d, ndown * dprev);
+                if (s == 0) v = fma(j0, o2 - cur, v);
+                r[s] = fma(c2[s], v + base, v);
+                dprev = d;
             }
-            if (edge_live) edges_forward(v, x);
-#pragma unroll
-            for (int s = 0; s < K; ++s) r[s] = fma(c2[s], v[s], v[s]);
         }
-    }
-
-    // One backward step: r <- G o P r (flux: on the deviation from `base`).
-    __device__ __forceinline__ void backward_step(const Ext<R, K> &x, bool edge_live, R base)
-    {
-        R v[K];
-        if constexpr (!Mode::kFlux) {
-#pragma unroll
-            for (int s = 0; s < K; ++s) {
-                R t = c0[s] * x.e[s + 3];
-                t = fma(c1[s], x.e[s + 2], t);
-                t = fma(c2[s], x.e[s + 1], t);
-                v[s] = t;
-            }
-            if (edge_live) edges_backward(v, x);
-#pragma unroll
-            for (int s = 0; s < K; ++s) r[s] = v[s];
-        } else {
-#pragma unroll
-            for (int s = 0; s < K; ++s) {
-                const R d0 = x.e[s + 2];
-                const R up = x.e[s + 3] - d0, dn = x.e[s + 1] - d0;
-                v[s] = d0 + fma(c0[s], up, c1[s] * dn);
-            }
-            if (edge_live) edges_backward(v, x);
-#pragma unroll
-            for (int s = 0; s < K; ++s) r[s] = fma(c2[s], v[s] + base, v[s]);
-        }
+        if (edge_live) top_fixes<false>(w1, w3, w1b);
     }
 
     __device__ __forceinline__ S partial_sum(int k0, int W) const
@@ -517,40 +639,34 @@ struct Slice {
     }
 };
 
+// Halo within a warp segment of L lanes holding one tree.  The shuffles use width
+// L, so a lane never reads another tree: at the segment ends it gets its own
+// values back, which only ever meet a zero coefficient (the tree's outer nodes
+// branch nowhere outward) or feed nodes outside the active cone.  The second
+// neighbours are needed only while the edge jumps are live.
 template <typename R, int K>
-__device__ __forceinline__ void fill_ext(Ext<R, K> &x, const R (&r)[K])
+__device__ __forceinline__ Halo<R> exchange_warp(const R (&r)[K], int L, bool two)
 {
-#pragma unroll
-    for (int s = 0; s < K; ++s) x.e[s + 2] = r[s];
-}
-
-// Neighbour values within a warp segment of L lanes holding one tree.  The
-// shuffles use width L, so a lane never reads another tree: at the segment ends
-// it gets its own values back, which only ever meet a zero coefficient (the
-// tree's outer nodes branch nowhere outward) or feed nodes outside the active
-// cone.
-template <typename R, int K>
-__device__ __forceinline__ void exchange_warp(Ext<R, K> &x, const R (&r)[K], int L)
-{
-    fill_ext(x, r);
+    Halo<R> h;
     if constexpr (K >= 2) {
-        x.e[1] = __shfl_up_sync(FULL, r[K - 1], 1, L);
-        x.e[0] = __shfl_up_sync(FULL, r[K - 2], 1, L);
-        x.e[K + 2] = __shfl_down_sync(FULL, r[0], 1, L);
-        x.e[K + 3] = __shfl_down_sync(FULL, r[1], 1, L);
+        h.l1 = __shfl_up_sync(FULL, r[K - 1], 1, L);
+        h.r1 = __shfl_down_sync(FULL, r[0], 1, L);
+        h.l2 = two ? __shfl_up_sync(FULL, r[K - 2], 1, L) : (R)0;
+        h.r2 = two ? __shfl_down_sync(FULL, r[1], 1, L) : (R)0;
     } else {
-        x.e[1] = __shfl_up_sync(FULL, r[0], 1, L);
-        x.e[0] = __shfl_up_sync(FULL, r[0], 2, L);
-        x.e[3] = __shfl_down_sync(FULL, r[0], 1, L);
-        x.e[4] = __shfl_down_sync(FULL, r[0], 2, L);
+        h.l1 = __shfl_up_sync(FULL, r[0], 1, L);
+        h.r1 = __shfl_down_sync(FULL, r[0], 1, L);
+        h.l2 = two ? __shfl_up_sync(FULL, r[0], 2, L) : (R)0;
+        h.r2 = two ? __shfl_down_sync(FULL, r[0], 2, L) : (R)0;
     }
+    return h;
 }
 
-// Neighbour values across a whole block: shuffles inside each warp, the first and
-// last two nodes of every warp through shared memory (double buffered, so one
-// barrier per step is enough).
+// Halo across a warp group: shuffles inside each warp, the first and last two
+// nodes of every warp through shared memory (double buffered, so one barrier per
+// step is enough).
 template <typename R, int K>
-__device__ __forceinline__ void exchange_block(Ext<R, K> &x, const R (&r)[K], R *sh, int parity, const Group &gr)
+__device__ __forceinline__ Halo<R> exchange_block(const R (&r)[K], R *sh, int parity, const Group &gr)
 {
     // shared slots are indexed by the warp's index in the block; neighbours are
     // the adjacent warps of the same group
@@ -565,29 +681,30 @@ __device__ __forceinline__ void exchange_block(Ext<R, K> &x, const R (&r)[K], R 
         if (lane >= 30) buf[warp * 4 + lane - 28] = r[0];
     }
     tree_barrier(gr.bar, gr.nthreads);
-    exchange_warp<R, K>(x, r, 32);
+    Halo<R> h = exchange_warp<R, K>(r, 32, true);
     const bool hasl = warp > w0, hasr = warp + 1 < w1;
     if constexpr (K >= 2) {
         if (lane == 0) {
-            x.e[1] = hasl ? buf[(warp - 1) * 4 + 3] : (R)0;
-            x.e[0] = hasl ? buf[(warp - 1) * 4 + 2] : (R)0;
+            h.l1 = hasl ? buf[(warp - 1) * 4 + 3] : (R)0;
+            h.l2 = hasl ? buf[(warp - 1) * 4 + 2] : (R)0;
         }
         if (lane == 31) {
-            x.e[K + 2] = hasr ? buf[(warp + 1) * 4 + 0] : (R)0;
-            x.e[K + 3] = hasr ? buf[(warp + 1) * 4 + 1] : (R)0;
+            h.r1 = hasr ? buf[(warp + 1) * 4 + 0] : (R)0;
+            h.r2 = hasr ? buf[(warp + 1) * 4 + 1] : (R)0;
         }
     } else {
         if (lane == 0) {
-            x.e[1] = hasl ? buf[(warp - 1) * 4 + 3] : (R)0;
-            x.e[0] = hasl ? buf[(warp - 1) * 4 + 2] : (R)0;
+            h.l1 = hasl ? buf[(warp - 1) * 4 + 3] : (R)0;
+            h.l2 = hasl ? buf[(warp - 1) * 4 + 2] : (R)0;
         }
-        if (lane == 1) x.e[0] = hasl ? buf[(warp - 1) * 4 + 3] : (R)0;
+        if (lane == 1) h.l2 = hasl ? buf[(warp - 1) * 4 + 3] : (R)0;
         if (lane == 31) {
-            x.e[3] = hasr ? buf[(warp + 1) * 4 + 0] : (R)0;
-            x.e[4] = hasr ? buf[(warp + 1) * 4 + 1] : (R)0;
+            h.r1 = hasr ? buf[(warp + 1) * 4 + 0] : (R)0;
+            h.r2 = hasr ? buf[(warp + 1) * 4 + 1] : (R)0;
         }
-        if (lane == 30) x.e[4] = hasr ? buf[(warp + 1) * 4 + 0] : (R)0;
+        if (lane == 30) h.r2 = hasr ? buf[(warp + 1) * 4 + 0] : (R)0;
     }
+    return h;
 }
 
 // Scalars of one tree after its forward sweep.
@@ -646,13 +763,12 @@ __device__ void price_warp_task(const EngineParams &p, const WarpTask &task)
     const int k0 = lis * K;
     const int W = t.width;
     Slice<Mode, K> sl;
-    Ext<R, K> x;
 
     // ---- forward sweep: rows 1 .. n-1; the sums of rows m-1 and n-1 are kept.
     // Rows of trees that are done keep being updated (their segment is isolated by
     // the width-L shuffles), so the step loop carries no per-tree predicates.
     sl.setup_forward(t, k0);
-    sl.ts = (task.cls >> 6) & 7;  // the warp's common top-edge slot
+    sl.ts = (task.cls >> 6) & 15;  // the warp's common top-edge slot
     const int e_f = (int)__reduce_min_sync(FULL, (valid && t.edges) ? (unsigned)t.jmax : NONE);
     const int rm = (t.m >= 2 && t.m < t.n) ? t.m - 1 : -1;  // row m-1 (row 0 sums to 1)
     const int rn = (t.n >= 2) ? t.n - 1 : -1;               // row n-1
@@ -666,8 +782,9 @@ __device__ void price_warp_task(const EngineParams &p, const WarpTask &task)
         const int ev = (int)__reduce_min_sync(FULL, mine);  // next row whose sum someone needs
         const int stop = ev < fsteps ? ev : fsteps;          // steps i .. stop-1 produce rows .. stop
         for (; i < stop; ++i) {
-            exchange_warp<R, K>(x, sl.r, L);
-            sl.forward_step(x, i >= e_f);
+            const bool live = i >= e_f;
+            const Halo<R> h = exchange_warp<R, K>(sl.r, L, live);
+            sl.forward_step(h, live);
         }
         if (ev <= fsteps) {
             S acc = sl.partial_sum(k0, W);
@@ -693,8 +810,9 @@ __device__ void price_warp_task(const EngineParams &p, const WarpTask &task)
         const int pm = (int)__reduce_max_sync(FULL, (pays && t.m <= i) ? (unsigned)(t.m + 1) : 0u) - 1;
         const int lo = pm > 0 ? pm : 0;
         for (; i >= lo; --i) {
-            exchange_warp<R, K>(x, sl.r, L);
-            sl.backward_step(x, i >= e_b, base);
+            const bool live = i >= e_b;
+            const Halo<R> h = exchange_warp<R, K>(sl.r, L, live);
+            sl.backward_step(h, live, base);
             if (i >= n_min && i >= t.n) {
 #pragma unroll
                 for (int s = 0; s < K; ++s) sl.r[s] = (k0 + s < W) ? face : (R)0;
@@ -733,19 +851,18 @@ __device__ void price_block_tree(const EngineParams &p, const Tree &t, const Gro
     const int W = t.width, jc = t.jc;
     const int wk0 = warp * 32 * K, wk1 = wk0 + 32 * K;  // this warp's node range
     Slice<Mode, K> sl;
-    Ext<R, K> x;
     int parity = 0;
 
     sl.setup_forward(t, k0);
     S sum_m1 = (S)1, sum_n1 = (S)1;
     const int fsteps = t.n > 1 ? t.n - 1 : 0;
     for (int i = 0; i < fsteps; ++i) {
-        exchange_block<R, K>(x, sl.r, sh_x, parity, gr);
+        const Halo<R> h = exchange_block<R, K>(sl.r, sh_x, parity, gr);
         parity ^= 1;
         // rows outside the cone of row i+1 stay zero: skip whole warps there
         const int reach = (i + 1 < jc) ? i + 1 : jc;
         const bool active = wk1 > jc - reach && wk0 <= jc + reach && wk0 < W;
-        if (active) sl.forward_step(x, t.edges && i >= t.jmax);
+        if (active) sl.forward_step(h, t.edges && i >= t.jmax);
         const int row = i + 1;
         if (row == t.m - 1 || row == t.n - 1) {
             S acc = sl.partial_sum(k0, W);
@@ -764,11 +881,11 @@ __device__ void price_block_tree(const EngineParams &p, const Tree &t, const Gro
     sl.setup_backward(t, k0);
     R base = Mode::kFlux ? (R)100 : (R)0;
     for (int i = t.n - 1; i >= 0; --i) {
-        exchange_block<R, K>(x, sl.r, sh_x, parity, gr);
+        const Halo<R> h = exchange_block<R, K>(sl.r, sh_x, parity, gr);
         parity ^= 1;
         const int reach = (i < t.jmax) ? i : t.jmax;
         const bool active = wk1 > jc - reach && wk0 <= jc + reach && wk0 < W;
-        if (active) sl.backward_step(x, t.edges && i >= t.jmax, base);
+        if (active) sl.backward_step(h, t.edges && i >= t.jmax, base);
         if (i == t.m) {
             sl.payoff(sc.kappa, base, t.X, t.type);
             base = (R)0;
@@ -857,7 +974,13 @@ __global__ void __launch_bounds__(kPricingThreads, 1) price_kernel(EngineParams 
             case 3: price_warp_task<Mode, 3>(p, wt); break;
             case 4: price_warp_task<Mode, 4>(p, wt); break;
             case 6: price_warp_task<Mode, 6>(p, wt); break;
-            default: price_warp_task<Mode, 8>(p, wt); break;
+            case 8: price_warp_task<Mode, 8>(p, wt); break;
+            default:
+                if constexpr (Mode::kFlux) {
+                    if (cls_K(wt.cls & 63) == 12) price_warp_task<Mode, 12>(p, wt);
+                    else price_warp_task<Mode, 16>(p, wt);
+                }
+                break;
         }
     }
     if (p.record_busy) {
@@ -874,9 +997,9 @@ __global__ void __launch_bounds__(kPricingThreads, 1) price_kernel(EngineParams 
 
 int warp_class_of(int width, int *K, int *L)
 {
-    const int c = pick_warp_class(width);
+    const int c = pick_warp_class(width, 16);
     if (c < 0) return -1;
-    if (K) *K = c / kNumL + 1;
+    if (K) *K = kWarpK[c / kNumL];
     if (L) *L = 1 << (c % kNumL);
     return c;
 }

@@ -52,24 +52,25 @@ struct WarpTask {
 };
 
 // Warp classes: L lanes per tree (power of two), K nodes per lane; L*K >= width.
-constexpr int kWarpK[] = {1, 2, 3, 4, 5, 6, 7, 8};
+// class = index of K in kWarpK * kNumL + log2(L); FP64 rows stop at K = 8.
+constexpr int kWarpK[] = {1, 2, 3, 4, 6, 8, 12, 16};
 constexpr int kNumK = 8;
 constexpr int kNumL = 6;                       // L = 1, 2, 4, 8, 16, 32
-constexpr int kNumWarpClasses = kNumK * kNumL; // class = (K-1) * kNumL + log2(L)
-constexpr int kMaxWarpWidth = 32 * 8;          // wider trees go to a whole block
+constexpr int kNumWarpClasses = kNumK * kNumL;
+constexpr int kMaxWarpWidth = 32 * 16;         // wider trees go to warp groups or whole blocks
 constexpr int kMaxBlockK = 8;                  // nodes per thread for block trees
 constexpr int kPricingThreads = 512;           // threads of every pricing block
 constexpr int kMaxTreeWidth = kMaxBlockK * kPricingThreads;  // widest tree accepted
 
-// Sort keys: [tier][work bucket][warp class].  Tier 0: trees wider than a group
-// can hold, priced by the whole block; tier 1: priced by a group of warps;
-// tier 2: small trees packed into warp tasks.  Descending work inside each tier.
-// A warp class is K and L (6 bits) and the slot of the top edge node (3 bits).
-constexpr int kWorkBuckets = 64;
-constexpr int kTiers = 3;
-constexpr int kClassSlots = 512;
-constexpr int kKeyBins = kTiers * kWorkBuckets * kClassSlots;
-constexpr int kTierBins = kWorkBuckets * kClassSlots;
+// Sort keys.  Tier 0 (trees wider than a group can hold, priced by the whole
+// block): bins [0, kBuckets) by work; tier 1 (priced by a group of warps): bins
+// [kBuckets, 2 kBuckets) by work; tier 2 (small trees packed into warp tasks):
+// 2 kBuckets + height bucket * kClassSlots + class slot, one slot per warp class
+// (K, L) and slot ts < K of the top edge node: 6 (L values) x (1+2+3+4+6+8+12+16)
+// = 312 slots.  Descending inside a tier.
+constexpr int kBuckets = 128;
+constexpr int kClassSlots = 312;
+constexpr int kKeyBins = 2 * kBuckets + kBuckets * kClassSlots;
 
 // Per-run status written by the device (read back after each run).
 struct RunStatus {
@@ -106,7 +107,8 @@ struct EngineParams {
     double *out;
     int32_t max_width;
     int32_t group_threads;  // threads of the warp group that prices one tier-1 tree
-    int32_t big_threshold;  // widths above this go to whole blocks
+    int32_t big_threshold;  // widths above this go to warp groups or whole blocks
+    int32_t max_warp_k;     // largest K of a warp task (8 for double rows, 16 for float)
     int32_t record_busy;
 };
 

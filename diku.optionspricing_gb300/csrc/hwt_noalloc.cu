@@ -11,7 +11,7 @@
 // caller passes device pointers for the options, the yield curve and the prices.
 //
 // The array is a __device__ variable: every GPU that loads the library holds it
-// (about 4 MB) until the process exits.  In host code its name is only a
+// (about 5 MB) until the process exits.  In host code its name is only a
 // host-side stand-in, so its device address is looked up once per device with
 // cudaGetSymbolAddress, on the first call made with that device current; make
 // that first call before any stream capture.  All calls share the array and it
@@ -128,7 +128,8 @@ extern "C" int hwt_price_device_noalloc(const hwt_options *dev_opts, const hwt_y
     p.out = dev_out_prices;
     p.max_width = kMaxTreeWidth;
     p.group_threads = 128;
-    p.big_threshold = 256;
+    p.max_warp_k = mode == HWT_BATCHED_FP64 ? 8 : 16;
+    p.big_threshold = 32 * p.max_warp_k;
     p.record_busy = 0;
 
     int sms = 0;

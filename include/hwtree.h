@@ -87,7 +87,8 @@ typedef struct hwt_config {
     int32_t block_size;    /* threads that price one wide tree, multiple of 32 in 32..512; raised
                               to width/8 for wider trees (8 nodes per thread at most) */
     int32_t sort;          /* HWT_SORT_*, accepted and ignored */
-    int32_t big_threshold; /* widths above this get a whole block (<= 256) */
+    int32_t big_threshold; /* widths above this leave warp tasks for warp groups (<= 256 for
+                              FP64 rows, <= 512 for float rows) */
     int32_t use_graph;     /* 1 = replay a captured CUDA graph (default), 0 = direct launches */
     int32_t record_busy;   /* 1 = record per-block busy time for the tail-imbalance stat */
 } hwt_config;
@@ -156,7 +157,7 @@ int hwt_price_device(hwt_ctx *ctx, const hwt_options *dev_opts, const hwt_yield 
  * another allocator; latency-bound paths where cudaMalloc/cudaFree, which may
  * synchronise the device, are not allowed): no context, no allocation of any
  * kind; the scratch the pricing kernels need lives in a static device array of
- * the library (about 4 MB on every GPU that loads it, until exit).
+ * the library (about 5 MB on every GPU that loads it, until exit).
  *   dev_opts, dev_yield, dev_out_prices: DEVICE pointers of the current device
  *   mode: HWT_BATCHED_FP64, HWT_BATCHED_FP32 or HWT_BATCHED_MIXED
  *   stream: cudaStream_t to run on (NULL: the default stream); the call waits for it
