@@ -199,11 +199,18 @@ def run_ours(args, rank, world, local):
     nodes = int(np.sum(pkg.active_nodes(shp["height"], shp["jmax"])))
     flop_per_batch = FLOP_PER_NODE * nodes
 
-    pricer = pkg.Pricer(local, os.path.join(ROOT, "profiles", "tune_cache.txt") if args.tune else None)
+    pricer = pkg.Pricer(local)
     mode = {"mixed": pkg.BATCHED_MIXED, "fp64": pkg.BATCHED_FP64, "fp32": pkg.BATCHED_FP32,
             "plain": pkg.PLAIN_FP64}[args.mode]
-    if args.tune:
-        pricer.autotune(opts, y, mode)
+    # the library's autotuner (hwt_autotune) picks group size, warp-task width
+    # threshold and K set for this batch, untimed, for every batched mode used below
+    tuned = {}
+    if not args.no_tune:
+        for m in (pkg.BATCHED_MIXED, pkg.BATCHED_FP32, pkg.BATCHED_FP64):
+            if m == mode or not args.skip_survey:
+                c = pricer.autotune(opts, y, m, repeats=2)
+                tuned[pkg.MODE_NAMES[m]] = {"block_size": c.block_size, "big_threshold": c.big_threshold,
+                                            "warp_k_mask": c.warp_k_mask}
 
     # device-resident inputs
     fields = {"strike": opts.StrikePrices, "bond_maturity": opts.Maturities, "option_maturity": opts.Lengths,
@@ -372,7 +379,8 @@ def run_ours(args, rank, world, local):
             "config": {"workload": args.workload, "options": n, "mode": pkg.MODE_NAMES[mode],
                        "active_nodes_per_pass": nodes, "parallelism": "replicas" if world > 1 else "single",
                        "l2": "flushed between steps (256 MB memset), inputs 1.35 MB",
-                       "block_size": st.block_size, "grid": st.grid},
+                       "block_size": st.block_size, "grid": st.grid,
+                       "tuned": tuned.get(pkg.MODE_NAMES[mode], "library defaults")},
             "clocks": clk.summary(),
             "gpu_launches": launches,
             "e2e": {"value": world * n / (e2e_ms * 1e-3), "unit": "options/s", "h2d_bytes_per_step": h2d_bytes,
@@ -407,7 +415,7 @@ def main():
     ap.add_argument("--mode", default="mixed", choices=["mixed", "fp64", "fp32", "plain"])
     ap.add_argument("--ref-sample", type=int, default=6000)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--tune", action="store_true")
+    ap.add_argument("--no-tune", action="store_true", help="library defaults instead of the autotuned configuration")
     ap.add_argument("--skip-survey", action="store_true", help="time only the headline mode (profiling runs)")
     ap.add_argument("--no-surrogate", action="store_true")
     ap.add_argument("--sur-samples", type=int, default=4_000_000)

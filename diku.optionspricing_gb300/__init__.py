@@ -44,12 +44,15 @@ class OptionType(enum.IntEnum):
 
 
 class SortType(str, enum.Enum):
-    """common/Options.hpp:15-22 (accepted; results never depend on it)."""
+    """common/Options.hpp:15-22: the order the engine schedules trees in (results
+    never depend on it).  NONE is the engine's own order (heaviest first); INPUT,
+    an addition, keeps arrival order without binning by size."""
     WIDTH_DESC = "W"
     WIDTH_ASC = "w"
     HEIGHT_DESC = "H"
     HEIGHT_ASC = "h"
     NONE = "-"
+    INPUT = "i"
 
 
 class HwtError(RuntimeError):
@@ -77,9 +80,10 @@ class _Yield(ctypes.Structure):
 
 
 class Config(ctypes.Structure):
-    """hwt_config: mode, block_size, sort, big_threshold, use_graph, record_busy."""
+    """hwt_config: mode, block_size, sort, big_threshold, use_graph, record_busy, warp_k_mask."""
     _fields_ = [("mode", ctypes.c_int32), ("block_size", ctypes.c_int32), ("sort", ctypes.c_int32),
-                ("big_threshold", ctypes.c_int32), ("use_graph", ctypes.c_int32), ("record_busy", ctypes.c_int32)]
+                ("big_threshold", ctypes.c_int32), ("use_graph", ctypes.c_int32), ("record_busy", ctypes.c_int32),
+                ("warp_k_mask", ctypes.c_int32)]
 
 
 class Stats(ctypes.Structure):
@@ -362,8 +366,9 @@ class Pricer:
             raise HwtError(rc, msg)
 
     def config(self, mode: int, block_size: int = 0, big_threshold: int = 0, use_graph: bool = True,
-               record_busy: bool = False, sort: str = "-") -> Config:
-        return Config(mode, block_size, ord(sort), big_threshold, 1 if use_graph else 0, 1 if record_busy else 0)
+               record_busy: bool = False, sort: str = "-", warp_k_mask: int = 0) -> Config:
+        return Config(mode, block_size, ord(sort), big_threshold, 1 if use_graph else 0, 1 if record_busy else 0,
+                      warp_k_mask)
 
     def price(self, options: Options, yield_: Yield, mode: int = BATCHED_FP64, out: np.ndarray | None = None,
               **cfg) -> np.ndarray:

@@ -25,18 +25,22 @@ using namespace hwt;
 namespace {
 
 constexpr int kMaxYield = 4096;
-constexpr int kDefaultBlock = 128;
+// smallest warp group: 128 threads for double rows (a tree's critical path runs
+// on the FP64 pipes of as many SM sub-partitions as it has warps), 64 for float rows
+constexpr int kDefaultBlockFP64 = 128;
+constexpr int kDefaultBlockFloat = 64;
 constexpr int kDefaultBig = 256;
 
 thread_local int g_create_status = HWT_OK;
 
 struct GraphKey {
-    int mode, n, block, big, grid, record, yn;
+    int mode, n, block, big, grid, record, yn, kmask, sort;
     const void *ptr[9];  // the eight option arrays and the output
     bool operator<(const GraphKey &o) const
     {
-        if (std::tie(mode, n, block, big, grid, record, yn) != std::tie(o.mode, o.n, o.block, o.big, o.grid, o.record, o.yn))
-            return std::tie(mode, n, block, big, grid, record, yn) < std::tie(o.mode, o.n, o.block, o.big, o.grid, o.record, o.yn);
+        const auto a = std::tie(mode, n, block, big, grid, record, yn, kmask, sort);
+        const auto b = std::tie(o.mode, o.n, o.block, o.big, o.grid, o.record, o.yn, o.kmask, o.sort);
+        if (a != b) return a < b;
         return memcmp(ptr, o.ptr, sizeof(ptr)) < 0;
     }
 };
@@ -210,6 +214,12 @@ int upload_yield(hwt_ctx *c, const hwt_yield *y)
     return HWT_OK;
 }
 
+bool valid_sort(int s)
+{
+    return s == 0 || s == HWT_SORT_NONE || s == HWT_SORT_WIDTH_DESC || s == HWT_SORT_WIDTH_ASC ||
+           s == HWT_SORT_HEIGHT_DESC || s == HWT_SORT_HEIGHT_ASC || s == HWT_SORT_INPUT;
+}
+
 hwt_config resolve(const hwt_ctx *c, const hwt_config *cfg, int mode)
 {
     hwt_config r = c->tuned[(mode >= 0 && mode < 4) ? mode : 0];
@@ -218,6 +228,7 @@ hwt_config resolve(const hwt_ctx *c, const hwt_config *cfg, int mode)
         if (cfg->block_size > 0) r.block_size = cfg->block_size;
         if (cfg->big_threshold > 0) r.big_threshold = cfg->big_threshold;
         r.sort = cfg->sort;
+        if (cfg->warp_k_mask != 0) r.warp_k_mask = cfg->warp_k_mask;
         r.use_graph = cfg->use_graph;
         r.record_busy = cfg->record_busy;
     } else {
@@ -226,6 +237,15 @@ hwt_config resolve(const hwt_ctx *c, const hwt_config *cfg, int mode)
     }
     return r;
 }
+
+int check_config(hwt_ctx *c, const hwt_config &cfg)
+{
+    if (cfg.block_size != 64 && cfg.block_size != 128 && cfg.block_size != 256 && cfg.block_size != 512)
+        return fail(c, HWT_EINVAL, "block_size must be 64, 128, 256 or 512");
+    if (!valid_sort(cfg.sort)) return fail(c, HWT_EINVAL, "unknown sort order (one of - W w H h i)");
+    return HWT_OK;
+}
+
 
 bool is_pinned(const void *p)
 {
@@ -300,7 +320,9 @@ int run_batch(hwt_ctx *c, const DevOptions &dopt, double *dev_out, const hwt_con
     p.s.status = c->d_status;
     p.out = dev_out;
     p.group_threads = cfg.block_size;
-    p.max_warp_k = cfg.mode == HWT_BATCHED_FP64 ? 8 : 16;
+    p.warp_k_mask = resolve_k_mask(cfg.mode, cfg.warp_k_mask, &p.max_warp_k);
+    p.max_group_k = cfg.mode == HWT_BATCHED_FP64 ? kMaxBlockK : kMaxGroupKFloat;
+    p.sort = cfg.sort;
     p.big_threshold = std::min(cfg.big_threshold, 32 * p.max_warp_k);
     p.max_width = kMaxTreeWidth;
     p.record_busy = cfg.record_busy ? 1 : 0;
@@ -323,7 +345,7 @@ int run_batch(hwt_ctx *c, const DevOptions &dopt, double *dev_out, const hwt_con
     *graph_used = 0;
     if (!use_graph) return enqueue_kernels(c, p, cfg, grid, timing, false);
 
-    GraphKey key{cfg.mode, dopt.n, cfg.block_size, p.big_threshold, grid, p.record_busy, p.yc.n,
+    GraphKey key{cfg.mode, dopt.n, cfg.block_size, p.big_threshold, grid, p.record_busy, p.yc.n, p.warp_k_mask, p.sort,
                  {dopt.strike, dopt.bond_maturity, dopt.option_maturity, dopt.term_unit, dopt.term_steps, dopt.a,
                   dopt.sigma, dopt.type, dev_out}};
     auto it = c->graphs.find(key);
@@ -366,7 +388,7 @@ int finish(hwt_ctx *c, const hwt_config &cfg, hwt_stats *stats, int launches, in
         stats->d2h_bytes = d2h;
         stats->device_bytes = c->device_bytes;
         stats->kernel_launches = launches;
-        stats->n_block_trees = st.n_cta + st.n_group;
+        stats->n_block_trees = st.tier_count[0] + st.tier_count[1] + st.tier_count[2] + st.tier_count[3];
         stats->n_warp_tasks = st.n_warp_tasks;
         stats->block_size = cfg.mode == HWT_PLAIN_FP64 ? 128 : kPricingThreads;
         stats->grid = grid_hint;
@@ -444,8 +466,9 @@ hwt_ctx *hwt_create(int device, const char *tune_cache)
         hwt_config &t = c->tuned[m];
         memset(&t, 0, sizeof(t));
         t.mode = m;
-        t.block_size = kDefaultBlock;
+        t.block_size = m == HWT_BATCHED_FP64 ? kDefaultBlockFP64 : kDefaultBlockFloat;
         t.big_threshold = m == HWT_BATCHED_FP64 ? kDefaultBig : kMaxWarpWidth;  // float rows fit 512 per warp
+        t.warp_k_mask = resolve_k_mask(m, 0, nullptr);
         t.use_graph = 1;
     }
     if (tune_cache && *tune_cache) {
@@ -455,13 +478,15 @@ hwt_ctx *hwt_create(int device, const char *tune_cache)
         while (ok && std::getline(in, line)) {
             std::istringstream ls(line);
             std::string name;
-            int mode = -1, block = 0, big = 0;
+            int mode = -1, block = 0, big = 0, kmask = 0;
             if (!std::getline(ls, name, '|')) continue;
             if (!(ls >> mode >> block >> big)) continue;
+            if (!(ls >> kmask)) kmask = 0;  // lines without a K mask keep the mode's default
             if (name == c->gpu_name && mode >= 0 && mode < 4 && (block == 64 || block == 128 || block == 256 || block == 512) &&
                 big >= 1 && big <= kMaxWarpWidth) {
                 c->tuned[mode].block_size = block;
                 c->tuned[mode].big_threshold = big;
+                c->tuned[mode].warp_k_mask = resolve_k_mask(mode, kmask, nullptr);
             }
         }
     }
@@ -507,8 +532,7 @@ int hwt_price_ex(hwt_ctx *c, const hwt_options *o, const hwt_yield *y, const hwt
     if (o->n == 0) return HWT_OK;
     if ((r = ensure_capacity(c, o->n))) return r;
     const hwt_config cfg = resolve(c, cfg_in, mode);
-    if (cfg.block_size != 64 && cfg.block_size != 128 && cfg.block_size != 256 && cfg.block_size != 512)
-        return fail(c, HWT_EINVAL, "block_size must be 64, 128, 256 or 512");
+    if ((r = check_config(c, cfg))) return r;
 
     const int64_t n = o->n;
     const Packing pk = packing(c->cap);
@@ -584,8 +608,7 @@ int hwt_price_device(hwt_ctx *c, const hwt_options *o, const hwt_yield *y, const
     if (o->n == 0) return HWT_OK;
     if ((r = ensure_capacity(c, o->n))) return r;
     const hwt_config cfg = resolve(c, cfg_in, mode);
-    if (cfg.block_size != 64 && cfg.block_size != 128 && cfg.block_size != 256 && cfg.block_size != 512)
-        return fail(c, HWT_EINVAL, "block_size must be 64, 128, 256 or 512");
+    if ((r = check_config(c, cfg))) return r;
     DevOptions dopt;
     dopt.n = o->n;
     dopt.strike = o->strike; dopt.bond_maturity = o->bond_maturity; dopt.option_maturity = o->option_maturity;
@@ -639,13 +662,19 @@ int hwt_autotune(hwt_ctx *c, const hwt_options *o, const hwt_yield *y, int mode,
     std::vector<double> out(o->n);
     const int blocks[] = {64, 128, 256, 512};
     const int bigs[] = {128, 256, 384, 512};
+    // the mode's default K set and a denser one (better fit, larger code footprint)
+    const int kmasks[] = {resolve_k_mask(mode, 0, nullptr),
+                          resolve_k_mask(mode, mode == HWT_BATCHED_FP64 ? kKMaskFP64Alt : kKMaskFloatAlt, nullptr)};
+    const int n_kmasks = 2;
     double best_ms = 1e300;
     hwt_config best_cfg = c->tuned[mode];
     for (int b : blocks) {
         for (int big : bigs) {
+          for (int km = 0; km < n_kmasks; ++km) {
             hwt_config cfg;
             memset(&cfg, 0, sizeof(cfg));
             cfg.mode = mode; cfg.block_size = b; cfg.big_threshold = big; cfg.use_graph = 1;
+            cfg.warp_k_mask = kmasks[km];
             double t = 1e300;
             for (int k = 0; k < repeats + 1; ++k) {
                 hwt_stats st;
@@ -656,6 +685,7 @@ int hwt_autotune(hwt_ctx *c, const hwt_options *o, const hwt_yield *y, int mode,
             }
             if (r == HWT_EUNSUPPORTED) continue;
             if (t < best_ms) { best_ms = t; best_cfg = cfg; }
+          }
         }
     }
     best_cfg.use_graph = 1;
@@ -677,7 +707,8 @@ int hwt_autotune(hwt_ctx *c, const hwt_options *o, const hwt_yield *y, int mode,
         }
         std::ofstream outf(c->tune_path, std::ios::trunc);
         for (auto &l : keep) outf << l << "\n";
-        outf << c->gpu_name << "|" << mode << " " << best_cfg.block_size << " " << best_cfg.big_threshold << "\n";
+        outf << c->gpu_name << "|" << mode << " " << best_cfg.block_size << " " << best_cfg.big_threshold << " "
+             << best_cfg.warp_k_mask << "\n";
     }
     return HWT_OK;
 }

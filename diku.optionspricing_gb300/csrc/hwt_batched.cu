@@ -61,7 +61,7 @@ struct ModeMix {
 __device__ __forceinline__ int cls_K(int cls)
 {
     const int k = cls / kNumL;
-    return k < 6 ? (k < 4 ? k + 1 : (k == 4 ? 6 : 8)) : (k == 6 ? 12 : 16);
+    return k < 8 ? k + 1 : (k == 8 ? 12 : 16);
 }
 
 // Named barrier `id` over the `nthreads` threads of one tree's warp group (id 0
@@ -83,8 +83,8 @@ __device__ __forceinline__ int cls_L(int cls) { return 1 << (cls % kNumL); }
 // kNumL * (sum of the K values before K_q) + ts * kNumL + l, so slot % kNumL = l.
 __device__ __forceinline__ int class_slot_base(int q)
 {
-    // kNumL x prefix sums of {1, 2, 3, 4, 6, 8, 12, 16}
-    return kNumL * (q < 4 ? q * (q + 1) / 2 : (q == 4 ? 10 : (q == 5 ? 16 : (q == 6 ? 24 : 36))));
+    // kNumL x prefix sums of {1, 2, ..., 8, 12, 16}
+    return kNumL * (q <= 8 ? q * (q + 1) / 2 : 48);
 }
 __device__ __forceinline__ int class_slot(int cls)
 {
@@ -100,17 +100,18 @@ __device__ __forceinline__ int slot_class(int slot)
     return (q * kNumL + rest % kNumL) | ((rest / kNumL) << 6);
 }
 
-// Smallest L*K >= width with K in {1,2,3,4,6,8,12,16} (up to max_k), L in
-// {1..32}; ties go to the larger K (more trees per warp, fewer shuffles per
-// node).  K = 5, 7, ... are left out to keep the kernel's code (and its
-// instruction-cache footprint) small.
-__host__ __device__ int pick_warp_class(int width, int max_k)
+// Smallest L*K >= width with K in the allowed set (bits of k_mask over
+// {1, 2, ..., 8, 12, 16}), L in {1..32}; ties go to the larger K (more trees per
+// warp, fewer shuffles per node).  Each K used adds its code to the working set
+// of the instruction cache, so float rows (whose warps are issue-bound) use only
+// 1, 2, 4, 8 and 16 by default; double rows (FP64-pipe-bound) use 1 .. 8.
+__host__ __device__ int pick_warp_class(int width, int k_mask)
 {
-    const int ks[kNumK] = {1, 2, 3, 4, 6, 8, 12, 16};  // the K values of kWarpK
+    const int ks[kNumK] = {1, 2, 3, 4, 5, 6, 7, 8, 12, 16};  // the K values of kWarpK
     int best = -1, best_slots = 1 << 30;
     for (int q = kNumK - 1; q >= 0; --q) {
         const int K = ks[q];
-        if (K > max_k) continue;
+        if (!((k_mask >> q) & 1)) continue;
         for (int l = 0; l < kNumL; ++l) {
             const int slots = K << l;
             if (slots >= width && slots < best_slots) {
@@ -128,6 +129,24 @@ __device__ __forceinline__ int desc_bucket(double v, int per)
     int b = (int)(log2(v + 1.0) * per);
     if (b > kBuckets - 1) b = kBuckets - 1;
     return kBuckets - 1 - b;
+}
+
+// Bucket of a tree inside its tier for sort order `sort` (HWT_SORT_*): the
+// default orders the group tiers by work and the warp tier by height, tallest
+// first; 'H'/'h' and 'W'/'w' order every tier by height or width, descending /
+// ascending; 'i' keeps one bucket per tier (trees in arrival order, close to input
+// order).
+__device__ __forceinline__ int sort_bucket(int sort, bool warp_tier, int n, int width, long long nodes)
+{
+    const int per = warp_tier ? 8 : 4;
+    switch (sort) {
+        case 'H': return desc_bucket((double)n, per);
+        case 'h': return kBuckets - 1 - desc_bucket((double)n, per);
+        case 'W': return desc_bucket((double)width, per);
+        case 'w': return kBuckets - 1 - desc_bucket((double)width, per);
+        case 'i': return 0;
+        default: return warp_tier ? desc_bucket((double)n, per) : desc_bucket((double)nodes + (double)width, per);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -160,18 +179,29 @@ __global__ void size_kernel(EngineParams p)
             t.term_unit = p.opt.term_unit[i]; t.type = ty; t.edges = (int8_t)s.edges;
             p.s.trees[i] = t;
             nodes = (unsigned long long)s.nodes;
+            // warp tier up to the warp-task width; wider trees go to the smallest
+            // group (not below group_threads) that holds them at max_group_k nodes
+            // per thread
             const int warp_max = p.big_threshold < 32 * p.max_warp_k ? p.big_threshold : 32 * p.max_warp_k;
-            const int tier = s.width <= warp_max ? 2 : (s.width <= kMaxBlockK * p.group_threads ? 1 : 0);
+            int tier = kWarpTier;
+            if (s.width > warp_max) {
+                tier = 0;
+                for (int t = kGroupTiers - 1; t > 0; --t) {
+                    const int gs = kPricingThreads >> t;
+                    if (gs >= p.group_threads && s.width <= p.max_group_k * gs) { tier = t; break; }
+                }
+            }
             int cls = 0;
-            if (tier == 2) {
-                cls = pick_warp_class(s.width, p.max_warp_k);
+            if (tier == kWarpTier) {
+                cls = pick_warp_class(s.width, p.warp_k_mask);
                 const int top = s.edges ? (s.width - 1) % cls_K(cls) : 0;  // slot of node W-1
                 cls |= top << 6;
             }
-            // tiers 0 and 1: one tree per task, by work (4 buckets per octave); tier 2:
-            // trees of one class in lockstep, by height (8 per octave, <= 9% apart)
-            if (tier == 2) key = 2 * kBuckets + desc_bucket((double)s.n, 8) * kClassSlots + class_slot(cls);
-            else key = tier * kBuckets + desc_bucket((double)s.nodes + (double)s.width, 4);
+            // group tiers: one tree per task, by work (4 buckets per octave); warp
+            // tier: trees of one class in lockstep, by height (8 per octave, <= 9% apart)
+            const int bucket = sort_bucket(p.sort, tier == kWarpTier, s.n, s.width, (long long)s.nodes);
+            if (tier == kWarpTier) key = kWarpTier * kBuckets + bucket * kClassSlots + class_slot(cls);
+            else key = tier * kBuckets + bucket;
             p.s.keys[i] = key;
             atomicMax(&p.s.status->max_width, s.width);
             atomicMax(&p.s.status->max_height, s.n);
@@ -188,8 +218,8 @@ __global__ void size_kernel(EngineParams p)
 // starts, and the tier sizes.
 __device__ __forceinline__ int bin_tasks(int b, int c)
 {
-    if (b < 2 * kBuckets || c == 0) return 0;  // tiers 0 and 1: no warp tasks
-    const int G = 32 / cls_L((b - 2 * kBuckets) % kClassSlots);  // slot % kNumL is the L index
+    if (b < kWarpTier * kBuckets || c == 0) return 0;  // group tiers: no warp tasks
+    const int G = 32 / cls_L((b - kWarpTier * kBuckets) % kClassSlots);  // slot % kNumL is the L index
     return (c + G - 1) / G;
 }
 
@@ -249,9 +279,11 @@ __global__ void __launch_bounds__(1024) scan_kernel(EngineParams p)
     // tier boundaries (global writes of the block are visible to it after the barrier)
     __syncthreads();
     if (threadIdx.x == 0) {
-        const int t1 = p.s.bin_start[kBuckets], t2 = p.s.bin_start[2 * kBuckets];
-        p.s.status->n_cta = t1;
-        p.s.status->n_group = t2 - t1;
+        for (int t = 0; t < kGroupTiers; ++t) {
+            const int a = p.s.bin_start[t * kBuckets], b = p.s.bin_start[(t + 1) * kBuckets];
+            p.s.status->tier_start[t] = a;
+            p.s.status->tier_count[t] = b - a;
+        }
     }
 }
 
@@ -266,8 +298,8 @@ __global__ void scatter_kernel(EngineParams p)
     const int q = atomicAdd(&p.s.fill[key], 1);
     const int pos = p.s.bin_start[key] + q;
     p.s.order[pos] = i;
-    if (key >= 2 * kBuckets) {
-        const int cls = slot_class((key - 2 * kBuckets) % kClassSlots);
+    if (key >= kWarpTier * kBuckets) {
+        const int cls = slot_class((key - kWarpTier * kBuckets) % kClassSlots);
         const int G = 32 / cls_L(cls & 63);
         if (q % G == 0) {
             WarpTask t;
@@ -903,17 +935,23 @@ __device__ void price_block_tree(const EngineParams &p, const Tree &t, const Gro
     }
 }
 
-// K = nodes per thread for a tree on group `gr` (width <= 8 * gr.nthreads).
+// K = nodes per thread for a tree on group `gr` (width <= 8 * gr.nthreads, or
+// 16 * gr.nthreads for float rows).  More nodes per thread spread the step's fixed
+// cost (halo exchange, barrier, loop control) over more nodes.
 template <class Mode>
 __device__ __forceinline__ void dispatch_block_tree(const EngineParams &p, const Tree &t, const Group &gr,
                                                     typename Mode::Row *sh_x, typename Mode::Scal *sh_red)
 {
-    // K rounded up to 1, 2, 4 or 8 (warps left past the width skip their steps)
+    // K rounded up to 1, 2, 4, 8 (12, 16) (warps left past the width skip their steps)
     const int K = (t.width + gr.nthreads - 1) / gr.nthreads;
     if (K <= 1) price_block_tree<Mode, 1>(p, t, gr, sh_x, sh_red);
     else if (K <= 2) price_block_tree<Mode, 2>(p, t, gr, sh_x, sh_red);
     else if (K <= 4) price_block_tree<Mode, 4>(p, t, gr, sh_x, sh_red);
-    else price_block_tree<Mode, 8>(p, t, gr, sh_x, sh_red);
+    else if (K <= 8 || !Mode::kFlux) price_block_tree<Mode, 8>(p, t, gr, sh_x, sh_red);
+    else if constexpr (Mode::kFlux) {
+        if (K <= 12) price_block_tree<Mode, 12>(p, t, gr, sh_x, sh_red);
+        else price_block_tree<Mode, 16>(p, t, gr, sh_x, sh_red);
+    }
 }
 
 template <class Mode>
@@ -923,43 +961,36 @@ __global__ void __launch_bounds__(kPricingThreads, 1) price_kernel(EngineParams 
     typedef typename Mode::Scal S;
     __shared__ R sh_x[2 * 32 * 4];
     __shared__ S sh_red[32];
-    __shared__ int sh_task[1 + 16];
+    __shared__ int sh_task[16];  // one per group of every group tier
     unsigned long long t_start = 0;
     if (p.record_busy && threadIdx.x == 0) asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t_start));
 
-    // Tier 0: trees wider than a group holds, one per block, heaviest first.
-    const int n_cta = p.s.status->n_cta;
-    for (;;) {
-        if (threadIdx.x == 0) sh_task[0] = atomicAdd(&p.s.status->cta_counter, 1);
-        __syncthreads();
-        const int tsk = sh_task[0];
-        __syncthreads();
-        if (tsk >= n_cta) break;
-        const Tree t = p.s.trees[p.s.order[tsk]];
-        const Group gr{0, (int)blockDim.x, 0};
-        dispatch_block_tree<Mode>(p, t, gr, sh_x, sh_red);
-        __syncthreads();  // shared buffers are reused by the next tree
-    }
-
-    // Tier 1: each group of group_threads threads prices its own trees.
-    {
-        const int n_group = p.s.status->n_group;
-        const int gsize = p.group_threads;
+    // Group tiers, heaviest first: tier t prices one tree per group of 512 >> t
+    // threads.  Group g of tier t uses named barrier and task slot 2^t - 1 + g
+    // (0: the whole block; 1-2: halves; 3-6: quarters; 7-14: eighths), so groups of
+    // different tiers never share one while some threads are still in the earlier
+    // tier.
+    for (int tier = 0; tier < kGroupTiers; ++tier) {
+        const int count = p.s.status->tier_count[tier];
+        if (count == 0) continue;
+        const int start = p.s.status->tier_start[tier];
+        const int gsize = kPricingThreads >> tier;
         const int g = (int)threadIdx.x / gsize;
-        const Group gr{g * gsize, gsize, 1 + g};
+        const int slot = (1 << tier) - 1 + g;
+        const Group gr{g * gsize, gsize, slot};
         for (;;) {
-            if ((int)threadIdx.x == gr.base) sh_task[1 + g] = atomicAdd(&p.s.status->group_counter, 1);
+            if ((int)threadIdx.x == gr.base) sh_task[slot] = atomicAdd(&p.s.status->tier_counter[tier], 1);
             tree_barrier(gr.bar, gr.nthreads);
-            const int tsk = sh_task[1 + g];
+            const int tsk = sh_task[slot];
             tree_barrier(gr.bar, gr.nthreads);
-            if (tsk >= n_group) break;
-            const Tree t = p.s.trees[p.s.order[n_cta + tsk]];
+            if (tsk >= count) break;
+            const Tree t = p.s.trees[p.s.order[start + tsk]];
             dispatch_block_tree<Mode>(p, t, gr, sh_x, sh_red);
-            tree_barrier(gr.bar, gr.nthreads);
+            tree_barrier(gr.bar, gr.nthreads);  // shared buffers are reused by the next tree
         }
     }
 
-    // Phase 2: warp tasks, each warp on its own.
+    // Warp tier: warp tasks, each warp on its own.
     const int n_tasks = p.s.status->n_warp_tasks;
     const int lane = threadIdx.x & 31;
     for (;;) {
@@ -973,7 +1004,9 @@ __global__ void __launch_bounds__(kPricingThreads, 1) price_kernel(EngineParams 
             case 2: price_warp_task<Mode, 2>(p, wt); break;
             case 3: price_warp_task<Mode, 3>(p, wt); break;
             case 4: price_warp_task<Mode, 4>(p, wt); break;
+            case 5: price_warp_task<Mode, 5>(p, wt); break;
             case 6: price_warp_task<Mode, 6>(p, wt); break;
+            case 7: price_warp_task<Mode, 7>(p, wt); break;
             case 8: price_warp_task<Mode, 8>(p, wt); break;
             default:
                 if constexpr (Mode::kFlux) {
@@ -995,9 +1028,21 @@ __global__ void __launch_bounds__(kPricingThreads, 1) price_kernel(EngineParams 
 
 }  // namespace
 
+int resolve_k_mask(int mode, int requested, int *max_k)
+{
+    const int allowed = mode == MODE_BATCHED_FP64 ? kKMaskFP64 : kKMaskAll;
+    int m = requested & allowed;
+    if (m == 0) m = mode == MODE_BATCHED_FP64 ? kKMaskFP64 : kKMaskFloat;
+    int mk = 1;
+    for (int q = 0; q < kNumK; ++q)
+        if ((m >> q) & 1) mk = kWarpK[q];
+    if (max_k) *max_k = mk;
+    return m;
+}
+
 int warp_class_of(int width, int *K, int *L)
 {
-    const int c = pick_warp_class(width, 16);
+    const int c = pick_warp_class(width, kKMaskFloat);
     if (c < 0) return -1;
     if (K) *K = kWarpK[c / kNumL];
     if (L) *L = 1 << (c % kNumL);

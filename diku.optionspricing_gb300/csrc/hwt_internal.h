@@ -52,36 +52,44 @@ struct WarpTask {
 };
 
 // Warp classes: L lanes per tree (power of two), K nodes per lane; L*K >= width.
-// class = index of K in kWarpK * kNumL + log2(L); FP64 rows stop at K = 8.
-constexpr int kWarpK[] = {1, 2, 3, 4, 6, 8, 12, 16};
-constexpr int kNumK = 8;
+// class = index of K in kWarpK * kNumL + log2(L); FP64 rows stop at K = 8.  A
+// call may restrict the K values used with a mask over kWarpK's indices.
+constexpr int kWarpK[] = {1, 2, 3, 4, 5, 6, 7, 8, 12, 16};
+constexpr int kNumK = 10;
+constexpr int kKMaskFP64 = 0xFF;      // default K set of double rows: 1 .. 8
+constexpr int kKMaskFP64Alt = 0xAF;   // autotuner's alternative: 1, 2, 3, 4, 6, 8
+constexpr int kKMaskFloat = 0x28B;    // default K set of float rows: 1, 2, 4, 8, 16
+constexpr int kKMaskFloatAlt = 0x3AF; // autotuner's alternative: 1, 2, 3, 4, 6, 8, 12, 16
+constexpr int kKMaskAll = 0x3FF;
 constexpr int kNumL = 6;                       // L = 1, 2, 4, 8, 16, 32
 constexpr int kNumWarpClasses = kNumK * kNumL;
 constexpr int kMaxWarpWidth = 32 * 16;         // wider trees go to warp groups or whole blocks
-constexpr int kMaxBlockK = 8;                  // nodes per thread for block trees
+constexpr int kMaxBlockK = 8;                  // nodes per thread for whole-block trees
+constexpr int kMaxGroupKFloat = 16;            // nodes per thread for warp-group trees, float rows
 constexpr int kPricingThreads = 512;           // threads of every pricing block
 constexpr int kMaxTreeWidth = kMaxBlockK * kPricingThreads;  // widest tree accepted
 
-// Sort keys.  Tier 0 (trees wider than a group can hold, priced by the whole
-// block): bins [0, kBuckets) by work; tier 1 (priced by a group of warps): bins
-// [kBuckets, 2 kBuckets) by work; tier 2 (small trees packed into warp tasks):
-// 2 kBuckets + height bucket * kClassSlots + class slot, one slot per warp class
-// (K, L) and slot ts < K of the top edge node: 6 (L values) x (1+2+3+4+6+8+12+16)
-// = 312 slots.  Descending inside a tier.
+// Sort keys.  Group tiers t = 0..3 (trees priced by a group of 512 >> t threads:
+// the whole block, halves, quarters, eighths): bins [t kBuckets, (t+1) kBuckets),
+// by work.  Warp tier (small trees packed into warp tasks): kWarpTier kBuckets +
+// height bucket * kClassSlots + class slot, one slot per warp class (K, L) and
+// slot ts < K of the top edge node: 6 (L values) x (1+2+...+8+12+16) = 384 slots.
+// Descending inside a tier.
+constexpr int kGroupTiers = 4;
+constexpr int kWarpTier = kGroupTiers;
 constexpr int kBuckets = 128;
-constexpr int kClassSlots = 312;
-constexpr int kKeyBins = 2 * kBuckets + kBuckets * kClassSlots;
+constexpr int kClassSlots = 384;
+constexpr int kKeyBins = kWarpTier * kBuckets + kBuckets * kClassSlots;
 
 // Per-run status written by the device (read back after each run).
 struct RunStatus {
     unsigned long long first_bad; // (index << 32) | reason of the lowest rejected option; all ones if none
     unsigned long long nodes;     // active nodes of one pass, summed over valid options
     int32_t bad_count;            // options rejected by validation
-    int32_t n_cta;                // tier 0: trees priced by whole blocks
-    int32_t n_group;              // tier 1: trees priced by warp groups
-    int32_t n_warp_tasks;         // tier 2: warp tasks
-    int32_t cta_counter;          // work-queue heads
-    int32_t group_counter;
+    int32_t tier_start[kGroupTiers];    // first sorted position of each group tier
+    int32_t tier_count[kGroupTiers];    // trees priced by groups of 512 >> t threads
+    int32_t tier_counter[kGroupTiers];  // work-queue heads of the group tiers
+    int32_t n_warp_tasks;         // warp tier: warp tasks
     int32_t warp_counter;
     int32_t max_width;            // widest / tallest valid tree
     int32_t max_height;
@@ -106,11 +114,18 @@ struct EngineParams {
     Scratch s;
     double *out;
     int32_t max_width;
-    int32_t group_threads;  // threads of the warp group that prices one tier-1 tree
+    int32_t group_threads;  // smallest warp group (64..512 threads) a wide tree is given
     int32_t big_threshold;  // widths above this go to warp groups or whole blocks
     int32_t max_warp_k;     // largest K of a warp task (8 for double rows, 16 for float)
+    int32_t warp_k_mask;    // K values warp tasks may use (bits over kWarpK's indices)
+    int32_t max_group_k;    // largest K of a warp-group tree: 8 double rows, 16 float
+    int32_t sort;           // HWT_SORT_* order inside the tiers (0 / '-': heaviest first)
     int32_t record_busy;
 };
+
+// Resolves a requested K mask for `mode` (0 = the mode's default) and the largest
+// K it allows.
+int resolve_k_mask(int mode, int requested, int *max_k);
 
 // Launchers (hwt_batched.cu / hwt_plain.cu).  All enqueue on `stream`; none syncs.
 cudaError_t launch_sizing(const EngineParams &p, cudaStream_t stream);

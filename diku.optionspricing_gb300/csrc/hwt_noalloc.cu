@@ -127,8 +127,10 @@ extern "C" int hwt_price_device_noalloc(const hwt_options *dev_opts, const hwt_y
     p.s.cta_busy = nullptr;
     p.out = dev_out_prices;
     p.max_width = kMaxTreeWidth;
-    p.group_threads = 128;
-    p.max_warp_k = mode == HWT_BATCHED_FP64 ? 8 : 16;
+    p.group_threads = mode == HWT_BATCHED_FP64 ? 128 : 64;
+    p.warp_k_mask = resolve_k_mask(mode, 0, &p.max_warp_k);
+    p.max_group_k = mode == HWT_BATCHED_FP64 ? kMaxBlockK : kMaxGroupKFloat;
+    p.sort = 0;
     p.big_threshold = 32 * p.max_warp_k;
     p.record_busy = 0;
 

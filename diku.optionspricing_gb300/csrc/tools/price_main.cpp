@@ -5,7 +5,7 @@
 //   -v|--version M ...  pricing mode(s): 0 plain FP64, 1 batched FP64 (default),
 //                       2 batched FP32, 3 batched mixed
 //   -b|--block B ...    threads per block-tree block (the reference's -b)
-//   -s|--sort S ...     sort order W w H h - (accepted; results do not depend on it)
+//   -s|--sort S ...     schedule order W w H h - i (results do not depend on it)
 //   -r|--runs R         time R runs and print "mode,block,sort,kernel_us,total_us,bytes"
 //   -d|--device D       CUDA device
 //   -t|--test           human-readable timing instead of the price array
@@ -50,7 +50,7 @@ Args parse(int argc, char **argv)
         else if (f == "-b" || f == "--block") many([&](const char *v) { a.blocks.push_back(std::atoi(v)); });
         else if (f == "-s" || f == "--sort") many([&](const char *v) {
             const char c = v[0];
-            if (std::strlen(v) == 1 && (c == 'W' || c == 'w' || c == 'H' || c == 'h' || c == '-')) a.sorts.push_back(c);
+            if (std::strlen(v) == 1 && (c == 'W' || c == 'w' || c == 'H' || c == 'h' || c == '-' || c == 'i')) a.sorts.push_back(c);
         });
         else if (f == "-r" || f == "--runs") a.runs = std::atoi(one().c_str());
         else if (f == "-d" || f == "--device") a.device = std::atoi(one().c_str());

@@ -46,14 +46,18 @@ extern "C" {
 #define HWT_BATCHED_FP32 2   /* binned persistent engine, float throughout */
 #define HWT_BATCHED_MIXED 3  /* float rows, double alpha-fit sums, scales, payoff, discount */
 
-/* Sort orders accepted for compatibility with the reference's -s flag
- * (common/Options.hpp:15-22).  Results never depend on them; the engine always
- * bins by width x height and orders work heaviest first. */
+/* Sort orders of the reference's -s flag (common/Options.hpp:15-22).  They set the
+ * order in which the engine schedules trees inside each of its tiers (whole-block
+ * trees, warp-group trees, warp tasks); results never depend on them.  NONE (and
+ * 0) is the engine's own order: heaviest work first, warp tasks by class and
+ * height.  INPUT keeps the arrival order inside each tier and class (no binning by
+ * size), the baseline for A/B runs against the sorted orders. */
 #define HWT_SORT_NONE '-'
 #define HWT_SORT_WIDTH_DESC 'W'
 #define HWT_SORT_WIDTH_ASC 'w'
 #define HWT_SORT_HEIGHT_DESC 'H'
 #define HWT_SORT_HEIGHT_ASC 'h'
+#define HWT_SORT_INPUT 'i'
 
 /* Option records, SoA, one entry per option (common/Options.hpp:48-58).
  * strike = StrikePrices, bond_maturity = Maturities [years], option_maturity =
@@ -84,13 +88,17 @@ typedef struct hwt_yield {
  * block_size plays the part of the reference's -b flag (common/Args.hpp:43). */
 typedef struct hwt_config {
     int32_t mode;          /* HWT_* mode */
-    int32_t block_size;    /* threads that price one wide tree, multiple of 32 in 32..512; raised
-                              to width/8 for wider trees (8 nodes per thread at most) */
-    int32_t sort;          /* HWT_SORT_*, accepted and ignored */
+    int32_t block_size;    /* smallest warp group (64, 128, 256 or 512 threads) that prices one
+                              wide tree; each tree gets the smallest group at least this large
+                              that holds it at 8 (FP64 rows) or 16 (float rows) nodes per thread */
+    int32_t sort;          /* HWT_SORT_* schedule order (0 = HWT_SORT_NONE) */
     int32_t big_threshold; /* widths above this leave warp tasks for warp groups (<= 256 for
                               FP64 rows, <= 512 for float rows) */
     int32_t use_graph;     /* 1 = replay a captured CUDA graph (default), 0 = direct launches */
     int32_t record_busy;   /* 1 = record per-block busy time for the tail-imbalance stat */
+    int32_t warp_k_mask;   /* nodes-per-lane values warp tasks may use: bit q allows the q-th of
+                              {1, 2, 3, 4, 5, 6, 7, 8, 12, 16}; 12 and 16 apply to float rows
+                              only; 0 = the mode's default (FP64: 1..8; float rows: 1, 2, 4, 8, 16) */
 } hwt_config;
 
 /* Run statistics, filled when a non-NULL pointer is passed.  Times are CUDA-event

@@ -23,8 +23,8 @@
 
 namespace hwtree {
 
-// common/Options.hpp:15-22
-enum class SortType : char { WIDTH_DESC = 'W', WIDTH_ASC = 'w', HEIGHT_DESC = 'H', HEIGHT_ASC = 'h', NONE = '-' };
+// common/Options.hpp:15-22, plus INPUT (arrival order, no binning by size)
+enum class SortType : char { WIDTH_DESC = 'W', WIDTH_ASC = 'w', HEIGHT_DESC = 'H', HEIGHT_ASC = 'h', NONE = '-', INPUT = 'i' };
 
 // common/Options.hpp:24-46: 0 = CALL, 1 = PUT; other values are rejected on read.
 enum class OptionType : int8_t { CALL = 0, PUT = 1 };

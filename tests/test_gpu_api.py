@@ -203,3 +203,26 @@ int main() {{
     with open(os.path.join(d, "book.out64")) as f:
         gold = np.array(pkg.read_arrays(f.read())[0], dtype=np.float64)
     assert np.max(np.abs(got - gold)) <= 1e-10 * np.max(gold) + 1e-12
+
+
+def test_sort_orders_give_the_same_bits(pkg, pricer, uneven):
+    """-s changes the schedule (which trees share a warp task, in which order),
+    never a tree's arithmetic."""
+    opts, y, _ = uneven
+    for mode in (pkg.BATCHED_FP64, pkg.BATCHED_MIXED):
+        base = pricer.price(opts, y, mode)
+        for s in "WwHhi-":
+            assert np.array_equal(pricer.price(opts, y, mode, sort=s), base), (mode, s)
+    with pytest.raises(pkg.InvalidInput):
+        pricer.price(opts, y, pkg.BATCHED_FP64, sort="x")
+
+
+def test_warp_k_sets(pkg, pricer, uneven):
+    """Restricting or widening the nodes-per-lane set moves trees between warp
+    classes and tiers (K = 1 alone sends every tree wider than 32 nodes to the
+    warp-group tier); prices stay within the mode's bound."""
+    opts, y, ref = uneven
+    for mask in (0xFF, 0xAF, 0x01, 0x10 | 0x40):
+        assert_fp64(pricer.price(opts, y, pkg.BATCHED_FP64, warp_k_mask=mask), ref, f"fp64 mask {mask:#x}")
+    for mask in (0x3AF, 0x3FF, 0x01, 0x200):
+        assert_lowp(pricer.price(opts, y, pkg.BATCHED_MIXED, warp_k_mask=mask), ref, f"mixed mask {mask:#x}")
