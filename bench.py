@@ -334,6 +334,11 @@ def run_ours(args, rank, world, local):
     if dist is not None:
         dist.barrier()
     torch.cuda.synchronize(dev)
+    # NVTX range "timed" marks the measured steps (ncu --nvtx --nvtx-include "timed/"
+    # limits a launch list to them)
+    nvtx = getattr(torch.cuda, "nvtx", None)
+    if nvtx is not None:
+        nvtx.range_push("timed")
     with ClockSampler(local) as clk:
         times, launches, st = device_steps(mode, args.steps, args.warmup)
         torch.cuda.synchronize(dev)
@@ -348,6 +353,8 @@ def run_ours(args, rank, world, local):
             t0 = time.perf_counter()
             pricer.price_host_ptrs(host_ptr, n, y, host_out.data_ptr(), mode)
             e2e_t.append(time.perf_counter() - t0)
+    if nvtx is not None:
+        nvtx.range_pop()
     ms = sum(times) / len(times)
     ms = max_over_ranks(ms, dist, dev)
     e2e_ms = max_over_ranks(1e3 * sum(e2e_t) / len(e2e_t), dist, dev)
