@@ -36,9 +36,22 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "options/sec at <=1e-4 abs err: FP64 tree vs mixed/batched tree vs surrogate"
+# Best CUDA options/s the reference's thesis reports per benchmark set (FP64, FP32):
+# max over cuda-option and cuda-multi of 65,536 / best kernel time, GTX 780 Ti
+# (results/main/option.csv:107,66,266,2796,416,2844,566,2894,876,814,1019,3044;
+# results/main/multi.csv:361,346 for 4_SKEWED).
+THESIS_BEST = {
+    "0_UNIFORM": (2.66e5, 1.24e6), "1_RAND": (7.85e3, 3.29e4), "2_RANDCONSTHEIGHT": (1.22e5, 6.28e5),
+    "3_RANDCONSTWIDTH": (4.40e4, 2.26e5), "4_SKEWED": (5.75e4, 1.47e5), "5_SKEWEDCONSTHEIGHT": (1.01e5, 2.74e5),
+    "6_SKEWEDCONSTWIDTH": (1.05e5, 2.94e5),
+}
 # FLOP per active node of the two sweeps (forward: Q*E*G 2 + 3-term gather 5 +
 # alpha accumulate 2; backward: gather 5 + discount 2), the fixed work unit.
 FLOP_PER_NODE = 16
+
+
+WORKLOAD_NAMES = ["uniform_1k", "uneven_30k", "skewed_100k", "0_uniform", "1_rand", "2_randconstheight",
+                  "3_randconstwidth", "4_skewed", "5_skewedconstheight", "6_skewedconstwidth"]
 
 
 def dist_env():
@@ -323,6 +336,27 @@ def run_ours(args, rank, world, local):
                                  "fp64_tree_ms": tree_q, "x_fp64_tree": tree_q / (wq * 1e3),
                                  "reference": "batched FP64 tree on the same 1M options"}}
         sur.close()
+    # the reference's seven benchmark distributions (65,536 options each, data/yield.in
+    # curve), device time per batch, beside the thesis's best CUDA numbers
+    datasets = None
+    if modes and not args.no_datasets:
+        datasets = {}
+        y15 = pkg.Yield.from_file(os.path.join(ROOT, "tests", "golden", "reference", "yield.in"))
+        for k, name in enumerate(wl.THESIS_DATASETS):
+            dopts = pkg.Options.from_batch(wl.thesis_dataset(k, 65536, seed=k))
+            dsh = pkg.shape(dopts)
+            entry = {"options": dopts.N,
+                     "active_nodes_per_pass": int(np.sum(pkg.active_nodes(dsh["height"], dsh["jmax"])))}
+            for m in (pkg.BATCHED_FP64, pkg.BATCHED_FP32, pkg.BATCHED_MIXED):
+                best = 1e300
+                for _ in range(3):
+                    pricer.price(dopts, y15, m)
+                    best = min(best, pricer.last_stats.total_ms)
+                entry[pkg.MODE_NAMES[m] + "_options_per_s"] = dopts.N / (best * 1e-3)
+            th = THESIS_BEST[name]
+            entry["thesis_best_cuda_fp64_options_per_s"] = th[0]
+            entry["thesis_best_cuda_fp32_options_per_s"] = th[1]
+            datasets[name] = entry
     if modes:
         fp64_rate = modes["batched_fp64"]["options_per_s"]
         plain_rate = modes["plain_fp64"]["options_per_s"]
@@ -403,6 +437,13 @@ def run_ours(args, rank, world, local):
         }
         if surrogate is not None:
             line["surrogate"] = surrogate
+        if datasets is not None:
+            line["thesis_datasets"] = {
+                "note": "distributions of data-generator/RandomDataGenerator.cpp (seeded numpy draws, not the "
+                        "reference's files); device time per batch (sizing + pricing, no transfers), best of 3; "
+                        "thesis numbers: best CUDA kernel time on a GTX 780 Ti over versions, block sizes and sorts "
+                        "(results/main/option.csv, multi.csv)",
+                "sets": datasets}
         if cpu is not None:
             line["cpu_baseline"] = cpu
         print(json.dumps(line))
@@ -418,13 +459,14 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="uneven_30k", choices=["uniform_1k", "uneven_30k", "skewed_100k"])
+    ap.add_argument("--workload", default="uneven_30k", choices=sorted(WORKLOAD_NAMES))
     ap.add_argument("--mode", default="mixed", choices=["mixed", "fp64", "fp32", "plain"])
     ap.add_argument("--ref-sample", type=int, default=6000)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="library defaults instead of the autotuned configuration")
     ap.add_argument("--skip-survey", action="store_true", help="time only the headline mode (profiling runs)")
     ap.add_argument("--no-surrogate", action="store_true")
+    ap.add_argument("--no-datasets", action="store_true", help="skip the seven thesis benchmark distributions")
     ap.add_argument("--sur-samples", type=int, default=4_000_000)
     ap.add_argument("--sur-epochs", type=int, default=24)
     args = ap.parse_args()

@@ -125,6 +125,11 @@ _SIGNATURES = {
                                          ctypes.POINTER(ctypes.c_double)]),
     "hwt_price_device_noalloc": (ctypes.c_int, [ctypes.POINTER(_Options), ctypes.POINTER(_Yield), ctypes.c_int,
                                                 ctypes.c_void_p, ctypes.c_void_p]),
+    "hwt_read_options": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(_Options), ctypes.c_char_p, ctypes.c_int]),
+    "hwt_free_options": (None, [ctypes.POINTER(_Options)]),
+    "hwt_write_options_bin": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(_Options)]),
+    "hwt_read_yield": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(_Yield), ctypes.c_char_p, ctypes.c_int]),
+    "hwt_free_yield": (None, [ctypes.POINTER(_Yield)]),
 }
 
 
@@ -226,15 +231,43 @@ class Options:
     @classmethod
     def from_file(cls, filename: str) -> "Options":
         """Options(const std::string&) (common/Options.hpp:73-98): eight arrays in
-        field order; a type other than 0/1 is out_of_range."""
+        field order (or a binary cache file from to_bin); a type other than 0/1 is
+        rejected.  Parsed by the library's threaded reader (hwt_read_options)."""
         if not filename:
             raise ValueError("File not specified.")
         if not os.path.exists(filename):
             raise ValueError(f"File '{filename}' does not exist.")
-        with open(filename) as f:
-            arrs = read_arrays(f.read())
+        o = _Options()
+        err = ctypes.create_string_buffer(512)
+        rc = lib().hwt_read_options(filename.encode(), ctypes.byref(o), err, len(err))
+        if rc != 0:
+            msg = err.value.decode()
+            # the reference throws out_of_range for a bad type, invalid_argument otherwise
+            raise (IndexError if msg.startswith("Invalid OptionType") else ValueError)(msg)
+        try:
+            n = o.n
+
+            def arr(ptr, dt):
+                return np.ctypeslib.as_array((ctypes.c_char * (n * np.dtype(dt).itemsize)).from_address(ptr)) \
+                    .view(dt).copy() if n else np.zeros(0, dtype=dt)
+            return cls(arr(o.strike, np.float64), arr(o.bond_maturity, np.float64), arr(o.option_maturity, np.float64),
+                       arr(o.term_unit, np.uint16), arr(o.term_steps, np.uint16), arr(o.a, np.float64),
+                       arr(o.sigma, np.float64), arr(o.type, np.int8))
+        finally:
+            lib().hwt_free_options(ctypes.byref(o))
+
+    def to_bin(self, filename: str) -> None:
+        """Writes the binary cache file hwt_read_options / from_file read back."""
+        o = self._c()
+        if lib().hwt_write_options_bin(filename.encode(), ctypes.byref(o)) != 0:
+            raise OSError(f"cannot write '{filename}'")
+
+    @classmethod
+    def from_text(cls, text: str) -> "Options":
+        """Parses the eight "[..]" arrays of a text in Python (common/Arrays.hpp:15-32)."""
+        arrs = read_arrays(text)
         if len(arrs) < 8:
-            raise ValueError(f"File '{filename}' holds {len(arrs)} arrays, expected 8.")
+            raise ValueError(f"The text holds {len(arrs)} arrays, expected 8.")
         types = np.array([int(float(t)) for t in arrs[7]], dtype=np.int64)
         if np.any((types != 0) & (types != 1)):
             raise IndexError("Invalid OptionType read from stream.")
@@ -297,9 +330,17 @@ class Yield:
             raise ValueError("File not specified.")
         if not os.path.exists(filename):
             raise ValueError("File does not exist.")
-        with open(filename) as f:
-            arrs = read_arrays(f.read())
-        return cls(np.array(arrs[0], dtype=np.float64), np.array([int(float(t)) for t in arrs[1]]))
+        y = _Yield()
+        err = ctypes.create_string_buffer(512)
+        if lib().hwt_read_yield(filename.encode(), ctypes.byref(y), err, len(err)) != 0:
+            raise ValueError(err.value.decode())
+        try:
+            n = y.n
+            rates = np.ctypeslib.as_array((ctypes.c_double * n).from_address(y.rate)).copy()
+            days = np.ctypeslib.as_array((ctypes.c_int32 * n).from_address(y.day)).copy()
+        finally:
+            lib().hwt_free_yield(ctypes.byref(y))
+        return cls(rates, days)
 
     def _c(self) -> _Yield:
         return _Yield(self.N, self.Prices.ctypes.data, self.TimeSteps.ctypes.data)

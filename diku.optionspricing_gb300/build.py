@@ -26,6 +26,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "--expt-relaxed-constexpr", "-I" + INCLUDE, "-I" + CSRC]
 CU_SOURCES = ["hwt_batched.cu", "hwt_plain.cu", "hwt_api.cu", "hwt_noalloc.cu", "hwt_surrogate.cu"]
+HOST_SOURCES = ["hwt_io.cpp"]  # host-only code of the library (g++)
 TOOLS = {"hwt-price": "tools/price_main.cpp", "hwt-compare": "tools/compare_main.cpp"}
 
 
@@ -64,13 +65,19 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
         if _stale(o, [s] + headers) or ptxas_info:
             extra = ["-Xptxas", "-v"] if ptxas_info else []
             jobs.append([cc] + ARCH + NVCC_FLAGS + extra + ["-c", s, "-o", o])
+    for src in HOST_SOURCES:
+        s = os.path.join(CSRC, src)
+        o = os.path.join(OUT, src.replace(".cpp", ".o"))
+        objs.append(o)
+        if _stale(o, [s] + headers):
+            jobs.append(["g++", "-std=c++17", "-O2", "-fPIC", "-pthread", "-I" + INCLUDE, "-I" + CSRC, "-c", s, "-o", o])
     logs = []
     if jobs:
         with cf.ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
             logs = list(ex.map(_run, jobs))
     lib = os.path.join(OUT, "libhwtree.so")
     if jobs or not os.path.exists(lib):
-        _run([cc] + ARCH + ["-shared", "-o", lib] + objs)
+        _run([cc] + ARCH + ["-shared", "-o", lib] + objs + ["-Xcompiler", "-pthread"])
     tool_jobs = []
     for name, src in TOOLS.items():
         s = os.path.join(CSRC, src)

@@ -9,6 +9,7 @@
 //   -r|--runs R         time R runs and print "mode,block,sort,kernel_us,total_us,bytes"
 //   -d|--device D       CUDA device
 //   -t|--test           human-readable timing instead of the price array
+//   -w|--write-bin FILE write the options as a binary cache file (read back by -o) and exit
 // Without -r the prices are printed as one "[p0, p1, ...]" array, the format
 // test/Compare reads.
 #include <cstdio>
@@ -23,7 +24,7 @@
 namespace {
 
 struct Args {
-    std::string options, yield;
+    std::string options, yield, write_bin;
     std::vector<int> modes, blocks;
     std::vector<char> sorts;
     int runs = 0, device = 0;
@@ -55,6 +56,7 @@ Args parse(int argc, char **argv)
         else if (f == "-r" || f == "--runs") a.runs = std::atoi(one().c_str());
         else if (f == "-d" || f == "--device") a.device = std::atoi(one().c_str());
         else if (f == "-t" || f == "--test") a.test = true;
+        else if (f == "-w" || f == "--write-bin") a.write_bin = one();
         else throw std::invalid_argument("unknown flag " + f);
     }
     if (a.modes.empty()) a.modes.push_back(HWT_BATCHED_FP64);
@@ -71,6 +73,10 @@ int main(int argc, char **argv)
         const Args args = parse(argc, argv);
         if (args.test) std::cout << "Loading options " << args.options << ", yield " << args.yield << std::endl;
         hwtree::Options options(args.options);
+        if (!args.write_bin.empty()) {
+            options.writeBinary(args.write_bin);
+            return 0;
+        }
         hwtree::Yield yield(args.yield);
         hwtree::Pricer pricer(args.device);
         for (int mode : args.modes) {

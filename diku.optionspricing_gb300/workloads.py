@@ -105,11 +105,99 @@ def book_batch(count=100):
                   np.full(count, 0.1), np.full(count, 0.01), np.ones(count))
 
 
+# ---------------------------------------------------------------------------
+# The reference's seven benchmark distributions
+# ---------------------------------------------------------------------------
+# data-generator/RandomDataGenerator.cpp:114-257 writes the seven data/*.in sets
+# the thesis benchmarks (65,536 options each): every option is a PUT on a bond,
+# option maturity 3 y, strike 63, term unit 365, 12 steps per year, sigma 0.01;
+# what varies is the bond maturity T (tree height 12 T + 1) and the tree width,
+# which the generator sets through the mean reversion a.  It draws widths from a
+# table of odd widths 7..1023 with a 5-decimal `a` for each; here `a` is computed
+# for any odd width from the width formula itself (reversion_rate_for_width), and
+# the draws come from numpy's generator instead of C rand(), so the sets have the
+# reference's distributions, not its exact records.
+
+THESIS_DATASETS = ("0_UNIFORM", "1_RAND", "2_RANDCONSTHEIGHT", "3_RANDCONSTWIDTH", "4_SKEWED",
+                   "5_SKEWEDCONSTHEIGHT", "6_SKEWEDCONSTWIDTH")
+
+
+def reversion_rate_for_width(width, steps_per_year=12):
+    """Mean reversion a for which the reference's width formula
+    (common/OptionConstants.hpp:45-52: jmax = (int)(-0.184 / (exp(-a dt) - 1)) + 1,
+    width = 2 jmax + 1, dt = 1 / steps_per_year at term unit 365) gives `width`
+    (odd, >= 5): the midpoint of the interval of a that truncates to that jmax."""
+    w = np.asarray(width, dtype=np.int64)
+    if np.any(w % 2 == 0) or np.any(w < 5):
+        raise ValueError("widths are odd and at least 5")
+    jmax = (w - 1) // 2
+    dt = 1.0 / steps_per_year
+    # -0.184 / (exp(-a dt) - 1) in [jmax - 1, jmax)  <=>  a in (a_lo, a_hi]
+    a_lo = -np.log1p(-0.184 / jmax) / dt
+    a_hi = -np.log1p(-0.184 / (jmax - 1)) / dt
+    return 0.5 * (a_lo + a_hi)
+
+
+def _odd_widths(rng, lo, hi, n):
+    """Uniform draws from the odd widths in [lo, hi]."""
+    first = lo if lo % 2 else lo + 1
+    count = (hi - first) // 2 + 1
+    return first + 2 * rng.integers(0, count, n)
+
+
+def thesis_dataset(kind, n=65536, skew_percent=1, seed=0):
+    """One of the reference's seven benchmark distributions (kind 0..6 or its name),
+    n options, shuffled:
+      0 UNIFORM            T = 9, a = 0.1 (width 47)
+      1 RAND               T U{1..100}, width U(odd 7..511)
+      2 RANDCONSTHEIGHT    T = 9, width U(odd 7..511)
+      3 RANDCONSTWIDTH     T U{1..100}, a = 0.1
+      4 SKEWED             skew%: T U{70..100}, width U(odd 411..511); rest T U{1..30}, width U(odd 7..107)
+      5 SKEWEDCONSTHEIGHT  skew%: T = 100, width U(odd 7..107); rest as in 4
+      6 SKEWEDCONSTWIDTH   skew%: T U{1..30}, one width from U(odd 509..511); rest as in 4
+    (RandomDataGenerator.cpp:114-257; the skewed share is ceil(skew% x n))."""
+    if isinstance(kind, str):
+        kind = THESIS_DATASETS.index(kind)
+    rng = np.random.default_rng(seed)
+    n_skew = int(np.ceil(skew_percent / 100.0 * n)) if kind >= 4 else 0
+    n_rest = n - n_skew
+    a = np.full(n, 0.1)
+    if kind == 0:
+        T = np.full(n, 9)
+    elif kind == 1:
+        T = rng.integers(1, 101, n)
+        a = reversion_rate_for_width(_odd_widths(rng, 7, 511, n))
+    elif kind == 2:
+        T = np.full(n, 9)
+        a = reversion_rate_for_width(_odd_widths(rng, 7, 511, n))
+    elif kind == 3:
+        T = rng.integers(1, 101, n)
+    else:
+        if kind == 4:
+            T_s = rng.integers(70, 101, n_skew)
+            w_s = _odd_widths(rng, 411, 511, n_skew)
+        elif kind == 5:
+            T_s = np.full(n_skew, 100)
+            w_s = _odd_widths(rng, 7, 107, n_skew)
+        elif kind == 6:
+            T_s = rng.integers(1, 31, n_skew)
+            w_s = np.full(n_skew, _odd_widths(rng, 509, 511, 1)[0])
+        else:
+            raise ValueError(f"unknown dataset kind {kind}")
+        T = np.concatenate([T_s, rng.integers(1, 31, n_rest)])
+        a = reversion_rate_for_width(np.concatenate([w_s, _odd_widths(rng, 7, 107, n_rest)]))
+    perm = rng.permutation(n)
+    T = np.asarray(T, dtype=np.float64)[perm]
+    a = np.asarray(a, dtype=np.float64)[perm]
+    return _batch(np.full(n, 63.0), T, np.full(n, 3.0), np.full(n, 12), a, np.full(n, 0.01), np.ones(n))
+
+
 WORKLOADS = {
     "uniform_1k": uniform_book,
     "uneven_30k": uneven_batch,
     "skewed_100k": skewed_batch,
 }
+WORKLOADS.update({name.lower(): (lambda k: (lambda: thesis_dataset(k)))(k) for k, name in enumerate(THESIS_DATASETS)})
 
 
 # ---------------------------------------------------------------------------

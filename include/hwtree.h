@@ -277,6 +277,22 @@ int hwt_surrogate_forward(hwt_surrogate *s, const float *x, int n, float *out);
 int hwt_surrogate_loss_grads(hwt_surrogate *s, const float *x, const float *y, int n, double *loss,
                              float *grads);
 
+/* ---- Input files ------------------------------------------------------------
+ * Replace trinom::Options(const std::string&) and trinom::Yield(const
+ * std::string&) (common/Options.hpp:73-98, common/Yield.hpp:20-38), which read
+ * the "[..]" arrays value by value with iostream extraction.  hwt_read_options
+ * parses the eight arrays with host threads (values correctly rounded, the same
+ * doubles as the reference's reader; integer fields must be integral and in
+ * range; types 0 or 1), or reads a binary cache file written by
+ * hwt_write_options_bin (recognised by its magic), into arrays the library
+ * allocates; hwt_free_options releases them.  On error the message goes to
+ * err[err_len] (may be NULL).  No GPU is needed. */
+int hwt_read_options(const char *path, hwt_options *out, char *err, int err_len);
+void hwt_free_options(hwt_options *opts);
+int hwt_write_options_bin(const char *path, const hwt_options *opts);
+int hwt_read_yield(const char *path, hwt_yield *out, char *err, int err_len);
+void hwt_free_yield(hwt_yield *yield);
+
 #ifdef __cplusplus
 }
 #endif

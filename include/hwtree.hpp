@@ -17,6 +17,7 @@
 #include <stdexcept>
 #include <string>
 #include <type_traits>
+#include <cstring>
 #include <vector>
 
 #include "hwtree.h"
@@ -85,24 +86,38 @@ struct Options {
         TermStepCounts.reserve(N); ReversionRates.reserve(N); Volatilities.reserve(N); Types.reserve(N);
     }
 
+    // Reads a .in text file (or the library's binary cache) with the library's
+    // threaded reader (hwt_read_options); same values as the stream reader.
     explicit Options(const std::string &filename)
     {
         if (filename.empty()) throw std::invalid_argument("File not specified.");
-        std::ifstream in(filename);
-        if (!in) throw std::invalid_argument("File '" + filename + "' does not exist.");
-        Arrays::read_array(in, StrikePrices);
-        Arrays::read_array(in, Maturities);
-        Arrays::read_array(in, Lengths);
-        Arrays::read_array(in, TermUnits);
-        Arrays::read_array(in, TermStepCounts);
-        Arrays::read_array(in, ReversionRates);
-        Arrays::read_array(in, Volatilities);
-        Arrays::read_array(in, Types);
-        N = (int)StrikePrices.size();
-        const size_t n = StrikePrices.size();
-        if (Maturities.size() != n || Lengths.size() != n || TermUnits.size() != n || TermStepCounts.size() != n ||
-            ReversionRates.size() != n || Volatilities.size() != n || Types.size() != n)
-            throw std::invalid_argument("File '" + filename + "' has option arrays of different lengths.");
+        hwt_options o;
+        char err[512];
+        const int rc = hwt_read_options(filename.c_str(), &o, err, (int)sizeof(err));
+        if (rc != HWT_OK) {
+            if (std::strncmp(err, "Invalid OptionType", 18) == 0) throw std::out_of_range(err);
+            throw std::invalid_argument(err);
+        }
+        const size_t n = (size_t)o.n;
+        StrikePrices.assign(o.strike, o.strike + n);
+        Maturities.assign(o.bond_maturity, o.bond_maturity + n);
+        Lengths.assign(o.option_maturity, o.option_maturity + n);
+        TermUnits.assign(o.term_unit, o.term_unit + n);
+        TermStepCounts.assign(o.term_steps, o.term_steps + n);
+        ReversionRates.assign(o.a, o.a + n);
+        Volatilities.assign(o.sigma, o.sigma + n);
+        Types.resize(n);
+        for (size_t i = 0; i < n; ++i) Types[i] = static_cast<OptionType>(o.type[i]);
+        N = (int)n;
+        hwt_free_options(&o);
+    }
+
+    // Writes the binary cache file the reader above recognises.
+    void writeBinary(const std::string &filename) const
+    {
+        const hwt_options o = view();
+        if (hwt_write_options_bin(filename.c_str(), &o) != HWT_OK)
+            throw std::invalid_argument("cannot write '" + filename + "'");
     }
 
     void writeToFile(const std::string &filename) const
