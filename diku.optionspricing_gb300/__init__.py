@@ -29,7 +29,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libhwtree.so")
 
 # Status codes (hwtree.h)
-HWT_OK, HWT_EINVAL, HWT_ECUDA, HWT_ENOMEM, HWT_EUNSUPPORTED, HWT_ENODEV = 0, -1, -2, -3, -4, -5
+HWT_OK, HWT_EINVAL, HWT_ECUDA, HWT_ENOMEM, HWT_EUNSUPPORTED, HWT_ENODEV, HWT_ETIMEOUT = 0, -1, -2, -3, -4, -5, -6
 
 # Pricing modes (hwtree.h)
 PLAIN_FP64, BATCHED_FP64, BATCHED_FP32, BATCHED_MIXED = 0, 1, 2, 3

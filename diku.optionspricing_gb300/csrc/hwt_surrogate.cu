@@ -1,7 +1,8 @@
 // Learned surrogate: a 7 -> 256 -> 256 -> 256 -> 256 -> 1 SiLU MLP that maps
 // standardised option parameters to price / forward bond price.  Weights are
-// kept as fp32 masters with bf16 copies for the tensor-core GEMMs
-// (hwt_mlp.cuh); activations between layers are bf16, accumulation fp32.
+// kept as fp32 masters with bf16 copies for the tcgen05 tensor-core GEMMs
+// (hwt_umma.cuh); activations between layers are bf16, accumulation fp32 in
+// tensor memory.
 // Training: Adam with cosine decay on labels priced by the batched FP64 tree.
 // Inference: options inside the training box go through the network, the rest
 // to the tree; a random sample of the in-box options is re-priced by the tree
@@ -18,11 +19,11 @@
 
 #include "../../include/hwtree.h"
 #include "hwt_internal.h"
-#include "hwt_mlp.cuh"
+#include "hwt_umma.cuh"
 #include "hwt_model.cuh"
 
 using namespace hwt;
-using namespace hwt::mlp;
+using namespace hwt::umma;
 
 namespace {
 
@@ -225,6 +226,7 @@ struct hwt_surrogate {
     float *d_dzf = nullptr;
     double *d_loss = nullptr;
     float *d_y = nullptr;
+    int *d_gemm_err = nullptr;  // raised by a GEMM whose mbarrier wait ran out
 };
 
 namespace {
@@ -262,20 +264,46 @@ int ensure_act(hwt_surrogate *s, int rows)
     return HWT_OK;
 }
 
-template <bool TA, bool TB>
-cudaError_t gemm(const GemmArgs &a, int splits, cudaStream_t st)
+template <bool TA, bool TB, int BN>
+cudaError_t gemm_bn(const GemmArgs &a, int splits, cudaStream_t st)
 {
+    auto kern = umma_gemm_kernel<TA, TB, BN>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes(BN));
+    if (e != cudaSuccess) return e;
     dim3 grid((a.N + BN - 1) / BN, (a.M + BM - 1) / BM, splits);
-    gemm_kernel<TA, TB><<<grid, GEMM_THREADS, 0, st>>>(a);
+    kern<<<grid, THREADS, smem_bytes(BN), st>>>(a);
     return cudaGetLastError();
 }
 
-GemmArgs gargs(const __nv_bfloat16 *A, const __nv_bfloat16 *B, int M, int N, int K, int lda, int ldb, int epi)
+// Tile width: the output width rounded up to 16 (one tile for the 1-wide output
+// layer), at most 128 so that a 256-wide layer spreads over two column tiles.
+template <bool TA, bool TB>
+cudaError_t gemm(const GemmArgs &a, int splits, cudaStream_t st)
+{
+    if (a.N <= 16) return gemm_bn<TA, TB, 16>(a, splits, st);
+    if (a.N <= 64) return gemm_bn<TA, TB, 64>(a, splits, st);
+    return gemm_bn<TA, TB, 128>(a, splits, st);
+}
+
+GemmArgs gargs(const hwt_surrogate *s, const __nv_bfloat16 *A, const __nv_bfloat16 *B, int M, int N, int K, int lda,
+               int ldb, int epi)
 {
     GemmArgs g;
     memset(&g, 0, sizeof(g));
-    g.A = A; g.B = B; g.M = M; g.N = N; g.K = K; g.lda = lda; g.ldb = ldb; g.k_chunk = K; g.epi = epi;
+    g.A = A; g.B = B; g.M = M; g.N = N; g.K = K; g.lda = lda; g.ldb = ldb; g.epi = epi;
+    g.k_chunk = (K + BK - 1) / BK * BK;
+    g.err = s->d_gemm_err;
     return g;
+}
+
+// HWT_ETIMEOUT (and the flag cleared) if a GEMM gave up waiting since the last check.
+int gemm_status(hwt_surrogate *s)
+{
+    int flag = 0;
+    SCUDA(s, cudaMemcpy(&flag, s->d_gemm_err, sizeof(int), cudaMemcpyDeviceToHost), "GEMM status");
+    if (flag == 0) return HWT_OK;
+    SCUDA(s, cudaMemset(s->d_gemm_err, 0, sizeof(int)), "GEMM status");
+    return sfail(s, HWT_ETIMEOUT, "tensor-core GEMM: an mbarrier wait ran out");
 }
 
 // Forward through all layers for `rows` samples already in d_h[0].  Output
@@ -284,7 +312,7 @@ int forward(hwt_surrogate *s, int rows)
 {
     for (int l = 0; l < kLayers; ++l) {
         const bool last = l == kLayers - 1;
-        GemmArgs g = gargs(s->d_h[l], s->d_wt[l], rows, kFanOut[l], kFanIn[l], kFanIn[l], kFanIn[l],
+        GemmArgs g = gargs(s, s->d_h[l], s->d_wt[l], rows, kFanOut[l], kFanIn[l], kFanIn[l], kFanIn[l],
                            last ? EPI_BIAS : EPI_BIAS_SILU);
         g.bias = s->d_w + s->b_off[l];
         g.Cf = s->d_z[l];
@@ -310,7 +338,7 @@ int backward(hwt_surrogate *s, int rows, bool zero_loss)
     for (int l = kLayers - 1; l >= 0; --l) {
         const int in = kFanIn[l], out = kFanOut[l];
         // dW_l[in][out] = H_l^T dZ_l   (split-K over the batch)
-        GemmArgs gw = gargs(s->d_h[l], dz, in, out, rows, in, out, EPI_ATOMIC);
+        GemmArgs gw = gargs(s, s->d_h[l], dz, in, out, rows, in, out, EPI_ATOMIC);
         gw.Cf = s->d_g + s->w_off[l];
         gw.ldc = out;
         gw.k_chunk = kc;
@@ -321,7 +349,7 @@ int backward(hwt_surrogate *s, int rows, bool zero_loss)
         SCUDA(s, cudaGetLastError(), "db kernel");
         if (l == 0) break;
         // dZ_{l-1} = (dZ_l W_l^T) * silu'(Z_{l-1})
-        GemmArgs gd = gargs(dz, s->d_wb[l], rows, in, out, out, out, EPI_DSILU);
+        GemmArgs gd = gargs(s, dz, s->d_wb[l], rows, in, out, out, out, EPI_DSILU);
         gd.Zin = s->d_z[l - 1];
         gd.Cf = s->d_dzf;
         gd.ldc = in;
@@ -390,7 +418,8 @@ hwt_surrogate *hwt_surrogate_create(hwt_ctx *ctx, const hwt_box *box, uint64_t s
     s->n_params = off;
     ok = ok && cudaMalloc(&s->d_w, 4 * off) == cudaSuccess && cudaMalloc(&s->d_m, 4 * off) == cudaSuccess &&
          cudaMalloc(&s->d_v, 4 * off) == cudaSuccess && cudaMalloc(&s->d_g, 4 * off) == cudaSuccess &&
-         cudaMalloc(&s->d_loss, sizeof(double)) == cudaSuccess;
+         cudaMalloc(&s->d_loss, sizeof(double)) == cudaSuccess &&
+         cudaMalloc(&s->d_gemm_err, sizeof(int)) == cudaSuccess && cudaMemset(s->d_gemm_err, 0, sizeof(int)) == cudaSuccess;
     for (int l = 0; l < kLayers && ok; ++l) {
         ok = cudaMalloc(&s->d_wt[l], 2 * (size_t)kFanIn[l] * kFanOut[l]) == cudaSuccess &&
              cudaMalloc(&s->d_wb[l], 2 * (size_t)kFanIn[l] * kFanOut[l]) == cudaSuccess;
@@ -431,7 +460,7 @@ void hwt_surrogate_destroy(hwt_surrogate *s)
 {
     if (!s) return;
     if (s->stream) cudaStreamSynchronize(s->stream);
-    cudaFree(s->d_w); cudaFree(s->d_m); cudaFree(s->d_v); cudaFree(s->d_g); cudaFree(s->d_loss);
+    cudaFree(s->d_w); cudaFree(s->d_m); cudaFree(s->d_v); cudaFree(s->d_g); cudaFree(s->d_loss); cudaFree(s->d_gemm_err);
     for (int l = 0; l < kLayers; ++l) { cudaFree(s->d_wt[l]); cudaFree(s->d_wb[l]); cudaFree(s->d_z[l]); }
     for (int l = 0; l <= kLayers; ++l) cudaFree(s->d_h[l]);
     cudaFree(s->d_dz); cudaFree(s->d_dz2); cudaFree(s->d_dzf); cudaFree(s->d_y);
@@ -469,7 +498,7 @@ int hwt_surrogate_forward(hwt_surrogate *s, const float *x, int n, float *out)
     if ((r = forward(s, n))) return r;
     SCUDA(s, cudaMemcpyAsync(out, s->d_z[kLayers - 1], 4 * (size_t)n, cudaMemcpyDeviceToHost, s->stream), "out D2H");
     SCUDA(s, cudaStreamSynchronize(s->stream), "forward");
-    return HWT_OK;
+    return gemm_status(s);
 }
 
 int hwt_surrogate_loss_grads(hwt_surrogate *s, const float *x, const float *y, int n, double *loss, float *grads)
@@ -489,7 +518,7 @@ int hwt_surrogate_loss_grads(hwt_surrogate *s, const float *x, const float *y, i
     SCUDA(s, cudaMemcpyAsync(&l, s->d_loss, sizeof(double), cudaMemcpyDeviceToHost, s->stream), "loss D2H");
     SCUDA(s, cudaStreamSynchronize(s->stream), "grads");
     if (loss) *loss = l;
-    return HWT_OK;
+    return gemm_status(s);
 }
 
 }  // extern "C"
@@ -735,7 +764,7 @@ int hwt_surrogate_train(hwt_surrogate *s, const hwt_options *samples, const hwt_
         stats->y_mean = s->ymean;
         stats->y_std = s->ystd;
     }
-    return HWT_OK;
+    return gemm_status(s);
 }
 
 int hwt_surrogate_price(hwt_surrogate *s, const hwt_options *o, const hwt_yield *y, double judge_fraction,
@@ -872,7 +901,7 @@ int hwt_surrogate_price(hwt_surrogate *s, const hwt_options *o, const hwt_yield 
         stats->total_ms = t1 + fallback_ms;
     }
     for (auto &e : ev) cudaEventDestroy(e);
-    return HWT_OK;
+    return gemm_status(s);
 }
 
 int hwt_surrogate_save(const hwt_surrogate *s, const char *path)

@@ -38,6 +38,8 @@ extern "C" {
 #define HWT_ENOMEM (-3)      /* device or pinned host allocation failed */
 #define HWT_EUNSUPPORTED (-4)/* mode not available for these inputs */
 #define HWT_ENODEV (-5)      /* no CUDA device */
+#define HWT_ETIMEOUT (-6)    /* a bounded device-side wait ran out; the kernel gave up and the
+                                context stays usable */
 
 /* Pricing modes.  The reference selects precision at compile time
  * (common/Real.hpp:9-21); here it is a run-time argument. */
