@@ -550,6 +550,7 @@ _SIGNATURES.update({
     "hwt_surrogate_param_count": (ctypes.c_int64, [ctypes.c_void_p]),
     "hwt_surrogate_params": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int]),
     "hwt_surrogate_forward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
+    "hwt_surrogate_inject_stall": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "hwt_surrogate_loss_grads": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                                                 ctypes.POINTER(ctypes.c_double), ctypes.c_void_p]),
 })
@@ -627,6 +628,11 @@ class Surrogate:
         flat = np.concatenate([np.concatenate([np.asarray(W, np.float32).ravel(), np.asarray(b, np.float32)])
                                for W, b in params]).astype(np.float32)
         self._check(lib().hwt_surrogate_params(self._s, flat.ctypes.data, len(flat), 1))
+
+    def inject_stall(self, on: bool) -> None:
+        """Test hook: GEMMs wait on an mbarrier phase nothing completes (bounded),
+        so calls return HWT_ETIMEOUT; the context stays usable."""
+        self._check(lib().hwt_surrogate_inject_stall(self._s, 1 if on else 0))
 
     def forward(self, x: np.ndarray) -> np.ndarray:
         x = np.ascontiguousarray(x, dtype=np.float32)

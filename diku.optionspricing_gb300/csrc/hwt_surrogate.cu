@@ -104,9 +104,16 @@ __global__ void colsum_kernel(const float *d, int n, int cols, int ld, float *db
     if (c >= cols) return;
     const int rows_per = (n + gridDim.y - 1) / gridDim.y;
     const int r0 = blockIdx.y * rows_per, r1 = min(n, r0 + rows_per);
-    float s = 0.f;
-    for (int r = r0; r < r1; ++r) s += d[(size_t)r * ld + c];
-    atomicAdd(db + c, s);
+    float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;  // four independent chains of loads
+    int r = r0;
+    for (; r + 4 <= r1; r += 4) {
+        s0 += d[(size_t)r * ld + c];
+        s1 += d[(size_t)(r + 1) * ld + c];
+        s2 += d[(size_t)(r + 2) * ld + c];
+        s3 += d[(size_t)(r + 3) * ld + c];
+    }
+    for (; r < r1; ++r) s0 += d[(size_t)r * ld + c];
+    atomicAdd(db + c, (s0 + s1) + (s2 + s3));
 }
 
 struct AdamArgs {
@@ -227,6 +234,7 @@ struct hwt_surrogate {
     double *d_loss = nullptr;
     float *d_y = nullptr;
     int *d_gemm_err = nullptr;  // raised by a GEMM whose mbarrier wait ran out
+    int stall = 0;              // fault injection for tests (hwt_surrogate_inject_stall)
 };
 
 namespace {
@@ -293,6 +301,7 @@ GemmArgs gargs(const hwt_surrogate *s, const __nv_bfloat16 *A, const __nv_bfloat
     g.A = A; g.B = B; g.M = M; g.N = N; g.K = K; g.lda = lda; g.ldb = ldb; g.epi = epi;
     g.k_chunk = (K + BK - 1) / BK * BK;
     g.err = s->d_gemm_err;
+    g.test_stall = s->stall;
     return g;
 }
 
@@ -344,7 +353,7 @@ int backward(hwt_surrogate *s, int rows, bool zero_loss)
         gw.k_chunk = kc;
         SCUDA(s, (gemm<true, true>(gw, (rows + kc - 1) / kc, s->stream)), "dW gemm");
         // db_l = column sums of dZ_l (fp32 copy in d_dzf)
-        dim3 cg((out + 255) / 256, std::max(1, std::min(64, rows / 256)));
+        dim3 cg((out + 255) / 256, std::max(1, std::min(256, rows / 32)));
         colsum_kernel<<<cg, 256, 0, s->stream>>>(s->d_dzf, rows, out, out, s->d_g + s->b_off[l]);
         SCUDA(s, cudaGetLastError(), "db kernel");
         if (l == 0) break;
@@ -469,6 +478,13 @@ void hwt_surrogate_destroy(hwt_surrogate *s)
 }
 
 const char *hwt_surrogate_last_error(const hwt_surrogate *s) { return s ? s->err.c_str() : "no surrogate"; }
+
+int hwt_surrogate_inject_stall(hwt_surrogate *s, int on)
+{
+    if (!s) return HWT_EINVAL;
+    s->stall = on ? 1 : 0;
+    return HWT_OK;
+}
 
 int64_t hwt_surrogate_param_count(const hwt_surrogate *s) { return s ? (int64_t)s->n_params : 0; }
 

@@ -9,15 +9,16 @@
 // One CTA of 128 threads computes a 128 x BN tile (BN = 16..256, a multiple of
 // 16) with one tcgen05.mma.cta_group::1.kind::f16 per 16-wide K step (M = 128,
 // N = BN), accumulating in BN columns of TMEM.  K advances in blocks of 64 through
-// STAGES shared-memory stages: operands stored with K contiguous arrive by
-// cp.async (16-byte chunks, zero fill past the edges), STAGES - 1 blocks ahead of
-// the tensor core; operands stored transposed are loaded 16 bytes at a time along
-// their rows and written transposed.  One thread issues a block's four MMAs and
-// commits them to the stage's mbarrier; a stage is refilled once the MMAs that
-// read it have completed.  Operands sit in shared memory in the canonical K-major
-// layout without swizzle: 8 x 8 "core matrices" of 128 contiguous bytes, the
-// K-adjacent core matrices 128 bytes apart (leading byte offset) and the next 8
-// rows 1024 bytes apart (stride byte offset).  The epilogue reads the accumulator
+// STAGES shared-memory stages filled by cp.async (16-byte chunks, zero fill past
+// the edges), STAGES - 1 blocks ahead of the tensor core.  One thread issues a
+// block's four MMAs and commits them to the stage's mbarrier; a stage is refilled
+// once the MMAs that read it have completed.  Operands sit in shared memory in the
+// canonical layouts without swizzle, made of 8 x 8 "core matrices" of 128
+// contiguous bytes: K-major for operands stored with K contiguous, MN-major for
+// operands stored transposed (the weight-gradient product), so that every copy
+// moves 16 contiguous bytes.  In both layouts the descriptors' leading byte offset
+// is the K-direction core-matrix stride and the stride byte offset the
+// MN-direction one (each reading checked on GB300 against the swapped one).  The epilogue reads the accumulator
 // with tcgen05.ld (warp w owns TMEM lanes 32w..32w+31 = tile rows), 16 columns at
 // a time, and applies the surrogate's fused operations (bias + SiLU, bias,
 // dY * SiLU'(Z), split-K atomics) with 16-byte loads and stores.
@@ -57,6 +58,7 @@ struct GemmArgs {
     int ldc, ldcb;
     int epi;
     int *err;            // set to 1 by a CTA whose mbarrier wait ran out
+    int test_stall;      // fault injection: first wait on a phase nothing completes
 };
 
 // Dynamic shared memory of one CTA for tile width bn.
@@ -168,66 +170,75 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
 // Element offset of (row r, k) in a K-major no-swizzle tile with BK columns.
 __device__ __forceinline__ int core_offset(int r, int k) { return (((r >> 3) * (BK / 8) + (k >> 3)) << 6) + ((r & 7) << 3) + (k & 7); }
 
-__device__ __forceinline__ void cp_async16(uint32_t dst, const void *src, bool valid)
-{
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(valid ? 16 : 0) : "memory");
-}
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
-// Stages rows [row0, row0+ROWS) x K [k0, k0+BK) of an operand into sh (core-matrix
-// layout); out-of-range elements are zero.
-//  * K contiguous (element (r, k) at r * ld + k), `async`: 16-byte cp.async chunks
-//    (needs ld % 8 == 0, a 16-byte aligned base and kend % 8 == 0);
-//  * K contiguous otherwise: element loads;
-//  * transposed (element (r, k) at k * ld + r): 16-byte loads of 8 rows at one k
-//    when ld % 8 == 0 and the base is aligned, written to the 8 rows' slots.
-__device__ __forceinline__ void stage(__nv_bfloat16 *sh, int ROWS, const __nv_bfloat16 *g, int row0, int k0,
-                                      int rows, int kend, int ld, bool trans, bool vec)
+// Element offset of (row r, k) in an MN-major no-swizzle tile of ROWS rows: a core
+// matrix holds 8 K-rows of 8 consecutive rows (16 bytes each); MN-adjacent core
+// matrices are 128 bytes apart, K-adjacent ones (ROWS / 8) * 128 bytes.
+template <int ROWS>
+__device__ __forceinline__ int mn_offset(int r, int k) { return (((k >> 3) * (ROWS / 8) + (r >> 3)) << 6) + ((k & 7) << 3) + (r & 7); }
+
+// Stages rows [row0, row0+ROWS) x K [k0, k0+BK) of an operand into sh; elements
+// past the edges are zero.
+//  * TRANS = false (element (r, k) at r * ld + k): K-major tile;
+//  * TRANS = true (element (r, k) at k * ld + r): MN-major tile,
+// so that both read 16 contiguous bytes per copy.  With `vec` (ld % 8 == 0 and a
+// 16-byte aligned base) every 16-byte chunk is one cp.async whose byte count
+// zero-fills what lies past the edge, and a warp writes whole core matrices;
+// otherwise element copies.
+template <int ROWS, bool TRANS>
+__device__ __forceinline__ void stage(__nv_bfloat16 *sh, const __nv_bfloat16 *g, int row0, int k0, int rows, int kend,
+                                      int ld, bool vec)
 {
     const __nv_bfloat16 zero = __float2bfloat16(0.f);
-    if (!trans) {
+    if (vec) {
         for (int idx = threadIdx.x; idx < ROWS * (BK / 8); idx += THREADS) {
-            const int r = idx / (BK / 8), c8 = (idx % (BK / 8)) * 8;
-            const int gr = row0 + r, gk = k0 + c8;
-            __nv_bfloat16 *dst = sh + core_offset(r, c8);
-            if (vec) {
-                const bool in = gr < rows && gk < kend;  // kend % 8 == 0: a chunk is all in or all out
-                cp_async16(smem_u32(dst), in ? (const void *)(g + (size_t)gr * ld + gk) : (const void *)g, in);
+            int n = 0;  // valid elements of the chunk (0..8)
+            const __nv_bfloat16 *src = g;
+            __nv_bfloat16 *dst;
+            if (!TRANS) {
+                // lane -> (row, 8-wide K chunk): one core-matrix row each
+                const int r = idx / (BK / 8), k = (idx % (BK / 8)) * 8;
+                const int gr = row0 + r, gk = k0 + k;
+                n = gr < rows ? max(0, min(8, kend - gk)) : 0;
+                if (n) src = g + (size_t)gr * ld + gk;
+                dst = sh + core_offset(r, k);
             } else {
-#pragma unroll
-                for (int q = 0; q < 8; ++q) dst[q] = (gr < rows && gk + q < kend) ? g[(size_t)gr * ld + gk + q] : zero;
+                // lane -> (k & 7, 8-row chunk, k / 8): 8 lanes fill one core matrix
+                const int kl = idx & 7, rest = idx >> 3;
+                const int rc = rest % (ROWS / 8), kh = rest / (ROWS / 8);
+                const int r = rc * 8, k = kh * 8 + kl;
+                const int gr = row0 + r, gk = k0 + k;
+                n = gk < kend ? max(0, min(8, rows - gr)) : 0;
+                if (n) src = g + (size_t)gk * ld + gr;
+                dst = sh + mn_offset<ROWS>(r, k);
             }
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32(dst)), "l"(src), "r"(2 * n)
+                         : "memory");
         }
-    } else if (vec) {
-        // lane -> (k & 7, 8-row chunk): a warp reads four 16-byte chunks of 8 K rows
-        for (int idx = threadIdx.x; idx < (ROWS / 8) * BK; idx += THREADS) {
-            const int kl = idx & 7, rest = idx >> 3;
-            const int rc = rest % (ROWS / 8), kh = rest / (ROWS / 8);
-            const int k = kh * 8 + kl, r = rc * 8;
+    } else if (!TRANS) {
+        for (int idx = threadIdx.x; idx < ROWS * BK; idx += THREADS) {
+            const int r = idx / BK, k = idx % BK;
             const int gr = row0 + r, gk = k0 + k;
-            uint4 v = make_uint4(0, 0, 0, 0);
-            if (gk < kend && gr + 8 <= rows) {
-                v = *reinterpret_cast<const uint4 *>(g + (size_t)gk * ld + gr);
-            } else if (gk < kend) {
-                __nv_bfloat16 t[8];
-#pragma unroll
-                for (int q = 0; q < 8; ++q) t[q] = gr + q < rows ? g[(size_t)gk * ld + gr + q] : zero;
-                v = *reinterpret_cast<const uint4 *>(t);
-            }
-            const __nv_bfloat16 *e = reinterpret_cast<const __nv_bfloat16 *>(&v);
-            __nv_bfloat16 *dst = sh + core_offset(r, k);
-#pragma unroll
-            for (int q = 0; q < 8; ++q) dst[q * 8] = e[q];  // rows r..r+7 of one core matrix are 8 elements apart
+            sh[core_offset(r, k)] = (gr < rows && gk < kend) ? g[(size_t)gr * ld + gk] : zero;
         }
     } else {
         for (int idx = threadIdx.x; idx < ROWS * BK; idx += THREADS) {
             const int k = idx / ROWS, r = idx % ROWS;  // consecutive threads read consecutive rows
             const int gr = row0 + r, gk = k0 + k;
-            sh[core_offset(r, k)] = (gr < rows && gk < kend) ? g[(size_t)gk * ld + gr] : zero;
+            sh[mn_offset<ROWS>(r, k)] = (gr < rows && gk < kend) ? g[(size_t)gk * ld + gr] : zero;
         }
     }
+}
+
+// Descriptor of the 16-wide K step kk of a staged tile of ROWS rows.
+template <int ROWS, bool TRANS>
+__device__ __forceinline__ uint64_t step_desc(uint32_t base, int kk)
+{
+    if (!TRANS) return make_desc(base + kk * 256, 128, (BK / 8) * 128);
+    return make_desc(base + kk * 2 * (ROWS / 8) * 128, (ROWS / 8) * 128, 128);
 }
 
 template <bool TA, bool TB, int BN>
@@ -247,7 +258,7 @@ __global__ void __launch_bounds__(THREADS) umma_gemm_kernel(GemmArgs p)
     const int kbeg = blockIdx.z * p.k_chunk;
     const int kend = min(kbeg + p.k_chunk, p.K);
     constexpr int NCOLS = tmem_cols(BN);
-    constexpr uint32_t IDESC = make_idesc(BN);
+    constexpr uint32_t IDESC = make_idesc(BN) | ((TA ? 1u : 0u) << 15) | ((TB ? 1u : 0u) << 16);  // MN-major bits
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; ++s) mbar_init(smem_u32(&bars[s]), 1);
@@ -259,14 +270,22 @@ __global__ void __launch_bounds__(THREADS) umma_gemm_kernel(GemmArgs p)
     fence_after_sync();
     const uint32_t tmem = *tmem_slot;
 
-    const bool alignK = (kend % 8 == 0) && (kbeg % 8 == 0);
-    const bool vecA = (p.lda % 8 == 0) && ((reinterpret_cast<uintptr_t>(p.A) & 15) == 0) && (TA || alignK);
-    const bool vecB = (p.ldb % 8 == 0) && ((reinterpret_cast<uintptr_t>(p.B) & 15) == 0) && (TB || alignK);
-    const int nkb = kend > kbeg ? (kend - kbeg + BK - 1) / BK : 0;
+    // 16-byte chunks start at multiples of 8 elements: along K for K-major operands
+    // (kbeg % 8 == 0), along the rows for MN-major ones (tile origins are multiples of 16)
+    const bool vecA = (p.lda % 8 == 0) && ((reinterpret_cast<uintptr_t>(p.A) & 15) == 0) && (TA || kbeg % 8 == 0);
+    const bool vecB = (p.ldb % 8 == 0) && ((reinterpret_cast<uintptr_t>(p.B) & 15) == 0) && (TB || kbeg % 8 == 0);
+    int nkb = kend > kbeg ? (kend - kbeg + BK - 1) / BK : 0;
+    bool ok = true;
+    if (p.test_stall) {
+        // a fresh mbarrier's phase 0 never completes without arrivals: the bounded
+        // wait runs out, and the CTA skips its work and reports it
+        ok = mbar_wait(smem_u32(&bars[0]), 0u);
+        if (!ok) nkb = 0;
+    }
     auto load = [&](int kb) {
         const int s = kb % STAGES, k0 = kbeg + kb * BK;
-        stage(sA[s], BM, p.A, m0, k0, p.M, kend, p.lda, TA, vecA);
-        stage(sB[s], BN, p.B, n0, k0, p.N, kend, p.ldb, TB, vecB);
+        stage<BM, TA>(sA[s], p.A, m0, k0, p.M, kend, p.lda, vecA);
+        stage<BN, TB>(sB[s], p.B, n0, k0, p.N, kend, p.ldb, vecB);
     };
     // prologue: the first STAGES - 1 blocks in flight (one cp.async group each)
 #pragma unroll
@@ -274,7 +293,6 @@ __global__ void __launch_bounds__(THREADS) umma_gemm_kernel(GemmArgs p)
         if (kb < nkb) load(kb);
         cp_async_commit();
     }
-    bool ok = true;
     for (int kb = 0; kb < nkb; ++kb) {
         const int s = kb % STAGES;
         cp_async_wait<STAGES - 2>();  // this thread's copies of block kb have landed
@@ -284,12 +302,8 @@ __global__ void __launch_bounds__(THREADS) umma_gemm_kernel(GemmArgs p)
             fence_after_sync();
             const uint32_t a0 = smem_u32(sA[s]), b0 = smem_u32(sB[s]);
 #pragma unroll
-            for (int kk = 0; kk < BK / 16; ++kk) {
-                // a 16-wide K step is two core matrices along K: 2 x 128 bytes
-                const uint64_t ad = make_desc(a0 + kk * 256, 128, (BK / 8) * 128);
-                const uint64_t bd = make_desc(b0 + kk * 256, 128, (BK / 8) * 128);
-                mma_bf16(tmem, ad, bd, IDESC, (kb > 0 || kk > 0) ? 1u : 0u);
-            }
+            for (int kk = 0; kk < BK / 16; ++kk)
+                mma_bf16(tmem, step_desc<BM, TA>(a0, kk), step_desc<BN, TB>(b0, kk), IDESC, (kb > 0 || kk > 0) ? 1u : 0u);
             mma_commit(smem_u32(&bars[s]));
         }
         // refill the stage block kb - 1 used, once its MMAs are done

@@ -276,6 +276,11 @@ int hwt_surrogate_params(hwt_surrogate *s, float *params, int64_t count, int set
  * x [n][7] and standardised targets y [n] (no update): the hooks the gradient
  * check against the CPU oracle uses. */
 int hwt_surrogate_forward(hwt_surrogate *s, const float *x, int n, float *out);
+/* Fault injection for tests of the failure path: while on, every GEMM first waits
+ * on an mbarrier phase that nothing completes; the bounded wait runs out (about a
+ * second), the GEMM skips its work and the call returns HWT_ETIMEOUT with the
+ * context still usable.  No GPU fault is involved. */
+int hwt_surrogate_inject_stall(hwt_surrogate *s, int on);
 int hwt_surrogate_loss_grads(hwt_surrogate *s, const float *x, const float *y, int n, double *loss,
                              float *grads);
 

@@ -96,3 +96,21 @@ def test_train_route_judge_and_checkpoint(pkg, pricer, orc, tmp_path):
     assert np.array_equal(s.forward(x), s2.forward(x))
     s.close()
     s2.close()
+
+
+def test_bounded_wait_reports_timeout_and_context_survives(pkg, sur):
+    """Failure path of the tensor-core GEMM without a GPU fault: with the stall
+    injected, every GEMM's mbarrier wait runs out (a phase nothing completes), the
+    call returns HWT_ETIMEOUT, and the next call on the same surrogate works."""
+    params = _oracle_params(2)
+    sur.set_params(params)
+    x = np.random.default_rng(1).standard_normal((300, 7))
+    ok = sur.forward(x)
+    sur.inject_stall(True)
+    try:
+        with pytest.raises(pkg.HwtError) as e:
+            sur.forward(x)
+        assert e.value.code == pkg.HWT_ETIMEOUT
+    finally:
+        sur.inject_stall(False)
+    assert np.array_equal(sur.forward(x), ok)
