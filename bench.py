@@ -213,13 +213,13 @@ def run_ours(args, rank, world, local):
     flop_per_batch = FLOP_PER_NODE * nodes
 
     pricer = pkg.Pricer(local)
-    mode = {"mixed": pkg.BATCHED_MIXED, "fp64": pkg.BATCHED_FP64, "fp32": pkg.BATCHED_FP32,
+    mode = {"mixed": pkg.BATCHED_MIXED, "fp64": pkg.BATCHED_FP64, "fp32": pkg.BATCHED_FP32, "df64": pkg.BATCHED_DF64,
             "plain": pkg.PLAIN_FP64}[args.mode]
     # the library's autotuner (hwt_autotune) picks group size, warp-task width
     # threshold and K set for this batch, untimed, for every batched mode used below
     tuned = {}
     if not args.no_tune:
-        for m in (pkg.BATCHED_MIXED, pkg.BATCHED_FP32, pkg.BATCHED_FP64):
+        for m in (pkg.BATCHED_MIXED, pkg.BATCHED_FP32, pkg.BATCHED_FP64, pkg.BATCHED_DF64):
             if m == mode or not args.skip_survey:
                 c = pricer.autotune(opts, y, m, repeats=2)
                 tuned[pkg.MODE_NAMES[m]] = {"block_size": c.block_size, "big_threshold": c.big_threshold,
@@ -271,7 +271,8 @@ def run_ours(args, rank, world, local):
 
     # per-mode survey (prices + errors + device time), untimed by the contract
     modes = {}
-    for m in (() if args.skip_survey else (pkg.BATCHED_MIXED, pkg.BATCHED_FP32, pkg.BATCHED_FP64, pkg.PLAIN_FP64)):
+    for m in (() if args.skip_survey else (pkg.BATCHED_MIXED, pkg.BATCHED_FP32, pkg.BATCHED_FP64, pkg.BATCHED_DF64,
+                                           pkg.PLAIN_FP64)):
         name = pkg.MODE_NAMES[m]
         k = args.steps if m != pkg.PLAIN_FP64 else max(1, min(args.steps, 3))
         t, _, st = device_steps(m, k, 1)
@@ -347,7 +348,7 @@ def run_ours(args, rank, world, local):
             dsh = pkg.shape(dopts)
             entry = {"options": dopts.N,
                      "active_nodes_per_pass": int(np.sum(pkg.active_nodes(dsh["height"], dsh["jmax"])))}
-            for m in (pkg.BATCHED_FP64, pkg.BATCHED_FP32, pkg.BATCHED_MIXED):
+            for m in (pkg.BATCHED_FP64, pkg.BATCHED_DF64, pkg.BATCHED_FP32, pkg.BATCHED_MIXED):
                 best = 1e300
                 for _ in range(3):
                     pricer.price(dopts, y15, m)
@@ -400,7 +401,7 @@ def run_ours(args, rank, world, local):
     achieved = flop_per_batch / (pricing_ms * 1e-3) / 1e12
     prof = load_json(os.path.join(ROOT, "profiles", f"pricing_{args.workload}_{args.mode}.json")) or {}
     traffic = prof.get("dram_bytes_per_launch")
-    bound = {"mixed": "fp32", "fp32": "fp32", "fp64": "fp64", "plain": "fp64"}[args.mode]
+    bound = {"mixed": "fp32", "fp32": "fp32", "fp64": "fp64", "df64": "fp32", "plain": "fp64"}[args.mode]
     peak = fp32_peak if bound == "fp32" else peaks[0]
 
     if rank == 0:
@@ -415,7 +416,7 @@ def run_ours(args, rank, world, local):
             "higher_is_better": True,
             "scaling": "weak",
             "vs_baseline": None,
-            "dtype": {"mixed": "f32+f64", "fp32": "f32", "fp64": "f64", "plain": "f64"}[args.mode],
+            "dtype": {"mixed": "f32+f64", "fp32": "f32", "fp64": "f64", "df64": "f32x2+f64", "plain": "f64"}[args.mode],
             "data": "synthetic (seeded numpy; no public data set exists for this workload)",
             "config": {"workload": args.workload, "options": n, "mode": pkg.MODE_NAMES[mode],
                        "active_nodes_per_pass": nodes, "parallelism": "replicas" if world > 1 else "single",
@@ -460,7 +461,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="uneven_30k", choices=sorted(WORKLOAD_NAMES))
-    ap.add_argument("--mode", default="mixed", choices=["mixed", "fp64", "fp32", "plain"])
+    ap.add_argument("--mode", default="mixed", choices=["mixed", "fp64", "fp32", "df64", "plain"])
     ap.add_argument("--ref-sample", type=int, default=6000)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="library defaults instead of the autotuned configuration")

@@ -32,9 +32,9 @@ LIB_PATH = os.path.join(HERE, "_build", "libhwtree.so")
 HWT_OK, HWT_EINVAL, HWT_ECUDA, HWT_ENOMEM, HWT_EUNSUPPORTED, HWT_ENODEV, HWT_ETIMEOUT = 0, -1, -2, -3, -4, -5, -6
 
 # Pricing modes (hwtree.h)
-PLAIN_FP64, BATCHED_FP64, BATCHED_FP32, BATCHED_MIXED = 0, 1, 2, 3
+PLAIN_FP64, BATCHED_FP64, BATCHED_FP32, BATCHED_MIXED, BATCHED_DF64 = 0, 1, 2, 3, 4
 MODE_NAMES = {PLAIN_FP64: "plain_fp64", BATCHED_FP64: "batched_fp64", BATCHED_FP32: "batched_fp32",
-              BATCHED_MIXED: "batched_mixed"}
+              BATCHED_MIXED: "batched_mixed", BATCHED_DF64: "batched_df64"}
 
 
 class OptionType(enum.IntEnum):

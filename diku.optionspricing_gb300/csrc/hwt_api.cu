@@ -55,7 +55,7 @@ struct hwt_ctx {
     cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};  // call start, sizing start, pricing start, pricing end, call end
     std::string err;
     std::string tune_path;
-    hwt_config tuned[4];
+    hwt_config tuned[kNumModes];
 
     // device buffers, capacity `cap` options
     int64_t cap = 0;
@@ -220,9 +220,12 @@ bool valid_sort(int s)
            s == HWT_SORT_HEIGHT_DESC || s == HWT_SORT_HEIGHT_ASC || s == HWT_SORT_INPUT;
 }
 
+// Modes whose rows take 64 bits a node (double, double-float): at most 8 nodes a thread.
+bool wide_rows(int mode) { return mode == HWT_BATCHED_FP64 || mode == HWT_BATCHED_DF64; }
+
 hwt_config resolve(const hwt_ctx *c, const hwt_config *cfg, int mode)
 {
-    hwt_config r = c->tuned[(mode >= 0 && mode < 4) ? mode : 0];
+    hwt_config r = c->tuned[(mode >= 0 && mode < kNumModes) ? mode : 0];
     r.mode = mode;
     if (cfg) {
         if (cfg->block_size > 0) r.block_size = cfg->block_size;
@@ -321,7 +324,7 @@ int run_batch(hwt_ctx *c, const DevOptions &dopt, double *dev_out, const hwt_con
     p.out = dev_out;
     p.group_threads = cfg.block_size;
     p.warp_k_mask = resolve_k_mask(cfg.mode, cfg.warp_k_mask, &p.max_warp_k);
-    p.max_group_k = cfg.mode == HWT_BATCHED_FP64 ? kMaxBlockK : kMaxGroupKFloat;
+    p.max_group_k = wide_rows(cfg.mode) ? kMaxBlockK : kMaxGroupKFloat;
     p.sort = cfg.sort;
     p.big_threshold = std::min(cfg.big_threshold, 32 * p.max_warp_k);
     p.max_width = kMaxTreeWidth;
@@ -462,12 +465,12 @@ hwt_ctx *hwt_create(int device, const char *tune_cache)
     ok = ok && cudaHostAlloc((void **)&c->h_yrate, 8 * kMaxYield, cudaHostAllocDefault) == cudaSuccess;
     ok = ok && cudaHostAlloc((void **)&c->h_yrate_f, 4 * kMaxYield, cudaHostAllocDefault) == cudaSuccess;
     ok = ok && cudaHostAlloc((void **)&c->h_yday, 4 * kMaxYield, cudaHostAllocDefault) == cudaSuccess;
-    for (int m = 0; m < 4; ++m) {
+    for (int m = 0; m < kNumModes; ++m) {
         hwt_config &t = c->tuned[m];
         memset(&t, 0, sizeof(t));
         t.mode = m;
-        t.block_size = m == HWT_BATCHED_FP64 ? kDefaultBlockFP64 : kDefaultBlockFloat;
-        t.big_threshold = m == HWT_BATCHED_FP64 ? kDefaultBig : kMaxWarpWidth;  // float rows fit 512 per warp
+        t.block_size = wide_rows(m) ? kDefaultBlockFP64 : kDefaultBlockFloat;
+        t.big_threshold = wide_rows(m) ? kDefaultBig : kMaxWarpWidth;  // float rows fit 512 per warp
         t.warp_k_mask = resolve_k_mask(m, 0, nullptr);
         t.use_graph = 1;
     }
@@ -482,7 +485,7 @@ hwt_ctx *hwt_create(int device, const char *tune_cache)
             if (!std::getline(ls, name, '|')) continue;
             if (!(ls >> mode >> block >> big)) continue;
             if (!(ls >> kmask)) kmask = 0;  // lines without a K mask keep the mode's default
-            if (name == c->gpu_name && mode >= 0 && mode < 4 && (block == 64 || block == 128 || block == 256 || block == 512) &&
+            if (name == c->gpu_name && mode >= 0 && mode < kNumModes && (block == 64 || block == 128 || block == 256 || block == 512) &&
                 big >= 1 && big <= kMaxWarpWidth) {
                 c->tuned[mode].block_size = block;
                 c->tuned[mode].big_threshold = big;
@@ -524,7 +527,7 @@ int hwt_price_ex(hwt_ctx *c, const hwt_options *o, const hwt_yield *y, const hwt
     int r = check_options(c, o);
     if (r) return r;
     const int mode = cfg_in ? cfg_in->mode : HWT_BATCHED_FP64;
-    if (mode < 0 || mode > 3) return fail(c, HWT_EINVAL, "unknown mode");
+    if (mode < 0 || mode >= kNumModes) return fail(c, HWT_EINVAL, "unknown mode");
     if (o->n > 0 && !out) return fail(c, HWT_EINVAL, "output pointer is NULL");
     HWT_CUDA(c, cudaSetDevice(c->device), "cudaSetDevice");
     if ((r = upload_yield(c, y))) return r;
@@ -600,7 +603,7 @@ int hwt_price_device(hwt_ctx *c, const hwt_options *o, const hwt_yield *y, const
     int r = check_options(c, o);
     if (r) return r;
     const int mode = cfg_in ? cfg_in->mode : HWT_BATCHED_FP64;
-    if (mode < 0 || mode > 3) return fail(c, HWT_EINVAL, "unknown mode");
+    if (mode < 0 || mode >= kNumModes) return fail(c, HWT_EINVAL, "unknown mode");
     if (o->n > 0 && !dev_out) return fail(c, HWT_EINVAL, "output pointer is NULL");
     HWT_CUDA(c, cudaSetDevice(c->device), "cudaSetDevice");
     if ((r = upload_yield(c, y))) return r;
@@ -646,7 +649,7 @@ int64_t hwt_active_nodes(int32_t height, int32_t jmax) { return active_nodes(hei
 
 int hwt_get_config(const hwt_ctx *c, int mode, hwt_config *cfg)
 {
-    if (!c || !cfg || mode < 0 || mode > 3) return HWT_EINVAL;
+    if (!c || !cfg || mode < 0 || mode >= kNumModes) return HWT_EINVAL;
     *cfg = c->tuned[mode];
     return HWT_OK;
 }
@@ -654,7 +657,7 @@ int hwt_get_config(const hwt_ctx *c, int mode, hwt_config *cfg)
 int hwt_autotune(hwt_ctx *c, const hwt_options *o, const hwt_yield *y, int mode, int repeats, hwt_config *best)
 {
     if (!c) return HWT_EINVAL;
-    if (mode < 1 || mode > 3) return fail(c, HWT_EINVAL, "autotune applies to the batched modes");
+    if (mode < 1 || mode >= kNumModes) return fail(c, HWT_EINVAL, "autotune applies to the batched modes");
     if (repeats < 1) repeats = 3;
     int r = check_options(c, o);
     if (r) return r;
@@ -664,7 +667,7 @@ int hwt_autotune(hwt_ctx *c, const hwt_options *o, const hwt_yield *y, int mode,
     const int bigs[] = {128, 256, 384, 512};
     // the mode's default K set and a denser one (better fit, larger code footprint)
     const int kmasks[] = {resolve_k_mask(mode, 0, nullptr),
-                          resolve_k_mask(mode, mode == HWT_BATCHED_FP64 ? kKMaskFP64Alt : kKMaskFloatAlt, nullptr)};
+                          resolve_k_mask(mode, wide_rows(mode) ? kKMaskFP64Alt : kKMaskFloatAlt, nullptr)};
     const int n_kmasks = 2;
     double best_ms = 1e300;
     hwt_config best_cfg = c->tuned[mode];

@@ -34,6 +34,7 @@
 #include <float.h>
 #include <stdio.h>
 
+#include "hwt_df64.cuh"
 #include "hwt_internal.h"
 #include "hwt_model.cuh"
 
@@ -57,6 +58,34 @@ struct ModeMix {
     typedef double Scal;
     static constexpr bool kFlux = true;
 };
+struct ModeDF64 {
+    typedef df64 Row;     // gather form like double rows, arithmetic on the FP32 pipes
+    typedef double Scal;
+    static constexpr bool kFlux = false;
+};
+
+// Width-w warp shuffles for every row type (df64 moves as two floats).
+template <typename T>
+__device__ __forceinline__ T shfl_up(T v, unsigned d, int w) { return __shfl_up_sync(0xffffffffu, v, d, w); }
+template <typename T>
+__device__ __forceinline__ T shfl_down(T v, unsigned d, int w) { return __shfl_down_sync(0xffffffffu, v, d, w); }
+__device__ __forceinline__ df64 shfl_up(df64 v, unsigned d, int w)
+{
+    return df64_make(__shfl_up_sync(0xffffffffu, v.hi, d, w), __shfl_up_sync(0xffffffffu, v.lo, d, w));
+}
+__device__ __forceinline__ df64 shfl_down(df64 v, unsigned d, int w)
+{
+    return df64_make(__shfl_down_sync(0xffffffffu, v.hi, d, w), __shfl_down_sync(0xffffffffu, v.lo, d, w));
+}
+
+// a x + b y + c z in the gather form: two FMAs after a product for double rows
+// (this order is the one the FP64 results are pinned with), the compensated
+// three-term product for df64 rows.
+__device__ __forceinline__ double gather3(double a, double x, double b, double y, double c, double z)
+{
+    return fma(c, z, fma(b, y, a * x));
+}
+__device__ __forceinline__ df64 gather3(df64 a, df64 x, df64 b, df64 y, df64 c, df64 z) { return dot3(a, x, b, y, c, z); }
 
 __device__ __forceinline__ int cls_K(int cls)
 {
@@ -576,9 +605,7 @@ struct Slice {
             for (int s = 0; s < K; ++s) {
                 const R cur = r[s];
                 const R nxt = (s < K - 1) ? r[s + 1] : h.r1;
-                R v = c0[s] * prev;
-                v = fma(c1[s], cur, v);
-                v = fma(c2[s], nxt, v);
+                R v = gather3(c0[s], prev, c1[s], cur, c2[s], nxt);
                 if (s == S2) v = fma(jin, src2, v);
                 r[s] = v;
                 prev = cur;
@@ -615,9 +642,7 @@ struct Slice {
             for (int s = 0; s < K; ++s) {
                 const R cur = r[s];
                 const R nxt = (s < K - 1) ? r[s + 1] : h.r1;
-                R v = c0[s] * nxt;
-                v = fma(c1[s], cur, v);
-                v = fma(c2[s], prev, v);
+                R v = gather3(c0[s], nxt, c1[s], cur, c2[s], prev);
                 if (s == 0) v = fma(j0, o2, v);
                 r[s] = v;
                 prev = cur;
@@ -681,15 +706,15 @@ __device__ __forceinline__ Halo<R> exchange_warp(const R (&r)[K], int L, bool tw
 {
     Halo<R> h;
     if constexpr (K >= 2) {
-        h.l1 = __shfl_up_sync(FULL, r[K - 1], 1, L);
-        h.r1 = __shfl_down_sync(FULL, r[0], 1, L);
-        h.l2 = two ? __shfl_up_sync(FULL, r[K - 2], 1, L) : (R)0;
-        h.r2 = two ? __shfl_down_sync(FULL, r[1], 1, L) : (R)0;
+        h.l1 = shfl_up(r[K - 1], 1, L);
+        h.r1 = shfl_down(r[0], 1, L);
+        h.l2 = two ? shfl_up(r[K - 2], 1, L) : (R)0;
+        h.r2 = two ? shfl_down(r[1], 1, L) : (R)0;
     } else {
-        h.l1 = __shfl_up_sync(FULL, r[0], 1, L);
-        h.r1 = __shfl_down_sync(FULL, r[0], 1, L);
-        h.l2 = two ? __shfl_up_sync(FULL, r[0], 2, L) : (R)0;
-        h.r2 = two ? __shfl_down_sync(FULL, r[0], 2, L) : (R)0;
+        h.l1 = shfl_up(r[0], 1, L);
+        h.r1 = shfl_down(r[0], 1, L);
+        h.l2 = two ? shfl_up(r[0], 2, L) : (R)0;
+        h.r2 = two ? shfl_down(r[0], 2, L) : (R)0;
     }
     return h;
 }
@@ -1030,9 +1055,10 @@ __global__ void __launch_bounds__(kPricingThreads, 1) price_kernel(EngineParams 
 
 int resolve_k_mask(int mode, int requested, int *max_k)
 {
-    const int allowed = mode == MODE_BATCHED_FP64 ? kKMaskFP64 : kKMaskAll;
+    const bool dbl = mode == MODE_BATCHED_FP64 || mode == MODE_BATCHED_DF64;  // 64-bit rows: K <= 8
+    const int allowed = dbl ? kKMaskFP64 : kKMaskAll;
     int m = requested & allowed;
-    if (m == 0) m = mode == MODE_BATCHED_FP64 ? kKMaskFP64 : kKMaskFloat;
+    if (m == 0) m = dbl ? kKMaskFP64 : kKMaskFloat;
     int mk = 1;
     for (int q = 0; q < kNumK; ++q)
         if ((m >> q) & 1) mk = kWarpK[q];
@@ -1078,6 +1104,7 @@ cudaError_t launch_pricing(const EngineParams &p, int mode, int grid, cudaStream
         case MODE_BATCHED_FP64: price_kernel<ModeF64><<<grid, kPricingThreads, 0, stream>>>(p); break;
         case MODE_BATCHED_FP32: price_kernel<ModeF32><<<grid, kPricingThreads, 0, stream>>>(p); break;
         case MODE_BATCHED_MIXED: price_kernel<ModeMix><<<grid, kPricingThreads, 0, stream>>>(p); break;
+        case MODE_BATCHED_DF64: price_kernel<ModeDF64><<<grid, kPricingThreads, 0, stream>>>(p); break;
         default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
@@ -1092,6 +1119,7 @@ int pricing_blocks_per_sm(int mode)
         case MODE_BATCHED_FP64: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, price_kernel<ModeF64>, block_threads, 0); break;
         case MODE_BATCHED_FP32: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, price_kernel<ModeF32>, block_threads, 0); break;
         case MODE_BATCHED_MIXED: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, price_kernel<ModeMix>, block_threads, 0); break;
+        case MODE_BATCHED_DF64: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, price_kernel<ModeDF64>, block_threads, 0); break;
         default: break;
     }
     return e == cudaSuccess ? nb : 0;

@@ -13,7 +13,9 @@ enum Mode : int {
     MODE_BATCHED_FP64 = 1,  // binned persistent engine, double rows
     MODE_BATCHED_FP32 = 2,  // float rows, float sums and scales
     MODE_BATCHED_MIXED = 3, // float rows, double sums, scales, payoff and final discount
+    MODE_BATCHED_DF64 = 4,  // double-float rows on the FP32 pipes, double sums and scales
 };
+constexpr int kNumModes = 5;
 
 // Device copy of the option records (SoA, common/Options.hpp:48-58 with real=double).
 struct DevOptions {

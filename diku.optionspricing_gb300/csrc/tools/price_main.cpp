@@ -3,7 +3,7 @@
 //   -o|--options FILE   option records (.in)
 //   -y|--yield FILE     yield curve (.in)
 //   -v|--version M ...  pricing mode(s): 0 plain FP64, 1 batched FP64 (default),
-//                       2 batched FP32, 3 batched mixed
+//                       2 batched FP32, 3 batched mixed, 4 batched double-float
 //   -b|--block B ...    threads per block-tree block (the reference's -b)
 //   -s|--sort S ...     schedule order W w H h - i (results do not depend on it)
 //   -r|--runs R         time R runs and print "mode,block,sort,kernel_us,total_us,bytes"

@@ -47,6 +47,8 @@ extern "C" {
 #define HWT_BATCHED_FP64 1   /* binned persistent engine, double */
 #define HWT_BATCHED_FP32 2   /* binned persistent engine, float throughout */
 #define HWT_BATCHED_MIXED 3  /* float rows, double alpha-fit sums, scales, payoff, discount */
+#define HWT_BATCHED_DF64 4   /* double-float rows (hi + lo floats, ~48 bits) on the FP32 pipes,
+                                double sums, scales, payoff, discount; within 1e-10 relative of FP64 */
 
 /* Sort orders of the reference's -s flag (common/Options.hpp:15-22).  They set the
  * order in which the engine schedules trees inside each of its tiers (whole-block

@@ -30,6 +30,7 @@ def test_full_uneven_batch_fp64_and_mixed(pkg, pricer, uneven):
     """The whole 30,000-option uneven batch against the oracle."""
     opts, y, ref = uneven
     assert_fp64(pricer.price(opts, y, pkg.BATCHED_FP64), ref, "uneven_30k fp64")
+    assert_fp64(pricer.price(opts, y, pkg.BATCHED_DF64), ref, "uneven_30k df64")
     assert_lowp(pricer.price(opts, y, pkg.BATCHED_MIXED), ref, "uneven_30k mixed")
     assert_lowp(pricer.price(opts, y, pkg.BATCHED_FP32), ref, "uneven_30k fp32")
 
@@ -40,6 +41,7 @@ def test_full_skewed_batch_fp64(pkg, pricer, orc):
     y = _curve(pkg)
     ref = orc.price(opts, y, "f64")
     assert_fp64(pricer.price(opts, y, pkg.BATCHED_FP64), ref, "skewed_100k fp64")
+    assert_fp64(pricer.price(opts, y, pkg.BATCHED_DF64), ref, "skewed_100k df64")
     assert_lowp(pricer.price(opts, y, pkg.BATCHED_MIXED), ref, "skewed_100k mixed")
 
 
@@ -224,5 +226,7 @@ def test_warp_k_sets(pkg, pricer, uneven):
     opts, y, ref = uneven
     for mask in (0xFF, 0xAF, 0x01, 0x10 | 0x40):
         assert_fp64(pricer.price(opts, y, pkg.BATCHED_FP64, warp_k_mask=mask), ref, f"fp64 mask {mask:#x}")
+    for mask in (0xFF, 0x01):
+        assert_fp64(pricer.price(opts, y, pkg.BATCHED_DF64, warp_k_mask=mask), ref, f"df64 mask {mask:#x}")
     for mask in (0x3AF, 0x3FF, 0x01, 0x200):
         assert_lowp(pricer.price(opts, y, pkg.BATCHED_MIXED, warp_k_mask=mask), ref, f"mixed mask {mask:#x}")

@@ -11,7 +11,7 @@ ALL_SETS = REF_SETS + SYN_SETS
 
 
 @pytest.mark.parametrize("name", ALL_SETS)
-@pytest.mark.parametrize("mode", ["BATCHED_FP64", "PLAIN_FP64"])
+@pytest.mark.parametrize("mode", ["BATCHED_FP64", "BATCHED_DF64", "PLAIN_FP64"])
 def test_fp64_matches_reference_goldens(pkg, pricer, name, mode):
     opts, y, g64, _ = load_set(pkg, name)
     got = pricer.price(opts, y, getattr(pkg, mode))
@@ -19,11 +19,13 @@ def test_fp64_matches_reference_goldens(pkg, pricer, name, mode):
 
 
 @pytest.mark.parametrize("name", ALL_SETS)
-def test_fp64_matches_oracle(pkg, orc, pricer, name):
+@pytest.mark.parametrize("mode", ["BATCHED_FP64", "BATCHED_DF64"])
+def test_fp64_matches_oracle(pkg, orc, pricer, name, mode):
+    """Double rows, and double-float rows on the FP32 pipes, within 1e-10 relative."""
     opts, y, _, _ = load_set(pkg, name)
     ref = orc.price(opts, y, "f64")
-    got = pricer.price(opts, y, pkg.BATCHED_FP64)
-    assert_fp64(got, ref, name)
+    got = pricer.price(opts, y, getattr(pkg, mode))
+    assert_fp64(got, ref, f"{name} {mode}")
 
 
 @pytest.mark.parametrize("name", ALL_SETS)
