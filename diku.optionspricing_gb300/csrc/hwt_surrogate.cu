@@ -123,10 +123,51 @@ struct AdamArgs {
     float lr, b1, b2, eps, c1, c2;
 };
 
-__global__ void adam_kernel(AdamArgs a)
+// Per-step training state kept on the device, so that one captured CUDA graph
+// serves every step: the Adam step count t, the step index in the learning-rate
+// schedule, the batch index within the epoch, and the step's lr and bias corrections.
+struct StepState {
+    long long t;     // Adam steps taken
+    long long step;  // schedule position within this training call
+    int k;           // next batch of the epoch
+    int cur;         // batch this step trains on
+    float lr, c1, c2;
+};
+
+__global__ void step_begin_kernel(StepState *st, double lr0, double lr_min, long long total)
+{
+    const long long t = st->t + 1;
+    st->t = t;
+    const double step = (double)st->step;
+    st->step = st->step + 1;
+    st->lr = (float)(lr_min + 0.5 * (lr0 - lr_min) * (1.0 + cos(3.14159265358979323846 * step / (double)total)));
+    st->c1 = 1.f - powf(0.9f, (float)t);
+    st->c2 = 1.f - powf(0.999f, (float)t);
+    st->cur = st->k;
+    st->k = st->k + 1;
+}
+
+// Batch `cur` of the shuffled samples into the fixed input and target buffers.
+__global__ void batch_copy_kernel(const __nv_bfloat16 *Xs, const float *ys, const StepState *st, int batch,
+                                  __nv_bfloat16 *X, float *y)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= batch) return;
+    const size_t row = (size_t)st->cur * batch + i;
+    *reinterpret_cast<uint4 *>(X + (size_t)i * kInPad) = *reinterpret_cast<const uint4 *>(Xs + row * kInPad);
+    y[i] = ys[row];
+}
+
+// Adam with lr and bias corrections from the args, or from the step state if given.
+__global__ void adam_kernel(AdamArgs a, const StepState *st)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
+    if (st) {
+        a.lr = st->lr;
+        a.c1 = st->c1;
+        a.c2 = st->c2;
+    }
     const float g = a.g[i];
     const float m = a.b1 * a.m[i] + (1.f - a.b1) * g;
     const float v = a.b2 * a.v[i] + (1.f - a.b2) * g * g;
@@ -276,11 +317,26 @@ template <bool TA, bool TB, int BN>
 cudaError_t gemm_bn(const GemmArgs &a, int splits, cudaStream_t st)
 {
     auto kern = umma_gemm_kernel<TA, TB, BN>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes(BN));
-    if (e != cudaSuccess) return e;
     dim3 grid((a.N + BN - 1) / BN, (a.M + BM - 1) / BM, splits);
     kern<<<grid, THREADS, smem_bytes(BN), st>>>(a);
     return cudaGetLastError();
+}
+
+// Dynamic shared memory above 48 KB for every GEMM instantiation, once at set-up
+// (outside any stream capture).
+cudaError_t gemm_attributes()
+{
+    cudaError_t e = cudaSuccess;
+    auto set = [&](auto kern, int bn) {
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes(bn));
+    };
+    set(umma_gemm_kernel<false, false, 16>, 16);
+    set(umma_gemm_kernel<false, false, 64>, 64);
+    set(umma_gemm_kernel<false, false, 128>, 128);
+    set(umma_gemm_kernel<true, true, 16>, 16);
+    set(umma_gemm_kernel<true, true, 64>, 64);
+    set(umma_gemm_kernel<true, true, 128>, 128);
+    return e;
 }
 
 // Tile width: the output width rounded up to 16 (one tile for the 1-wide output
@@ -382,15 +438,22 @@ int refresh(hwt_surrogate *s)
     return HWT_OK;
 }
 
-int adam(hwt_surrogate *s, float lr)
+// One training step on the batch the step state names, everything from device
+// state: the body of the captured training graph.
+int train_step(hwt_surrogate *s, const __nv_bfloat16 *Xs, const float *ys, StepState *st, int batch, double lr0,
+               double lr_min, long long total)
 {
-    ++s->adam_t;
+    step_begin_kernel<<<1, 1, 0, s->stream>>>(st, lr0, lr_min, total);
+    SCUDA(s, cudaGetLastError(), "step kernel");
+    batch_copy_kernel<<<(batch + 255) / 256, 256, 0, s->stream>>>(Xs, ys, st, batch, s->d_h[0], s->d_y);
+    SCUDA(s, cudaGetLastError(), "batch kernel");
+    int r = forward(s, batch);
+    if (!r) r = backward(s, batch, false);
+    if (r) return r;
     AdamArgs a;
     a.w = s->d_w; a.m = s->d_m; a.v = s->d_v; a.g = s->d_g; a.n = (int)s->n_params;
-    a.lr = lr; a.b1 = 0.9f; a.b2 = 0.999f; a.eps = 1e-8f;
-    a.c1 = 1.f - powf(0.9f, (float)s->adam_t);
-    a.c2 = 1.f - powf(0.999f, (float)s->adam_t);
-    adam_kernel<<<((int)s->n_params + 255) / 256, 256, 0, s->stream>>>(a);
+    a.lr = 0.f; a.b1 = 0.9f; a.b2 = 0.999f; a.eps = 1e-8f; a.c1 = 1.f; a.c2 = 1.f;
+    adam_kernel<<<((int)s->n_params + 255) / 256, 256, 0, s->stream>>>(a, st);
     SCUDA(s, cudaGetLastError(), "adam kernel");
     return refresh(s);
 }
@@ -455,6 +518,7 @@ hwt_surrogate *hwt_surrogate_create(hwt_ctx *ctx, const hwt_box *box, uint64_t s
         }
         ok = cudaMemcpy(s->d_w, w.data(), 4 * off, cudaMemcpyHostToDevice) == cudaSuccess &&
              cudaMemset(s->d_m, 0, 4 * off) == cudaSuccess && cudaMemset(s->d_v, 0, 4 * off) == cudaSuccess;
+        ok = ok && gemm_attributes() == cudaSuccess;
         ok = ok && refresh(s) == HWT_OK && cudaStreamSynchronize(s->stream) == cudaSuccess;
     }
     if (!ok) {
@@ -740,6 +804,35 @@ int hwt_surrogate_train(hwt_surrogate *s, const hwt_options *samples, const hwt_
     const double lr0 = cfg->lr > 0 ? cfg->lr : 1e-3, lr_min = cfg->lr_min;
     long step = 0;
     double last_epoch_loss = 0;
+    // one training step captured as a CUDA graph (about 30 kernels), replayed per step
+    StepState *dstate = nullptr;
+    SCUDA(s, cudaMalloc(&dstate, sizeof(StepState)), "step state");
+    guard.ptrs.push_back(dstate);
+    {
+        StepState h;
+        memset(&h, 0, sizeof(h));
+        h.t = s->adam_t;
+        SCUDA(s, cudaMemcpy(dstate, &h, sizeof(h), cudaMemcpyHostToDevice), "step state H2D");
+    }
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    struct GraphGuard {
+        cudaGraph_t *g;
+        cudaGraphExec_t *x;
+        ~GraphGuard()
+        {
+            if (*x) cudaGraphExecDestroy(*x);
+            if (*g) cudaGraphDestroy(*g);
+        }
+    } gguard{&graph, &gexec};
+    SCUDA(s, cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+    r = train_step(s, Xs, ys, dstate, batch, lr0, lr_min, (long long)total);
+    {
+        const cudaError_t ce2 = cudaStreamEndCapture(s->stream, &graph);
+        if (r) return r;
+        SCUDA(s, ce2, "end capture");
+    }
+    SCUDA(s, cudaGraphInstantiate(&gexec, graph, 0), "instantiate training graph");
     cudaEventRecord(e0, s->stream);
     for (int ep = 0; ep < epochs; ++ep) {
         for (int64_t i = nin - 1; i > 0; --i) std::swap(idx[i], idx[rnd() % (unsigned long long)(i + 1)]);
@@ -747,17 +840,9 @@ int hwt_surrogate_train(hwt_surrogate *s, const hwt_options *samples, const hwt_
         gather_rows_kernel<<<(int)((nin + 255) / 256), 256, 0, s->stream>>>(X, yv, perm, (int)nin, Xs, ys);
         SCUDA(s, cudaStreamSynchronize(s->stream), "shuffle");  // perm host buffer is rewritten next epoch
         SCUDA(s, cudaMemsetAsync(s->d_loss, 0, sizeof(double), s->stream), "zero loss");
-        for (int k = 0; k < steps_per_epoch; ++k, ++step) {
-            SCUDA(s, cudaMemcpyAsync(s->d_y, ys + (size_t)k * batch, 4ull * batch, cudaMemcpyDeviceToDevice, s->stream), "batch y");
-            if ((r = forward_from(s, Xs + (size_t)k * batch * kInPad, batch))) return r;
-            __nv_bfloat16 *keep = s->d_h[0];
-            s->d_h[0] = Xs + (size_t)k * batch * kInPad;
-            r = backward(s, batch, false);
-            s->d_h[0] = keep;
-            if (r) return r;
-            const double lr = lr_min + 0.5 * (lr0 - lr_min) * (1.0 + cos(M_PI * (double)step / (double)total));
-            if ((r = adam(s, (float)lr))) return r;
-        }
+        SCUDA(s, cudaMemsetAsync(&dstate->k, 0, sizeof(int), s->stream), "epoch start");
+        for (int k = 0; k < steps_per_epoch; ++k, ++step)
+            SCUDA(s, cudaGraphLaunch(gexec, s->stream), "training step");
         double l = 0;
         SCUDA(s, cudaMemcpyAsync(&l, s->d_loss, sizeof(double), cudaMemcpyDeviceToHost, s->stream), "loss D2H");
         SCUDA(s, cudaStreamSynchronize(s->stream), "epoch");
@@ -765,6 +850,11 @@ int hwt_surrogate_train(hwt_surrogate *s, const hwt_options *samples, const hwt_
     }
     cudaEventRecord(e1, s->stream);
     cudaEventSynchronize(e1);
+    {
+        StepState h;
+        SCUDA(s, cudaMemcpy(&h, dstate, sizeof(h), cudaMemcpyDeviceToHost), "step state D2H");
+        s->adam_t = (long)h.t;
+    }
     float ms = 0;
     cudaEventElapsedTime(&ms, e0, e1);
     cudaEventDestroy(e0);
