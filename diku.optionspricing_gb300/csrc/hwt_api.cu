@@ -469,7 +469,7 @@ hwt_ctx *hwt_create(int device, const char *tune_cache)
         hwt_config &t = c->tuned[m];
         memset(&t, 0, sizeof(t));
         t.mode = m;
-        t.block_size = wide_rows(m) ? kDefaultBlockFP64 : kDefaultBlockFloat;
+        t.block_size = m == HWT_BATCHED_FP64 ? kDefaultBlockFP64 : kDefaultBlockFloat;
         t.big_threshold = wide_rows(m) ? kDefaultBig : kMaxWarpWidth;  // float rows fit 512 per warp
         t.warp_k_mask = resolve_k_mask(m, 0, nullptr);
         t.use_graph = 1;
@@ -667,7 +667,8 @@ int hwt_autotune(hwt_ctx *c, const hwt_options *o, const hwt_yield *y, int mode,
     const int bigs[] = {128, 256, 384, 512};
     // the mode's default K set and a denser one (better fit, larger code footprint)
     const int kmasks[] = {resolve_k_mask(mode, 0, nullptr),
-                          resolve_k_mask(mode, wide_rows(mode) ? kKMaskFP64Alt : kKMaskFloatAlt, nullptr)};
+                          resolve_k_mask(mode, mode == HWT_BATCHED_FP64 ? kKMaskFP64Alt
+                                                   : (mode == HWT_BATCHED_DF64 ? kKMaskFP64 : kKMaskFloatAlt), nullptr)};
     const int n_kmasks = 2;
     double best_ms = 1e300;
     hwt_config best_cfg = c->tuned[mode];

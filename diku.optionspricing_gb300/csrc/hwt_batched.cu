@@ -1058,7 +1058,9 @@ int resolve_k_mask(int mode, int requested, int *max_k)
     const bool dbl = mode == MODE_BATCHED_FP64 || mode == MODE_BATCHED_DF64;  // 64-bit rows: K <= 8
     const int allowed = dbl ? kKMaskFP64 : kKMaskAll;
     int m = requested & allowed;
-    if (m == 0) m = dbl ? kKMaskFP64 : kKMaskFloat;
+    // defaults: every K for the FP64-pipe-bound double rows; the issue-bound
+    // double-float rows, like float rows, do better with fewer K (less code)
+    if (m == 0) m = mode == MODE_BATCHED_FP64 ? kKMaskFP64 : (mode == MODE_BATCHED_DF64 ? kKMaskFP64Alt : kKMaskFloat);
     int mk = 1;
     for (int q = 0; q < kNumK; ++q)
         if ((m >> q) & 1) mk = kWarpK[q];

@@ -102,7 +102,8 @@ typedef struct hwt_config {
     int32_t record_busy;   /* 1 = record per-block busy time for the tail-imbalance stat */
     int32_t warp_k_mask;   /* nodes-per-lane values warp tasks may use: bit q allows the q-th of
                               {1, 2, 3, 4, 5, 6, 7, 8, 12, 16}; 12 and 16 apply to float rows
-                              only; 0 = the mode's default (FP64: 1..8; float rows: 1, 2, 4, 8, 16) */
+                              only; 0 = the mode's default (FP64: 1..8; double-float: 1, 2, 3, 4, 6, 8;
+                              float rows: 1, 2, 4, 8, 16) */
 } hwt_config;
 
 /* Run statistics, filled when a non-NULL pointer is passed.  Times are CUDA-event
