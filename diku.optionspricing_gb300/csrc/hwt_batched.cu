@@ -589,7 +589,32 @@ struct Slice {
         }
     }
 
-    // One forward step, in place: r <- G o gather(r).
+    // Top-edge fixes of the step just taken, then the halo of the next step and its
+    // top-edge values: one switch on ts where a step would otherwise take two.
+    // (exchange_warp is defined after Slice; X is that function, passed in.)
+    template <bool FWD, class X>
+    __device__ __forceinline__ void fix_then_next(R &w1, R &w3, R &w1b, Halo<R> &h, X &&exchange)
+    {
+        switch (ts) {
+#define HWT_FIX_NEXT(T)                                  \
+    case T:                                              \
+        if constexpr (T < K) {                           \
+            top_fix<T, FWD>(w1, w3, w1b);                \
+            h = exchange();                              \
+            save_top<T>(h, w1, w3, w1b);                 \
+        }                                                \
+        break;
+            HWT_FIX_NEXT(0) HWT_FIX_NEXT(1) HWT_FIX_NEXT(2) HWT_FIX_NEXT(3) HWT_FIX_NEXT(4) HWT_FIX_NEXT(5)
+            HWT_FIX_NEXT(6) HWT_FIX_NEXT(7) HWT_FIX_NEXT(8) HWT_FIX_NEXT(9) HWT_FIX_NEXT(10) HWT_FIX_NEXT(11)
+            HWT_FIX_NEXT(12) HWT_FIX_NEXT(13) HWT_FIX_NEXT(14) HWT_FIX_NEXT(15)
+#undef HWT_FIX_NEXT
+            default: break;
+        }
+    }
+
+    // One forward step, in place: r <- G o gather(r).  TOP = false leaves the
+    // top-edge terms to the caller (fix_then_next).
+    template <bool TOP = true>
     __device__ __forceinline__ void forward_step(const Halo<R> &h, bool edge_live)
     {
         constexpr int S2 = 2 % K;  // slot of node 2
@@ -598,7 +623,7 @@ struct Slice {
         const R jout = (edge_live && n0) ? jlo : (R)0;
         const R jin = (edge_live && n2) ? jlo : (R)0;
         const R src2 = old_at<S2, -2>(h);  // node 0 seen from node 2 (read before the update)
-        if (edge_live) top_values(h, w1, w3, w1b);
+        if (TOP && edge_live) top_values(h, w1, w3, w1b);
         if constexpr (!Mode::kFlux) {
             R prev = h.l1;
 #pragma unroll
@@ -626,16 +651,17 @@ struct Slice {
                 eprev = e;
             }
         }
-        if (edge_live) top_fixes<true>(w1, w3, w1b);
+        if (TOP && edge_live) top_fixes<true>(w1, w3, w1b);
     }
 
     // One backward step, in place: r <- G o P r (flux: on the deviation from `base`).
+    template <bool TOP = true>
     __device__ __forceinline__ void backward_step(const Halo<R> &h, bool edge_live, R base)
     {
         R w1 = (R)0, w3 = (R)0, w1b = (R)0;
         const R j0 = (edge_live && n0) ? jlo : (R)0;  // bottom-edge jump weight of node 0
         const R o2 = old_at<0, 2>(h);                 // node 2 seen from node 0 (read before the update)
-        if (edge_live) top_values(h, w1, w3, w1b);
+        if (TOP && edge_live) top_values(h, w1, w3, w1b);
         R prev = h.l1;
         if constexpr (!Mode::kFlux) {
 #pragma unroll
@@ -663,7 +689,7 @@ struct Slice {
                 dprev = d;
             }
         }
-        if (edge_live) top_fixes<false>(w1, w3, w1b);
+        if (TOP && edge_live) top_fixes<false>(w1, w3, w1b);
     }
 
     __device__ __forceinline__ S partial_sum(int k0, int W) const
@@ -838,10 +864,32 @@ __device__ void price_warp_task(const EngineParams &p, const WarpTask &task)
         if (rn > i && (unsigned)rn < mine) mine = (unsigned)rn;
         const int ev = (int)__reduce_min_sync(FULL, mine);  // next row whose sum someone needs
         const int stop = ev < fsteps ? ev : fsteps;          // steps i .. stop-1 produce rows .. stop
-        for (; i < stop; ++i) {
-            const bool live = i >= e_f;
-            const Halo<R> h = exchange_warp<R, K>(sl.r, L, live);
-            sl.forward_step(h, live);
+        if constexpr (!Mode::kFlux) {
+            // 64-bit rows (FP64-pipe-bound or 31 float operations a node): the
+            // top-edge lookups cost little beside the row update
+            for (; i < stop; ++i) {
+                const bool live = i >= e_f;
+                const Halo<R> h = exchange_warp<R, K>(sl.r, L, live);
+                sl.forward_step(h, live);
+            }
+        } else {
+            for (; i < stop && i < e_f; ++i) {
+                const Halo<R> h = exchange_warp<R, K>(sl.r, L, false);
+                sl.forward_step(h, false);
+            }
+            if (i < stop) {
+                // edge jumps live: one switch on the top-edge slot per step (two would
+                // cost the issue-bound float rows about a fifth of their time)
+                auto xch = [&]() { return exchange_warp<R, K>(sl.r, L, true); };
+                Halo<R> h = xch();
+                R w1 = (R)0, w3 = (R)0, w1b = (R)0;
+                sl.top_values(h, w1, w3, w1b);
+                for (; i < stop; ++i) {
+                    sl.template forward_step<false>(h, true);
+                    if (i + 1 < stop) sl.template fix_then_next<true>(w1, w3, w1b, h, xch);
+                    else sl.template top_fixes<true>(w1, w3, w1b);
+                }
+            }
         }
         if (ev <= fsteps) {
             S acc = sl.partial_sum(k0, W);
@@ -866,17 +914,50 @@ __device__ void price_warp_task(const EngineParams &p, const WarpTask &task)
         // next maturity step at or below i (one per tree), -1 if none left
         const int pm = (int)__reduce_max_sync(FULL, (pays && t.m <= i) ? (unsigned)(t.m + 1) : 0u) - 1;
         const int lo = pm > 0 ? pm : 0;
-        for (; i >= lo; --i) {
-            const bool live = i >= e_b;
-            const Halo<R> h = exchange_warp<R, K>(sl.r, L, live);
-            sl.backward_step(h, live, base);
-            if (i >= n_min && i >= t.n) {
+        auto after_step = [&](int row) {
+            if (row >= n_min && row >= t.n) {
 #pragma unroll
                 for (int s = 0; s < K; ++s) sl.r[s] = (k0 + s < W) ? face : (R)0;
             }
-            if (i == pm && pays && t.m == i) {
+            if (row == pm && pays && t.m == row) {
                 sl.payoff(sc.kappa, base, t.X, t.type);
                 base = (R)0;
+            }
+        };
+        if constexpr (!Mode::kFlux) {
+            for (; i >= lo; --i) {
+                const bool live = i >= e_b;
+                const Halo<R> h = exchange_warp<R, K>(sl.r, L, live);
+                sl.backward_step(h, live, base);
+                after_step(i);
+            }
+        } else {
+            if (i >= lo && i >= e_b) {
+                // edge jumps live: one switch on the top-edge slot per step, except where
+                // rows are reset or paid off between the fixes and the next exchange
+                auto xch = [&]() { return exchange_warp<R, K>(sl.r, L, true); };
+                Halo<R> h = xch();
+                R w1 = (R)0, w3 = (R)0, w1b = (R)0;
+                sl.top_values(h, w1, w3, w1b);
+                for (; i >= lo && i >= e_b; --i) {
+                    sl.template backward_step<false>(h, true, base);
+                    const bool more = i - 1 >= lo && i - 1 >= e_b;
+                    if (more && i < n_min && i != pm) {
+                        sl.template fix_then_next<false>(w1, w3, w1b, h, xch);
+                    } else {
+                        sl.template top_fixes<false>(w1, w3, w1b);
+                        after_step(i);
+                        if (more) {
+                            h = xch();
+                            sl.top_values(h, w1, w3, w1b);
+                        }
+                    }
+                }
+            }
+            for (; i >= lo; --i) {
+                const Halo<R> h = exchange_warp<R, K>(sl.r, L, false);
+                sl.backward_step(h, false, base);
+                after_step(i);
             }
         }
     }
