@@ -30,9 +30,13 @@
 // probability exactly (stay = 1 - up - down is never formed), with G written as
 // 1 + g, and the bond phase of the backward sweep carried as a deviation from
 // 100.  MIXED keeps the two alpha-fit sums, the scales, the payoff and the final
-// discount in double; FP32 does those in float too.
+// discount in double precision, as double-float pairs on the FP32 pipes (the
+// curve's discount factors come from the sizing pass, in double); FP32 does those
+// in float too.
 #include <float.h>
 #include <stdio.h>
+
+#include <type_traits>
 
 #include "hwt_df64.cuh"
 #include "hwt_internal.h"
@@ -55,7 +59,7 @@ struct ModeF32 {
 };
 struct ModeMix {
     typedef float Row;
-    typedef double Scal;
+    typedef df64 Scal;    // double precision without the FP64 pipe (GB300 issues it at 1/64 of FP32)
     static constexpr bool kFlux = true;
 };
 struct ModeDF64 {
@@ -76,6 +80,33 @@ __device__ __forceinline__ df64 shfl_up(df64 v, unsigned d, int w)
 __device__ __forceinline__ df64 shfl_down(df64 v, unsigned d, int w)
 {
     return df64_make(__shfl_down_sync(0xffffffffu, v.hi, d, w), __shfl_down_sync(0xffffffffu, v.lo, d, w));
+}
+
+template <typename T>
+__device__ __forceinline__ T shfl_xor(T v, int m) { return __shfl_xor_sync(0xffffffffu, v, m); }
+__device__ __forceinline__ df64 shfl_xor(df64 v, int m)
+{
+    return df64_make(__shfl_xor_sync(0xffffffffu, v.hi, m), __shfl_xor_sync(0xffffffffu, v.lo, m));
+}
+
+// Scalar types: double, float, or double-float pairs (df64) for float rows.
+template <typename S>
+constexpr bool kPairScal = std::is_same<S, df64>::value;
+
+// A row value as a scalar (exact).
+template <typename S, typename R>
+__device__ __forceinline__ S to_scal(R x)
+{
+    if constexpr (kPairScal<S>) return df64_make(x, 0.f);
+    else return (S)x;
+}
+
+// a + b of two row values as a scalar (exact for float rows).
+template <typename S, typename R>
+__device__ __forceinline__ S scal_sum(R a, R b)
+{
+    if constexpr (kPairScal<S>) return exact_sum(a, b);
+    else return (S)a + (S)b;
 }
 
 // a x + b y + c z in the gather form: two FMAs after a product for double rows
@@ -206,6 +237,16 @@ __global__ void size_kernel(EngineParams p)
             t.dt = s.dt; t.dr = s.dr; t.M = s.M; t.X = X;
             t.idx = i; t.jmax = s.jmax; t.n = s.n; t.m = s.m; t.jc = s.jc; t.width = s.width;
             t.term_unit = p.opt.term_unit[i]; t.type = ty; t.edges = (int8_t)s.edges;
+            t.disc = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (p.curve_discounts) {
+                // the curve's discount factors at steps n and m, once per option
+                // in double, for the pricing pass's double-float scales
+                const df64 pn(discount_at_step<double>(s.n, s.dt, t.term_unit, p.yc.rate, p.yc.day, p.yc.n));
+                const df64 pm((s.m >= 1 && s.m < s.n)
+                                  ? discount_at_step<double>(s.m, s.dt, t.term_unit, p.yc.rate, p.yc.day, p.yc.n)
+                                  : 1.0);
+                t.disc = make_float4(pn.hi, pn.lo, pm.hi, pm.lo);
+            }
             p.s.trees[i] = t;
             nodes = (unsigned long long)s.nodes;
             // warp tier up to the warp-task width; wider trees go to the smallest
@@ -694,22 +735,48 @@ struct Slice {
 
     __device__ __forceinline__ S partial_sum(int k0, int W) const
     {
-        S acc = (S)0;
+        if constexpr (kPairScal<S>) {
+            // float rows summed exactly: running TwoSums, their errors gathered
+            float hi = 0.f, lo = 0.f;
 #pragma unroll
-        for (int s = 0; s < K; ++s)
-            if (k0 + s < W) acc += (S)r[s];
-        return acc;
+            for (int s = 0; s < K; ++s) {
+                if (k0 + s < W) {
+                    float e;
+                    hi = two_sum(hi, r[s], e);
+                    lo = __fadd_rn(lo, e);
+                }
+            }
+            return fast_two_sum(hi, lo);
+        } else {
+            S acc = (S)0;
+#pragma unroll
+            for (int s = 0; s < K; ++s)
+                if (k0 + s < W) acc += (S)r[s];
+            return acc;
+        }
     }
 
     // Payoff at the maturity step: value = kappa * (base + row).
     __device__ __forceinline__ void payoff(S kappa, R base, double X, int type)
     {
+        if constexpr (kPairScal<S>) {
+            // the bond value and the strike nearly cancel: the difference is taken
+            // in double-float and rounded to the row's float once
+            const df64 x(X);
 #pragma unroll
-        for (int s = 0; s < K; ++s) {
-            const S c = kappa * ((S)base + (S)r[s]);
-            const S x = (S)X;
-            const S p = (type == 1) ? (x - c) : (c - x);
-            r[s] = (R)(p < (S)0 ? (S)0 : p);
+            for (int s = 0; s < K; ++s) {
+                const float d = diff_to_float(x, kappa * exact_sum(base, r[s]));
+                const float p = (type == 1) ? d : -d;
+                r[s] = p < 0.f ? 0.f : p;
+            }
+        } else {
+#pragma unroll
+            for (int s = 0; s < K; ++s) {
+                const S c = kappa * ((S)base + (S)r[s]);
+                const S x = (S)X;
+                const S p = (type == 1) ? (x - c) : (c - x);
+                r[s] = (R)(p < (S)0 ? (S)0 : p);
+            }
         }
     }
 
@@ -798,25 +865,41 @@ struct Scales {
 };
 
 template <typename S>
-__device__ __forceinline__ Scales<S> tree_scales(const Tree &t, S sum_m1, S sum_n1, const DevYield &yc)
+__device__ __forceinline__ Scales<S> tree_scales(const Tree &t, S sum_m1, S sum_n1, const EngineParams &p)
 {
     Scales<S> sc;
-    const S dt = (S)t.dt;
-    const S *rates;
-    if constexpr (sizeof(S) == 8) rates = (const S *)yc.rate; else rates = (const S *)yc.rate_f;
-    const S Pn = discount_at_step<S>(t.n, dt, t.term_unit, rates, yc.day, yc.n);
-    const S sn = Pn / sum_n1;
-    if (t.m >= 0 && t.m < t.n) {
-        S sm = (S)1;
-        if (t.m >= 1) {
-            const S Pm = discount_at_step<S>(t.m, dt, t.term_unit, rates, yc.day, yc.n);
-            sm = Pm / sum_m1;
+    if constexpr (kPairScal<S>) {
+        // discount factors from the sizing pass (read here, not with the tree
+        // record, so they hold no registers through the forward sweep)
+        const float4 d = t.idx >= 0 ? p.s.trees[t.idx].disc : make_float4(1.f, 0.f, 1.f, 0.f);
+        const df64 sn = df64_make(d.x, d.y) / sum_n1;
+        if (t.m >= 0 && t.m < t.n) {
+            const df64 sm = (t.m >= 1) ? df64_make(d.z, d.w) / sum_m1 : df64_make(1.f, 0.f);
+            sc.kappa = sn / sm;
+            sc.final = sm;
+        } else {
+            sc.kappa = df64_make(1.f, 0.f);
+            sc.final = sn;
         }
-        sc.kappa = sn / sm;
-        sc.final = sm;
     } else {
-        sc.kappa = (S)1;
-        sc.final = sn;
+        const DevYield &yc = p.yc;
+        const S dt = (S)t.dt;
+        const S *rates;
+        if constexpr (sizeof(S) == 8) rates = (const S *)yc.rate; else rates = (const S *)yc.rate_f;
+        const S Pn = discount_at_step<S>(t.n, dt, t.term_unit, rates, yc.day, yc.n);
+        const S sn = Pn / sum_n1;
+        if (t.m >= 0 && t.m < t.n) {
+            S sm = (S)1;
+            if (t.m >= 1) {
+                const S Pm = discount_at_step<S>(t.m, dt, t.term_unit, rates, yc.day, yc.n);
+                sm = Pm / sum_m1;
+            }
+            sc.kappa = sn / sm;
+            sc.final = sm;
+        } else {
+            sc.kappa = (S)1;
+            sc.final = sn;
+        }
     }
     return sc;
 }
@@ -893,12 +976,12 @@ __device__ void price_warp_task(const EngineParams &p, const WarpTask &task)
         }
         if (ev <= fsteps) {
             S acc = sl.partial_sum(k0, W);
-            for (int off = 1; off < L; off <<= 1) acc += __shfl_xor_sync(FULL, acc, off);
+            for (int off = 1; off < L; off <<= 1) acc += shfl_xor(acc, off);
             if (rm == ev) sum_m1 = acc;
             if (rn == ev) sum_n1 = acc;
         }
     }
-    const Scales<S> sc = tree_scales<S>(t, sum_m1, sum_n1, p.yc);
+    const Scales<S> sc = tree_scales<S>(t, sum_m1, sum_n1, p);
 
     // ---- backward sweep from each tree's own height; rows of trees that have not
     // started yet are put back to the face value after every step.
@@ -968,8 +1051,8 @@ __device__ void price_warp_task(const EngineParams &p, const WarpTask &task)
     if (valid && lis == owner) {
         double price;
         if (t.n <= 0) price = 100.0;
-        else if (pays_at(t)) price = (double)(sc.final * (S)v);
-        else price = (double)(sc.final * ((S)base + (S)v));
+        else if (pays_at(t)) price = (double)(sc.final * to_scal<S>(v));
+        else price = (double)(sc.final * scal_sum<S>(base, v));
         p.out[t.idx] = price;
     }
 }
@@ -1004,7 +1087,7 @@ __device__ void price_block_tree(const EngineParams &p, const Tree &t, const Gro
         const int row = i + 1;
         if (row == t.m - 1 || row == t.n - 1) {
             S acc = sl.partial_sum(k0, W);
-            for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(FULL, acc, off);
+            for (int off = 16; off > 0; off >>= 1) acc += shfl_xor(acc, off);
             if (lane == 0) sh_red[aw0 + warp] = acc;
             tree_barrier(gr.bar, gr.nthreads);
             S tot = (S)0;
@@ -1014,7 +1097,7 @@ __device__ void price_block_tree(const EngineParams &p, const Tree &t, const Gro
             if (row == t.n - 1) sum_n1 = tot;
         }
     }
-    const Scales<S> sc = tree_scales<S>(t, sum_m1, sum_n1, p.yc);
+    const Scales<S> sc = tree_scales<S>(t, sum_m1, sum_n1, p);
 
     sl.setup_backward(t, k0);
     R base = Mode::kFlux ? (R)100 : (R)0;
@@ -1035,8 +1118,8 @@ __device__ void price_block_tree(const EngineParams &p, const Tree &t, const Gro
     if (tid == owner) {
         double price;
         if (t.n <= 0) price = 100.0;
-        else if (pays_at(t)) price = (double)(sc.final * (S)v);
-        else price = (double)(sc.final * ((S)base + (S)v));
+        else if (pays_at(t)) price = (double)(sc.final * to_scal<S>(v));
+        else price = (double)(sc.final * scal_sum<S>(base, v));
         p.out[t.idx] = price;
     }
 }

@@ -85,6 +85,38 @@ __device__ __forceinline__ df64 &operator+=(df64 &x, df64 y)
     return x;
 }
 
+// a + b of two floats, exactly
+__device__ __forceinline__ df64 exact_sum(float a, float b)
+{
+    float e;
+    const float s = two_sum(a, b, e);
+    return df64_make(s, e);
+}
+
+// x / y: a float quotient, its remainder x - q1 y from the exact product and a
+// difference that keeps the cancelled bits, and one correction term (relative
+// error a few u^2, u = 2^-24)
+__device__ __forceinline__ df64 operator/(df64 x, df64 y)
+{
+    const float q1 = __fdiv_rn(x.hi, y.hi);
+    const float ph = __fmul_rn(q1, y.hi);
+    const float pl = __fmaf_rn(q1, y.lo, __fmaf_rn(q1, y.hi, -ph));
+    float e;
+    const float s = two_sum(x.hi, -ph, e);
+    const float rem = __fadd_rn(s, __fadd_rn(e, __fsub_rn(x.lo, pl)));
+    return fast_two_sum(q1, __fdiv_rn(rem, y.hi));
+}
+
+// x - y rounded to float, accurate when the two nearly cancel: the leading parts'
+// difference is taken exactly (TwoSum), so the result is within an ulp of the
+// exact difference plus about 2 u^2 |x|.
+__device__ __forceinline__ float diff_to_float(df64 x, df64 y)
+{
+    float e;
+    const float s = two_sum(x.hi, -y.hi, e);
+    return __fadd_rn(s, __fadd_rn(e, __fsub_rn(x.lo, y.lo)));
+}
+
 // fma for every row type.  Declaring the df64 overload in this namespace hides the
 // global fma from unqualified calls here, so the float and double ones are
 // restated as exact-match overloads that forward to the C functions.

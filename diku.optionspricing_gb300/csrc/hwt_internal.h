@@ -12,7 +12,7 @@ enum Mode : int {
     MODE_PLAIN_FP64 = 0,    // one block per option, per-step alpha fit as the reference does
     MODE_BATCHED_FP64 = 1,  // binned persistent engine, double rows
     MODE_BATCHED_FP32 = 2,  // float rows, float sums and scales
-    MODE_BATCHED_MIXED = 3, // float rows, double sums, scales, payoff and final discount
+    MODE_BATCHED_MIXED = 3, // float rows; sums, scales, payoff and final discount in double precision
     MODE_BATCHED_DF64 = 4,  // double-float rows on the FP32 pipes, double sums and scales
 };
 constexpr int kNumModes = 5;
@@ -37,6 +37,7 @@ struct DevYield {
 // One option's tree as the sizing pass leaves it for the pricing pass.
 struct Tree {
     double dt, dr, M, X;
+    float4 disc;        // P(n dt), P(m dt) as double-float pairs (hi, lo, hi, lo), when sizing is asked for them
     int32_t idx;        // position in the caller's arrays
     int32_t jmax, n, m; // edge index, height, maturity step
     int32_t jc, width;  // half-width and width of the nodes that can carry value
@@ -123,6 +124,7 @@ struct EngineParams {
     int32_t max_group_k;    // largest K of a warp-group tree: 8 double rows, 16 float
     int32_t sort;           // HWT_SORT_* order inside the tiers (0 / '-': heaviest first)
     int32_t record_busy;
+    int32_t curve_discounts;  // sizing stores Tree::disc (modes with double-float scalars)
 };
 
 // Resolves a requested K mask for `mode` (0 = the mode's default) and the largest

@@ -133,6 +133,7 @@ extern "C" int hwt_price_device_noalloc(const hwt_options *dev_opts, const hwt_y
     p.sort = 0;
     p.big_threshold = 32 * p.max_warp_k;
     p.record_busy = 0;
+    p.curve_discounts = mode == HWT_BATCHED_MIXED ? 1 : 0;
 
     int sms = 0;
     e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);

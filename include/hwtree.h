@@ -46,7 +46,7 @@ extern "C" {
 #define HWT_PLAIN_FP64 0     /* one block per option, reference step structure, double */
 #define HWT_BATCHED_FP64 1   /* binned persistent engine, double */
 #define HWT_BATCHED_FP32 2   /* binned persistent engine, float throughout */
-#define HWT_BATCHED_MIXED 3  /* float rows, double alpha-fit sums, scales, payoff, discount */
+#define HWT_BATCHED_MIXED 3  /* float rows; alpha-fit sums, scales, payoff, discount in double precision */
 #define HWT_BATCHED_DF64 4   /* double-float rows (hi + lo floats, ~48 bits) on the FP32 pipes,
                                 double sums, scales, payoff, discount; within 1e-10 relative of FP64 */
 
