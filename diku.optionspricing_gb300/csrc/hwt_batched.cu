@@ -393,13 +393,33 @@ struct Halo {
     R l1, l2, r1, r2;
 };
 
+// A thread's K node values in registers.  Float rows with an even K are held as
+// K/2 pairs (node s, node s + K/2), so the flux stencils run on the paired FP32
+// instructions (two FMAs per issue slot): the pair of right neighbours of pair p
+// is pair p+1, except across the slice's middle.
+template <typename R, int K, bool PAIRED = std::is_same<R, float>::value && K % 2 == 0>
+struct Nodes {
+    static constexpr bool kPaired = false;
+    R v[K];
+    __device__ __forceinline__ R &operator[](int s) { return v[s]; }
+    __device__ __forceinline__ const R &operator[](int s) const { return v[s]; }
+};
+template <int K>
+struct Nodes<float, K, true> {
+    static constexpr bool kPaired = true;
+    static constexpr int H = K / 2;
+    float2 v[H];
+    __device__ __forceinline__ float &operator[](int s) { return s < H ? v[s].x : v[s - H].y; }
+    __device__ __forceinline__ const float &operator[](int s) const { return s < H ? v[s].x : v[s - H].y; }
+};
+
 template <class Mode, int K>
 struct Slice {
     typedef typename Mode::Row R;
     typedef typename Mode::Scal S;
 
-    R r[K];                 // current row, nodes k0 .. k0+K-1
-    R c0[K], c1[K], c2[K];  // FP64: fa/fb/fc or ba/bb/bc.  Flux: up, -down of the next node, g.
+    Nodes<R, K> r;           // current row, nodes k0 .. k0+K-1
+    Nodes<R, K> c0, c1, c2;  // FP64: fa/fb/fc or ba/bb/bc.  Flux: up, -down of the next node, g.
     R cl, cd0;              // flux: up of node k0-1, -down of node k0
     // Edge jumps (+-jmax branch two nodes away).  Nodes 0 and 2 sit at compile-time
     // slots (0 and 2 % K) and their terms are part of the step loop; node W-1 sits
@@ -676,6 +696,27 @@ struct Slice {
                 r[s] = v;
                 prev = cur;
             }
+        } else if constexpr (Nodes<R, K>::kPaired) {
+            // the same operations on pairs (node p, node p+H); a - b as fma(b, -1, a)
+            // rounds as the subtraction, so the results are the unpaired ones
+            constexpr int H = K / 2;
+            const float2 m1 = make_float2(-1.f, -1.f);
+            // pair H-1's right neighbours are node H (pair 0's second) and the halo
+            const float2 e_last =
+                __ffma2_rn(c0.v[H - 1], r.v[H - 1], __fmul2_rn(c1.v[H - 1], make_float2(r.v[0].y, h.r1)));
+            float2 ep = make_float2(fma(cl, h.l1, cd0 * r[0]), e_last.x);  // links k0-1 and k0+H-1
+#pragma unroll
+            for (int q = 0; q < H; ++q) {
+                const float2 e = (q == H - 1) ? e_last : __ffma2_rn(c0.v[q], r.v[q], __fmul2_rn(c1.v[q], r.v[q + 1]));
+                float2 v = __fadd2_rn(r.v[q], __ffma2_rn(e, m1, ep));
+                if (q == 0) v.x = fma(-jout, r.v[0].x, v.x);
+                if (q == S2 % H) {
+                    if (S2 < H) v.x = fma(jin, src2, v.x);
+                    else v.y = fma(jin, src2, v.y);
+                }
+                r.v[q] = __ffma2_rn(c2.v[q], v, v);
+                ep = e;
+            }
         } else {
             // net flux e_k = up_k r_k - down_{k+1} r_{k+1} across each link, computed
             // once and used by both ends (the row's sum is kept exactly)
@@ -713,6 +754,22 @@ struct Slice {
                 if (s == 0) v = fma(j0, o2, v);
                 r[s] = v;
                 prev = cur;
+            }
+        } else if constexpr (Nodes<R, K>::kPaired) {
+            // paired as the forward step; -down of node p is c1 of node p-1
+            constexpr int H = K / 2;
+            const float2 m1 = make_float2(-1.f, -1.f);
+            const float2 b2 = make_float2(base, base);
+            const float2 d_last = __ffma2_rn(r.v[H - 1], m1, make_float2(r.v[0].y, h.r1));
+            float2 dp = make_float2(r[0] - prev, d_last.x);  // differences at nodes k0-1 and k0+H-1
+#pragma unroll
+            for (int q = 0; q < H; ++q) {
+                const float2 d = (q == H - 1) ? d_last : __ffma2_rn(r.v[q], m1, r.v[q + 1]);
+                const float2 nd = (q == 0) ? make_float2(cd0, c1.v[H - 1].x) : c1.v[q - 1];
+                float2 v = __fadd2_rn(r.v[q], __ffma2_rn(c0.v[q], d, __fmul2_rn(nd, dp)));
+                if (q == 0) v.x = fma(j0, o2 - r.v[0].x, v.x);
+                r.v[q] = __ffma2_rn(c2.v[q], __fadd2_rn(v, b2), v);
+                dp = d;
             }
         } else {
             // differences D_k = r_{k+1} - r_k, each computed once:
@@ -795,7 +852,7 @@ struct Slice {
 // branch nowhere outward) or feed nodes outside the active cone.  The second
 // neighbours are needed only while the edge jumps are live.
 template <typename R, int K>
-__device__ __forceinline__ Halo<R> exchange_warp(const R (&r)[K], int L, bool two)
+__device__ __forceinline__ Halo<R> exchange_warp(const Nodes<R, K> &r, int L, bool two)
 {
     Halo<R> h;
     if constexpr (K >= 2) {
@@ -816,7 +873,7 @@ __device__ __forceinline__ Halo<R> exchange_warp(const R (&r)[K], int L, bool tw
 // nodes of every warp through shared memory (double buffered, so one barrier per
 // step is enough).
 template <typename R, int K>
-__device__ __forceinline__ Halo<R> exchange_block(const R (&r)[K], R *sh, int parity, const Group &gr)
+__device__ __forceinline__ Halo<R> exchange_block(const Nodes<R, K> &r, R *sh, int parity, const Group &gr)
 {
     // shared slots are indexed by the warp's index in the block; neighbours are
     // the adjacent warps of the same group
