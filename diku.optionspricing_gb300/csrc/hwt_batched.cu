@@ -565,10 +565,15 @@ struct Slice {
     // Old values the top-edge terms need, per compile-time slot TS of node W-1.
     // Seen from the thread owning node W-1: w1 = node W-1, w3 = node W-3.  Seen
     // from the thread owning node W-3 (possibly the previous thread): w1b = node W-1.
+    // Slots node W-1 can take: W = 2 jc + 1 is odd, so for an even K the slot
+    // (W-1) % K is even; the other switch cases stay empty (less code to fetch).
+    template <int TS>
+    static constexpr bool kTopSlot = TS < K && (K % 2 == 1 || TS % 2 == 0);
+
     template <int TS>
     __device__ __forceinline__ void save_top(const Halo<R> &h, R &w1, R &w3, R &w1b) const
     {
-        if constexpr (TS < K) {
+        if constexpr (kTopSlot<TS>) {
             constexpr int S3 = (TS + 2 * K - 2) % K;  // slot of node W-3
             w1 = r[TS];
             w3 = old_at<TS, -2>(h);
@@ -594,7 +599,8 @@ struct Slice {
             case 12: save_top<12>(h, w1, w3, w1b); break;
             case 13: save_top<13>(h, w1, w3, w1b); break;
             case 14: save_top<14>(h, w1, w3, w1b); break;
-            default: save_top<15>(h, w1, w3, w1b); break;
+            case 15: save_top<15>(h, w1, w3, w1b); break;
+            default: break;
         }
     }
 
@@ -610,7 +616,7 @@ struct Slice {
     template <int TS, bool FWD>
     __device__ __forceinline__ void top_fix(R w1, R w3, R w1b)
     {
-        if constexpr (TS < K) {
+        if constexpr (kTopSlot<TS>) {
             constexpr int S3 = (TS + 2 * K - 2) % K;
             if constexpr (FWD) {
                 if constexpr (Mode::kFlux) {
@@ -646,7 +652,8 @@ struct Slice {
             case 12: top_fix<12, FWD>(w1, w3, w1b); break;
             case 13: top_fix<13, FWD>(w1, w3, w1b); break;
             case 14: top_fix<14, FWD>(w1, w3, w1b); break;
-            default: top_fix<15, FWD>(w1, w3, w1b); break;
+            case 15: top_fix<15, FWD>(w1, w3, w1b); break;
+            default: break;
         }
     }
 
@@ -659,7 +666,7 @@ struct Slice {
         switch (ts) {
 #define HWT_FIX_NEXT(T)                                  \
     case T:                                              \
-        if constexpr (T < K) {                           \
+        if constexpr (kTopSlot<T>) {                     \
             top_fix<T, FWD>(w1, w3, w1b);                \
             h = exchange();                              \
             save_top<T>(h, w1, w3, w1b);                 \
