@@ -184,9 +184,11 @@ __host__ __device__ int pick_warp_class(int width, int k_mask)
 }
 
 // Descending log buckets, `per` per octave: heavy work (tall trees) sorts first.
+// (A float logarithm: buckets only order the work, and the double one costs the
+// FP64-bound sizing pass about a tenth of its time.)
 __device__ __forceinline__ int desc_bucket(double v, int per)
 {
-    int b = (int)(log2(v + 1.0) * per);
+    int b = (int)(log2f((float)v + 1.0f) * (float)per);
     if (b > kBuckets - 1) b = kBuckets - 1;
     return kBuckets - 1 - b;
 }
@@ -219,6 +221,7 @@ __global__ void size_kernel(EngineParams p)
     const int lane = threadIdx.x & 31;
     int key = -1;
     unsigned long long nodes = 0;
+    int wmax = 0, hmax = 0;
     if (i < p.opt.n) {
         Shape s;
         int st = make_shape(s, p.opt.bond_maturity[i], p.opt.option_maturity[i], p.opt.term_unit[i],
@@ -273,9 +276,16 @@ __global__ void size_kernel(EngineParams p)
             if (tier == kWarpTier) key = kWarpTier * kBuckets + bucket * kClassSlots + class_slot(cls);
             else key = tier * kBuckets + bucket;
             p.s.keys[i] = key;
-            atomicMax(&p.s.status->max_width, s.width);
-            atomicMax(&p.s.status->max_height, s.n);
+            wmax = s.width;
+            hmax = s.n;
         }
+    }
+    // warp-aggregated: one atomic per warp, not 32 on the same address
+    wmax = (int)__reduce_max_sync(FULL, (unsigned)wmax);
+    hmax = (int)__reduce_max_sync(FULL, (unsigned)hmax);
+    if (lane == 0 && wmax > 0) {
+        atomicMax(&p.s.status->max_width, wmax);
+        atomicMax(&p.s.status->max_height, hmax);
     }
     // warp-aggregated histogram and node count
     for (int off = 16; off > 0; off >>= 1) nodes += __shfl_xor_sync(FULL, nodes, off);
@@ -284,13 +294,31 @@ __global__ void size_kernel(EngineParams p)
     if (key >= 0 && lane == __ffs(peers) - 1) atomicAdd(&p.s.hist[key], __popc(peers));
 }
 
-// One block: exclusive scans of the key histogram into bin starts and warp-task
-// starts, and the tier sizes.
+// Zeroes the key histogram and fill counters and resets the run status (one
+// launch instead of three memsets).
+__global__ void reset_kernel(EngineParams p)
+{
+    int4 *h = reinterpret_cast<int4 *>(p.s.hist);  // hist | fill, 2 kKeyBins counters
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < kKeyBins / 2; i += gridDim.x * blockDim.x)
+        h[i] = make_int4(0, 0, 0, 0);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        RunStatus z = {};
+        z.first_bad = ~0ull;
+        *p.s.status = z;
+    }
+}
+
+// Exclusive scans of the key histogram into bin starts and warp-task starts, one
+// bin per thread (coalesced), in kScanBlocks blocks: each block writes the starts
+// within itself and its totals; the last block to finish (a fence and a counter,
+// no waiting) turns the totals into block offsets, which the scatter adds.
 __device__ __forceinline__ int bin_tasks(int b, int c)
 {
     if (b < kWarpTier * kBuckets || c == 0) return 0;  // group tiers: no warp tasks
-    const int G = 32 / cls_L((b - kWarpTier * kBuckets) % kClassSlots);  // slot % kNumL is the L index
-    return (c + G - 1) / G;
+    // G = 32 / L = 2^(5 - l) trees per task, l = slot % kNumL (kClassSlots is a
+    // multiple of kNumL); shifts, not divisions: this runs for every bin
+    const int sh = 5 - (b - kWarpTier * kBuckets) % kNumL;
+    return (c + (1 << sh) - 1) >> sh;
 }
 
 __device__ __forceinline__ int warp_inclusive_scan(int v, int lane)
@@ -303,57 +331,59 @@ __device__ __forceinline__ int warp_inclusive_scan(int v, int lane)
     return v;
 }
 
-// Each warp owns a contiguous run of bins and reads it 32 bins at a time
-// (coalesced): pass 1 sums the run, warp 0 scans the 32 run sums, pass 2 scans
-// each 32-bin tile with shuffles and writes the starts.
-__global__ void __launch_bounds__(1024) scan_kernel(EngineParams p)
+__global__ void __launch_bounds__(kScanBlock) scan_kernel(EngineParams p)
 {
-    constexpr int T = 1024, NW = T / 32;
-    constexpr int SEG = (kKeyBins + NW - 1) / NW;
+    constexpr int NW = kScanBlock / 32;
     __shared__ int s_a[NW], s_b[NW];
+    __shared__ int s_last;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int b0 = warp * SEG, b1 = min(kKeyBins, b0 + SEG);
-    int sa = 0, sb = 0;
-    for (int b = b0 + lane; b < b1; b += 32) {
-        const int c = p.s.hist[b];
-        sa += c;
-        sb += bin_tasks(b, c);
-    }
-    for (int off = 16; off > 0; off >>= 1) {
-        sa += __shfl_xor_sync(FULL, sa, off);
-        sb += __shfl_xor_sync(FULL, sb, off);
-    }
-    if (lane == 0) { s_a[warp] = sa; s_b[warp] = sb; }
+    const int b = blockIdx.x * kScanBlock + threadIdx.x;
+    const int c = p.s.hist[b];
+    const int t = bin_tasks(b, c);
+    const int ia = warp_inclusive_scan(c, lane), it = warp_inclusive_scan(t, lane);
+    if (lane == 31) { s_a[warp] = ia; s_b[warp] = it; }
     __syncthreads();
     if (warp == 0) {
-        const int a = s_a[lane], t = s_b[lane];
-        const int ia = warp_inclusive_scan(a, lane), it = warp_inclusive_scan(t, lane);
-        s_a[lane] = ia - a;
-        s_b[lane] = it - t;
-        if (lane == 31) p.s.status->n_warp_tasks = it;
+        const int a = s_a[lane], x = s_b[lane];
+        const int xa = warp_inclusive_scan(a, lane), xt = warp_inclusive_scan(x, lane);
+        s_a[lane] = xa - a;
+        s_b[lane] = xt - x;
+        if (lane == 31) {
+            p.s.bin_start[kScanOffsets + blockIdx.x] = xa;  // the block's totals
+            p.s.task_start[kScanOffsets + blockIdx.x] = xt;
+        }
     }
     __syncthreads();
-    int ea = s_a[warp], eb = s_b[warp];
-    for (int base = b0; base < b1; base += 32) {
-        const int b = base + lane;
-        const int c = b < b1 ? p.s.hist[b] : 0;
-        const int t = b < b1 ? bin_tasks(b, c) : 0;
-        const int ic = warp_inclusive_scan(c, lane), it = warp_inclusive_scan(t, lane);
-        if (b < b1) {
-            p.s.bin_start[b] = ea + ic - c;
-            p.s.task_start[b] = eb + it - t;
-        }
-        ea += __shfl_sync(FULL, ic, 31);
-        eb += __shfl_sync(FULL, it, 31);
-    }
-    // tier boundaries (global writes of the block are visible to it after the barrier)
+    p.s.bin_start[b] = s_a[warp] + ia - c;
+    p.s.task_start[b] = s_b[warp] + it - t;
+    __threadfence();
     __syncthreads();
-    if (threadIdx.x == 0) {
-        for (int t = 0; t < kGroupTiers; ++t) {
-            const int a = p.s.bin_start[t * kBuckets], b = p.s.bin_start[(t + 1) * kBuckets];
-            p.s.status->tier_start[t] = a;
-            p.s.status->tier_count[t] = b - a;
-        }
+    if (threadIdx.x == 0) s_last = atomicAdd(&p.s.status->scan_blocks_done, 1) == kScanBlocks - 1;
+    __syncthreads();
+    if (!s_last || warp != 0) return;
+    // last block: exclusive scan of the block totals (<= 64, two per lane)
+    __threadfence();
+    const int *tb = p.s.bin_start + kScanOffsets, *tt = p.s.task_start + kScanOffsets;
+    const int a0 = lane < kScanBlocks ? __ldcg(tb + lane) : 0, a1 = lane + 32 < kScanBlocks ? __ldcg(tb + lane + 32) : 0;
+    const int t0 = lane < kScanBlocks ? __ldcg(tt + lane) : 0, t1 = lane + 32 < kScanBlocks ? __ldcg(tt + lane + 32) : 0;
+    const int ia0 = warp_inclusive_scan(a0, lane), ia1 = warp_inclusive_scan(a1, lane);
+    const int it0 = warp_inclusive_scan(t0, lane), it1 = warp_inclusive_scan(t1, lane);
+    const int sa0 = __shfl_sync(FULL, ia0, 31), st0 = __shfl_sync(FULL, it0, 31);
+    if (lane < kScanBlocks) {
+        p.s.bin_start[kScanOffsets + lane] = ia0 - a0;
+        p.s.task_start[kScanOffsets + lane] = it0 - t0;
+    }
+    if (lane + 32 < kScanBlocks) {
+        p.s.bin_start[kScanOffsets + lane + 32] = sa0 + ia1 - a1;
+        p.s.task_start[kScanOffsets + lane + 32] = st0 + it1 - t1;
+    }
+    if (lane == 31) p.s.status->n_warp_tasks = st0 + it1;
+    // tier boundaries: the group tiers' bins all lie in scan block 0 (offset 0)
+    static_assert((kGroupTiers + 1) * kBuckets <= kScanBlock, "tier bins in the first scan block");
+    if (lane < kGroupTiers) {
+        const int a = __ldcg(p.s.bin_start + lane * kBuckets), e = __ldcg(p.s.bin_start + (lane + 1) * kBuckets);
+        p.s.status->tier_start[lane] = a;
+        p.s.status->tier_count[lane] = e - a;
     }
 }
 
@@ -366,18 +396,19 @@ __global__ void scatter_kernel(EngineParams p)
     const int key = p.s.keys[i];
     if (key < 0) return;
     const int q = atomicAdd(&p.s.fill[key], 1);
-    const int pos = p.s.bin_start[key] + q;
+    const int blk = kScanOffsets + key / kScanBlock;
+    const int pos = p.s.bin_start[key] + p.s.bin_start[blk] + q;
     p.s.order[pos] = i;
     if (key >= kWarpTier * kBuckets) {
-        const int cls = slot_class((key - kWarpTier * kBuckets) % kClassSlots);
-        const int G = 32 / cls_L(cls & 63);
-        if (q % G == 0) {
+        const int sh = 5 - (key - kWarpTier * kBuckets) % kNumL;  // G = 2^sh trees per task
+        const int G = 1 << sh;
+        if ((q & (G - 1)) == 0) {
             WarpTask t;
             t.start = pos;
             const int left = p.s.hist[key] - q;
             t.count = (int16_t)(left < G ? left : G);
-            t.cls = (int16_t)cls;
-            p.s.tasks[p.s.task_start[key] + q / G] = t;
+            t.cls = (int16_t)slot_class((key - kWarpTier * kBuckets) % kClassSlots);
+            p.s.tasks[p.s.task_start[key] + p.s.task_start[blk] + (q >> sh)] = t;
         }
     }
 }
@@ -1305,21 +1336,21 @@ int warp_class_of(int width, int *K, int *L)
     return c;
 }
 
-int sizing_launches() { return 3; }
+int sizing_launches() { return 4; }
 
 cudaError_t launch_sizing(const EngineParams &p, cudaStream_t stream)
 {
     const int n = p.opt.n;
     cudaError_t e;
-    if ((e = cudaMemsetAsync(p.s.hist, 0, sizeof(int32_t) * kKeyBins * 2, stream)) != cudaSuccess) return e;
-    // status: zero counters, first_bad = all ones
-    if ((e = cudaMemsetAsync(p.s.status, 0, sizeof(RunStatus), stream)) != cudaSuccess) return e;
-    if ((e = cudaMemsetAsync(&p.s.status->first_bad, 0xff, 8, stream)) != cudaSuccess) return e;
+    reset_kernel<<<48, 512, 0, stream>>>(p);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
     if (n > 0) {
-        size_kernel<<<(n + 255) / 256, 256, 0, stream>>>(p);
+        // 64-thread blocks: the FP64-bound sizing of a 30,000-option batch reaches
+        // every SM (256-thread blocks left a quarter of them idle)
+        size_kernel<<<(n + 63) / 64, 64, 0, stream>>>(p);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
-    scan_kernel<<<1, 1024, 0, stream>>>(p);
+    scan_kernel<<<kScanBlocks, kScanBlock, 0, stream>>>(p);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     if (n > 0) {
         scatter_kernel<<<(n + 255) / 256, 256, 0, stream>>>(p);

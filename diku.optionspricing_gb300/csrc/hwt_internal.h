@@ -82,7 +82,14 @@ constexpr int kGroupTiers = 4;
 constexpr int kWarpTier = kGroupTiers;
 constexpr int kBuckets = 128;
 constexpr int kClassSlots = 384;
-constexpr int kKeyBins = kWarpTier * kBuckets + kBuckets * kClassSlots;
+constexpr int kKeyBinsUsed = kWarpTier * kBuckets + kBuckets * kClassSlots;  // keys are below this
+constexpr int kScanBlock = 1024;  // bins per block of the histogram scan
+constexpr int kScanBlocks = (kKeyBinsUsed + kScanBlock - 1) / kScanBlock;
+// bin_start / task_start hold the starts within each scan block for bins below
+// kScanOffsets and each scan block's offset at kScanOffsets + block
+constexpr int kScanOffsets = kScanBlocks * kScanBlock;
+constexpr int kKeyBins = kScanOffsets + 64;  // counters per array, padded with empty bins
+static_assert(kScanBlocks <= 64 && kKeyBins % 4 == 0 && kClassSlots % kNumL == 0, "bin layout");
 
 // Per-run status written by the device (read back after each run).
 struct RunStatus {
@@ -96,6 +103,7 @@ struct RunStatus {
     int32_t warp_counter;
     int32_t max_width;            // widest / tallest valid tree
     int32_t max_height;
+    int32_t scan_blocks_done;     // histogram scan blocks finished (the last one adds the offsets)
 };
 
 struct Scratch {
