@@ -699,7 +699,7 @@ struct Slice {
     case T:                                              \
         if constexpr (kTopSlot<T>) {                     \
             top_fix<T, FWD>(w1, w3, w1b);                \
-            h = exchange();                              \
+            h = exchange(K < 3 || T < 2 || !Mode::kFlux); \
             save_top<T>(h, w1, w3, w1b);                 \
         }                                                \
         break;
@@ -1030,6 +1030,11 @@ __device__ void price_warp_task(const EngineParams &p, const WarpTask &task)
     // the width-L shuffles), so the step loop carries no per-tree predicates.
     sl.setup_forward(t, k0);
     sl.ts = (task.cls >> 6) & 15;  // the warp's common top-edge slot
+    // While the edge jumps are live the second neighbours (l2, r2) are read only
+    // when node W-1 sits in slot 0 or 1 (node W-3 in the previous lane) or K < 3;
+    // otherwise float rows skip the step's two extra shuffles (double-float rows
+    // measured 1-2% slower without them, so they keep them).
+    const bool wide_halo = K < 3 || sl.ts < 2 || !Mode::kFlux;
     const int e_f = (int)__reduce_min_sync(FULL, (valid && t.edges) ? (unsigned)t.jmax : NONE);
     const int rm = (t.m >= 2 && t.m < t.n) ? t.m - 1 : -1;  // row m-1 (row 0 sums to 1)
     const int rn = (t.n >= 2) ? t.n - 1 : -1;               // row n-1
@@ -1047,7 +1052,7 @@ __device__ void price_warp_task(const EngineParams &p, const WarpTask &task)
             // top-edge lookups cost little beside the row update
             for (; i < stop; ++i) {
                 const bool live = i >= e_f;
-                const Halo<R> h = exchange_warp<R, K>(sl.r, L, live);
+                const Halo<R> h = exchange_warp<R, K>(sl.r, L, live && wide_halo);
                 sl.forward_step(h, live);
             }
         } else {
@@ -1058,8 +1063,8 @@ __device__ void price_warp_task(const EngineParams &p, const WarpTask &task)
             if (i < stop) {
                 // edge jumps live: one switch on the top-edge slot per step (two would
                 // cost the issue-bound float rows about a fifth of their time)
-                auto xch = [&]() { return exchange_warp<R, K>(sl.r, L, true); };
-                Halo<R> h = xch();
+                auto xch = [&](bool two) { return exchange_warp<R, K>(sl.r, L, two); };
+                Halo<R> h = xch(wide_halo);
                 R w1 = (R)0, w3 = (R)0, w1b = (R)0;
                 sl.top_values(h, w1, w3, w1b);
                 for (; i < stop; ++i) {
@@ -1105,7 +1110,7 @@ __device__ void price_warp_task(const EngineParams &p, const WarpTask &task)
         if constexpr (!Mode::kFlux) {
             for (; i >= lo; --i) {
                 const bool live = i >= e_b;
-                const Halo<R> h = exchange_warp<R, K>(sl.r, L, live);
+                const Halo<R> h = exchange_warp<R, K>(sl.r, L, live && wide_halo);
                 sl.backward_step(h, live, base);
                 after_step(i);
             }
@@ -1113,8 +1118,8 @@ __device__ void price_warp_task(const EngineParams &p, const WarpTask &task)
             if (i >= lo && i >= e_b) {
                 // edge jumps live: one switch on the top-edge slot per step, except where
                 // rows are reset or paid off between the fixes and the next exchange
-                auto xch = [&]() { return exchange_warp<R, K>(sl.r, L, true); };
-                Halo<R> h = xch();
+                auto xch = [&](bool two) { return exchange_warp<R, K>(sl.r, L, two); };
+                Halo<R> h = xch(wide_halo);
                 R w1 = (R)0, w3 = (R)0, w1b = (R)0;
                 sl.top_values(h, w1, w3, w1b);
                 for (; i >= lo && i >= e_b; --i) {
@@ -1126,7 +1131,7 @@ __device__ void price_warp_task(const EngineParams &p, const WarpTask &task)
                         sl.template top_fixes<false>(w1, w3, w1b);
                         after_step(i);
                         if (more) {
-                            h = xch();
+                            h = xch(wide_halo);
                             sl.top_values(h, w1, w3, w1b);
                         }
                     }
