@@ -50,6 +50,7 @@ struct GraphKey {
 struct hwt_ctx {
     int device = 0;
     int sms = 0;
+    bool host_coherent = false;  // the GPU reaches host memory through the host's page tables (NVLink-C2C)
     std::string gpu_name;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};  // call start, sizing start, pricing start, pricing end, call end
@@ -260,6 +261,17 @@ bool is_pinned(const void *p)
     return at.type == cudaMemoryTypeHost;
 }
 
+// The device address of a pinned (page-locked, mapped) host pointer, or null.
+void *device_view(const void *p)
+{
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
 std::string bad_option_message(const RunStatus &st)
 {
     const unsigned long long fb = st.first_bad;
@@ -452,6 +464,10 @@ hwt_ctx *hwt_create(int device, const char *tune_cache)
     if (ok) {
         c->sms = prop.multiProcessorCount;
         c->gpu_name = prop.name;
+        int coherent = 0;
+        if (cudaDeviceGetAttribute(&coherent, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device) != cudaSuccess)
+            cudaGetLastError();
+        c->host_coherent = coherent == 1;
     }
     ok = ok && cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) == cudaSuccess;
     for (int i = 0; i < 5 && ok; ++i) ok = cudaEventCreate(&c->ev[i]) == cudaSuccess;
@@ -539,6 +555,39 @@ int hwt_price_ex(hwt_ctx *c, const hwt_options *o, const hwt_yield *y, const hwt
     if ((r = check_config(c, cfg))) return r;
 
     const int64_t n = o->n;
+    const int grid = cfg.mode == HWT_PLAIN_FP64 ? 0 : pricing_blocks_per_sm(cfg.mode) * c->sms;
+    int launches = 0, graph_used = 0;
+    if (c->host_coherent) {
+        // Pinned caller arrays on a host that the GPU reaches coherently
+        // (NVLink-C2C): the sizing kernel reads the option fields where they are
+        // (one pass over 45 bytes per option, no copies in); the prices go to
+        // device memory and back in one copy (written straight into host memory
+        // from the pricing kernel, 8 scattered bytes per option, they cost the
+        // kernel ~5%).
+        void *v[9] = {device_view(o->strike), device_view(o->bond_maturity), device_view(o->option_maturity),
+                      device_view(o->a), device_view(o->sigma), device_view(o->term_unit),
+                      device_view(o->term_steps), device_view(o->type), device_view(out)};
+        bool all = true;
+        for (void *q : v) all = all && q;
+        if (all) {
+            DevOptions dopt;
+            dopt.n = o->n;
+            dopt.strike = (const double *)v[0];
+            dopt.bond_maturity = (const double *)v[1];
+            dopt.option_maturity = (const double *)v[2];
+            dopt.a = (const double *)v[3];
+            dopt.sigma = (const double *)v[4];
+            dopt.term_unit = (const uint16_t *)v[5];
+            dopt.term_steps = (const uint16_t *)v[6];
+            dopt.type = (const int8_t *)v[7];
+            if (stats) HWT_CUDA(c, cudaEventRecord(c->ev[0], c->stream), "event");
+            if ((r = run_batch(c, dopt, c->d_out, cfg, stats, &launches, &graph_used))) return r;
+            HWT_CUDA(c, cudaMemcpyAsync(out, c->d_out, 8 * n, cudaMemcpyDeviceToHost, c->stream), "prices D2H");
+            r = finish(c, cfg, stats, launches, graph_used, grid, 45 * n, 8 * n);
+            if (stats) timing_fill(c, stats, c->ev[0]);
+            return r;
+        }
+    }
     const Packing pk = packing(c->cap);
     char *d = (char *)c->d_opts;
     if (stats) HWT_CUDA(c, cudaEventRecord(c->ev[0], c->stream), "event");
@@ -576,12 +625,10 @@ int hwt_price_ex(hwt_ctx *c, const hwt_options *o, const hwt_yield *y, const hwt
     dopt.term_steps = (const uint16_t *)(d + pk.steps);
     dopt.type = (const int8_t *)(d + pk.type);
 
-    int launches = 0, graph_used = 0;
     if ((r = run_batch(c, dopt, c->d_out, cfg, stats, &launches, &graph_used))) return r;
     const bool out_pinned = is_pinned(out);
     double *dst = out_pinned ? out : c->h_out;
     HWT_CUDA(c, cudaMemcpyAsync(dst, c->d_out, 8 * n, cudaMemcpyDeviceToHost, c->stream), "prices D2H");
-    const int grid = cfg.mode == HWT_PLAIN_FP64 ? 0 : pricing_blocks_per_sm(cfg.mode) * c->sms;
     r = finish(c, cfg, stats, launches, graph_used, grid, h2d, 8 * n);
     if (!out_pinned) memcpy(out, c->h_out, 8 * n);
     if (stats) timing_fill(c, stats, c->ev[0]);
