@@ -428,7 +428,8 @@ struct Halo {
 // K/2 pairs (node s, node s + K/2), so the flux stencils run on the paired FP32
 // instructions (two FMAs per issue slot): the pair of right neighbours of pair p
 // is pair p+1, except across the slice's middle.
-template <typename R, int K, bool PAIRED = std::is_same<R, float>::value && K % 2 == 0>
+template <typename R, int K,
+          bool PAIRED = (std::is_same<R, float>::value || std::is_same<R, df64>::value) && K % 2 == 0>
 struct Nodes {
     static constexpr bool kPaired = false;
     R v[K];
@@ -443,6 +444,63 @@ struct Nodes<float, K, true> {
     __device__ __forceinline__ float &operator[](int s) { return s < H ? v[s].x : v[s - H].y; }
     __device__ __forceinline__ const float &operator[](int s) const { return s < H ? v[s].x : v[s - H].y; }
 };
+
+// One double-float node inside the paired storage (its hi and lo sit in two pairs).
+struct DF64Ref {
+    float &hi, &lo;
+    __device__ __forceinline__ operator df64() const { return df64_make(hi, lo); }
+    __device__ __forceinline__ DF64Ref &operator=(df64 x)
+    {
+        hi = x.hi;
+        lo = x.lo;
+        return *this;
+    }
+    __device__ __forceinline__ DF64Ref &operator+=(df64 x) { return *this = df64_make(hi, lo) + x; }
+};
+
+// Double-float rows with an even K: the same pairing, hi and lo parts in separate
+// pairs, so the compensated products run on the paired instructions.
+template <int K>
+struct Nodes<df64, K, true> {
+    static constexpr bool kPaired = true;
+    static constexpr int H = K / 2;
+    float2 hi[H], lo[H];
+    __device__ __forceinline__ DF64Ref operator[](int s)
+    {
+        return s < H ? DF64Ref{hi[s].x, lo[s].x} : DF64Ref{hi[s - H].y, lo[s - H].y};
+    }
+    __device__ __forceinline__ df64 operator[](int s) const
+    {
+        return s < H ? df64_make(hi[s].x, lo[s].x) : df64_make(hi[s - H].y, lo[s - H].y);
+    }
+    __device__ __forceinline__ df64x2 pair(int q) const
+    {
+        df64x2 r;
+        r.hi = hi[q];
+        r.lo = lo[q];
+        return r;
+    }
+    __device__ __forceinline__ void set_pair(int q, const df64x2 &x)
+    {
+        hi[q] = x.hi;
+        lo[q] = x.lo;
+    }
+};
+
+// Adds d * s to lane (S < H ? x : y) of a double-float pair (a scalar fix-up of one node).
+template <int S, int H>
+__device__ __forceinline__ void fma_lane(df64x2 &v, df64 d, df64 s)
+{
+    if constexpr (S < H) {
+        const df64 t = fma(d, s, df64_make(v.hi.x, v.lo.x));
+        v.hi.x = t.hi;
+        v.lo.x = t.lo;
+    } else {
+        const df64 t = fma(d, s, df64_make(v.hi.y, v.lo.y));
+        v.hi.y = t.hi;
+        v.lo.y = t.lo;
+    }
+}
 
 template <class Mode, int K>
 struct Slice {
@@ -723,7 +781,24 @@ struct Slice {
         const R jin = (edge_live && n2) ? jlo : (R)0;
         const R src2 = old_at<S2, -2>(h);  // node 0 seen from node 2 (read before the update)
         if (TOP && edge_live) top_values(h, w1, w3, w1b);
-        if constexpr (!Mode::kFlux) {
+        if constexpr (!Mode::kFlux && Nodes<R, K>::kPaired) {
+            // double-float rows on pairs (node q, node q+H): the compensated products
+            // of two nodes per instruction; the prices are bitwise the scalar loop's
+            constexpr int H = K / 2;
+            df64x2 prev, last;
+            prev.hi = make_float2(h.l1.hi, r.hi[H - 1].x);  // left neighbours of pair 0
+            prev.lo = make_float2(h.l1.lo, r.lo[H - 1].x);
+            last.hi = make_float2(r.hi[0].y, h.r1.hi);      // right neighbours of pair H-1
+            last.lo = make_float2(r.lo[0].y, h.r1.lo);
+#pragma unroll
+            for (int q = 0; q < H; ++q) {
+                const df64x2 cur = r.pair(q);
+                df64x2 v = dot3x2(c0.pair(q), prev, c1.pair(q), cur, c2.pair(q), (q == H - 1) ? last : r.pair(q + 1));
+                if (q == S2 % H) fma_lane<S2, H>(v, jin, src2);
+                r.set_pair(q, v);
+                prev = cur;
+            }
+        } else if constexpr (!Mode::kFlux) {
             R prev = h.l1;
 #pragma unroll
             for (int s = 0; s < K; ++s) {
@@ -783,7 +858,22 @@ struct Slice {
         const R o2 = old_at<0, 2>(h);                 // node 2 seen from node 0 (read before the update)
         if (TOP && edge_live) top_values(h, w1, w3, w1b);
         R prev = h.l1;
-        if constexpr (!Mode::kFlux) {
+        if constexpr (!Mode::kFlux && Nodes<R, K>::kPaired) {
+            constexpr int H = K / 2;
+            df64x2 pv, last;
+            pv.hi = make_float2(h.l1.hi, r.hi[H - 1].x);
+            pv.lo = make_float2(h.l1.lo, r.lo[H - 1].x);
+            last.hi = make_float2(r.hi[0].y, h.r1.hi);
+            last.lo = make_float2(r.lo[0].y, h.r1.lo);
+#pragma unroll
+            for (int q = 0; q < H; ++q) {
+                const df64x2 cur = r.pair(q);
+                df64x2 v = dot3x2(c0.pair(q), (q == H - 1) ? last : r.pair(q + 1), c1.pair(q), cur, c2.pair(q), pv);
+                if (q == 0) fma_lane<0, H>(v, j0, o2);
+                r.set_pair(q, v);
+                pv = cur;
+            }
+        } else if constexpr (!Mode::kFlux) {
 #pragma unroll
             for (int s = 0; s < K; ++s) {
                 const R cur = r[s];
@@ -846,7 +936,7 @@ struct Slice {
             S acc = (S)0;
 #pragma unroll
             for (int s = 0; s < K; ++s)
-                if (k0 + s < W) acc += (S)r[s];
+                if (k0 + s < W) acc += (S)(R)r[s];
             return acc;
         }
     }
@@ -867,7 +957,7 @@ struct Slice {
         } else {
 #pragma unroll
             for (int s = 0; s < K; ++s) {
-                const S c = kappa * ((S)base + (S)r[s]);
+                const S c = kappa * ((S)base + (S)(R)r[s]);
                 const S x = (S)X;
                 const S p = (type == 1) ? (x - c) : (c - x);
                 r[s] = (R)(p < (S)0 ? (S)0 : p);

@@ -158,4 +158,55 @@ __device__ __forceinline__ df64 dot3(df64 a, df64 x, df64 b, df64 y, df64 c, df6
     return fast_two_sum(s, lo);
 }
 
+// Two double-float numbers side by side (lanes .x and .y) for the paired FP32
+// instructions (__fadd2_rn, __fmul2_rn, __ffma2_rn: two operations per issue slot).
+// a - b is issued as fma(b, -1, a), which rounds as the subtraction, so every lane
+// of these functions gives bitwise the result of its scalar counterpart above.
+struct df64x2 {
+    float2 hi, lo;
+};
+
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
+
+__device__ __forceinline__ float2 two_sum2(float2 a, float2 b, float2 &e)
+{
+    const float2 s = __fadd2_rn(a, b);
+    const float2 bb = sub2(s, a);
+    e = __fadd2_rn(sub2(a, sub2(s, bb)), sub2(b, bb));
+    return s;
+}
+
+__device__ __forceinline__ df64x2 fast_two_sum2(float2 a, float2 b)
+{
+    const float2 s = __fadd2_rn(a, b);
+    df64x2 r;
+    r.hi = s;
+    r.lo = sub2(b, sub2(s, a));
+    return r;
+}
+
+// dot3 on two lanes, in an order that retires each product's terms early (the
+// operations and their operands are dot3's, so the results are bitwise the same)
+__device__ __forceinline__ float2 prod_err2(const df64x2 &a, const df64x2 &x, float2 &p)
+{
+    p = __fmul2_rn(a.hi, x.hi);
+    float2 e = __ffma2_rn(a.hi, x.hi, make_float2(-p.x, -p.y));
+    e = __ffma2_rn(a.hi, x.lo, e);
+    return __ffma2_rn(a.lo, x.hi, e);
+}
+
+__device__ __forceinline__ df64x2 dot3x2(const df64x2 &a, const df64x2 &x, const df64x2 &b, const df64x2 &y,
+                                         const df64x2 &c, const df64x2 &z)
+{
+    float2 p1, p2, p3, t1, t2;
+    const float2 e1 = prod_err2(a, x, p1);
+    const float2 e2 = prod_err2(b, y, p2);
+    float2 s = two_sum2(p1, p2, t1);
+    const float2 e12 = __fadd2_rn(e1, e2);
+    const float2 e3 = prod_err2(c, z, p3);
+    s = two_sum2(s, p3, t2);
+    const float2 lo = __fadd2_rn(e12, __fadd2_rn(e3, __fadd2_rn(t1, t2)));
+    return fast_two_sum2(s, lo);
+}
+
 }  // namespace hwt
