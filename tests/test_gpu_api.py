@@ -103,6 +103,33 @@ def test_device_entry_point_and_graph_equal_host(pkg, pricer, uneven):
     assert np.array_equal(out.cpu().numpy(), host)
 
 
+@pytest.mark.parametrize("mode", ["BATCHED_MIXED", "BATCHED_FP64", "PLAIN_FP64"])
+def test_pinned_host_arrays_equal_pageable(pkg, pricer, uneven, mode):
+    """Pinned (page-locked) host arrays: on a host the GPU reaches coherently the
+    sizing kernel reads them in place, elsewhere they are copied; the prices are
+    bitwise those of pageable arrays, and an invalid record in pinned memory is
+    still rejected with a NaN price."""
+    import torch
+    opts, y, _ = uneven
+    n = 4000 if mode == "PLAIN_FP64" else opts.N
+    sub = pkg.Options.from_batch({k: v[:n] for k, v in pkg.workloads.uneven_batch().items()})
+    m = getattr(pkg, mode)
+    ref = pricer.price(sub, y, m)
+    fields = {"strike": sub.StrikePrices, "bond_maturity": sub.Maturities, "option_maturity": sub.Lengths,
+              "term_unit": sub.TermUnits.view(np.int16), "term_steps": sub.TermStepCounts.view(np.int16),
+              "a": sub.ReversionRates, "sigma": sub.Volatilities, "type": sub.Types}
+    pin = {k: torch.from_numpy(np.ascontiguousarray(v)).pin_memory() for k, v in fields.items()}
+    out = torch.full((n,), -1.0, dtype=torch.float64).pin_memory()
+    st = pricer.price_host_ptrs({k: t.data_ptr() for k, t in pin.items()}, n, y, out.data_ptr(), m)
+    assert np.array_equal(out.numpy(), ref)
+    assert st.h2d_bytes == 45 * n and st.d2h_bytes == 8 * n
+    pin["a"][7] = -1.0  # mean reversion must be > 0
+    with pytest.raises(pkg.InvalidInput):
+        pricer.price_host_ptrs({k: t.data_ptr() for k, t in pin.items()}, n, y, out.data_ptr(), m)
+    got = out.numpy()
+    assert np.isnan(got[7]) and np.array_equal(np.delete(got, 7), np.delete(ref, 7))
+
+
 def test_block_sizes_agree(pkg, pricer, uneven):
     """Group size changes which trees share a warp or a block, not the answer."""
     opts, y, ref = uneven
