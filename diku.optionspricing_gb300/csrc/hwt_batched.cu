@@ -822,10 +822,12 @@ struct Slice {
             for (int q = 0; q < H; ++q) {
                 const float2 e = (q == H - 1) ? e_last : __ffma2_rn(c0.v[q], r.v[q], __fmul2_rn(c1.v[q], r.v[q + 1]));
                 float2 v = __fadd2_rn(r.v[q], __ffma2_rn(e, m1, ep));
-                if (q == 0) v.x = fma(-jout, r.v[0].x, v.x);
-                if (q == S2 % H) {
-                    if (S2 < H) v.x = fma(jin, src2, v.x);
-                    else v.y = fma(jin, src2, v.y);
+                if (edge_live) {  // a constant in the step loops: no dead fix-ups
+                    if (q == 0) v.x = fma(-jout, r.v[0].x, v.x);
+                    if (q == S2 % H) {
+                        if (S2 < H) v.x = fma(jin, src2, v.x);
+                        else v.y = fma(jin, src2, v.y);
+                    }
                 }
                 r.v[q] = __ffma2_rn(c2.v[q], v, v);
                 ep = e;
@@ -895,7 +897,7 @@ struct Slice {
                 const float2 d = (q == H - 1) ? d_last : __ffma2_rn(r.v[q], m1, r.v[q + 1]);
                 const float2 nd = (q == 0) ? make_float2(cd0, c1.v[H - 1].x) : c1.v[q - 1];
                 float2 v = __fadd2_rn(r.v[q], __ffma2_rn(c0.v[q], d, __fmul2_rn(nd, dp)));
-                if (q == 0) v.x = fma(j0, o2 - r.v[0].x, v.x);
+                if (edge_live && q == 0) v.x = fma(j0, o2 - r.v[0].x, v.x);
                 r.v[q] = __ffma2_rn(c2.v[q], __fadd2_rn(v, b2), v);
                 dp = d;
             }
