@@ -54,7 +54,10 @@ HWT_HD int32_t make_shape(Shape &s, double bond_maturity, double option_maturity
     if (!(a > 0.0)) return SHAPE_BAD_A;
     if (!isfinite(bond_maturity) || !isfinite(option_maturity) || !isfinite(sigma) || !isfinite(a))
         return SHAPE_NONFINITE;
-    const int units_per_year = (int)ceil(365.0 / term_unit);            // :33
+    // ceil(365.0 / term_unit) (:33) in integers: the double quotient is exact when
+    // term_unit divides 365 and otherwise lies at least 1/term_unit from an integer,
+    // so the two agree, and the sizing pass saves a double division per option
+    const int units_per_year = (365 + term_unit - 1) / term_unit;
     const double nreal = term_steps * units_per_year * bond_maturity;   // :35 (int * double)
     if (nreal > 1.0e7) return SHAPE_TOO_WIDE;
     s.n = (int32_t)nreal;
