@@ -341,7 +341,7 @@ int run_batch(hwt_ctx *c, const DevOptions &dopt, double *dev_out, const hwt_con
     p.big_threshold = std::min(cfg.big_threshold, 32 * p.max_warp_k);
     p.max_width = kMaxTreeWidth;
     p.record_busy = cfg.record_busy ? 1 : 0;
-    p.curve_discounts = cfg.mode == HWT_BATCHED_MIXED ? 1 : 0;
+    p.curve_discounts = (cfg.mode == HWT_BATCHED_MIXED || cfg.mode == HWT_BATCHED_DF64) ? 1 : 0;
 
     int grid = 0;
     if (cfg.mode != HWT_PLAIN_FP64) {

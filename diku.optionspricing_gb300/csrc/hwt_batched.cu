@@ -50,21 +50,25 @@ constexpr unsigned FULL = 0xffffffffu;
 struct ModeF64 {
     typedef double Row;
     typedef double Scal;
+    static constexpr bool kSizingDiscounts = false;  // P(n dt), P(m dt) from the sizing pass
     static constexpr bool kFlux = false;
 };
 struct ModeF32 {
     typedef float Row;
     typedef float Scal;
+    static constexpr bool kSizingDiscounts = false;  // P(n dt), P(m dt) from the sizing pass
     static constexpr bool kFlux = true;
 };
 struct ModeMix {
     typedef float Row;
     typedef df64 Scal;    // double precision without the FP64 pipe (GB300 issues it at 1/64 of FP32)
+    static constexpr bool kSizingDiscounts = true;  // P(n dt), P(m dt) from the sizing pass
     static constexpr bool kFlux = true;
 };
 struct ModeDF64 {
     typedef df64 Row;     // gather form like double rows, arithmetic on the FP32 pipes
     typedef double Scal;
+    static constexpr bool kSizingDiscounts = true;  // P(n dt), P(m dt) from the sizing pass
     static constexpr bool kFlux = false;
 };
 
@@ -934,6 +938,14 @@ struct Slice {
                 }
             }
             return fast_two_sum(hi, lo);
+        } else if constexpr (std::is_same<R, df64>::value) {
+            // double-float rows summed in double-float (terms of one sign), one
+            // conversion to the double scalar
+            df64 acc = df64_make(0.f, 0.f);
+#pragma unroll
+            for (int s = 0; s < K; ++s)
+                if (k0 + s < W) acc = acc + (R)r[s];
+            return (S)acc;
         } else {
             S acc = (S)0;
 #pragma unroll
@@ -1051,11 +1063,24 @@ struct Scales {
     S final;  // s_m (payoff) or s_n (bond only)
 };
 
-template <typename S>
+template <typename S, bool kSizingDisc>
 __device__ __forceinline__ Scales<S> tree_scales(const Tree &t, S sum_m1, S sum_n1, const EngineParams &p)
 {
     Scales<S> sc;
-    if constexpr (kPairScal<S>) {
+    if constexpr (kSizingDisc && std::is_same<S, double>::value) {
+        // double scalars, discount factors from the sizing pass (double-float rows:
+        // no curve lookups or exponentials on the FP64 pipe here)
+        const float4 d = t.idx >= 0 ? p.s.trees[t.idx].disc : make_float4(1.f, 0.f, 1.f, 0.f);
+        const double sn = (double)df64_make(d.x, d.y) / sum_n1;
+        if (t.m >= 0 && t.m < t.n) {
+            const double sm = (t.m >= 1) ? (double)df64_make(d.z, d.w) / sum_m1 : 1.0;
+            sc.kappa = sn / sm;
+            sc.final = sm;
+        } else {
+            sc.kappa = 1.0;
+            sc.final = sn;
+        }
+    } else if constexpr (kPairScal<S>) {
         // discount factors from the sizing pass (read here, not with the tree
         // record, so they hold no registers through the forward sweep)
         const float4 d = t.idx >= 0 ? p.s.trees[t.idx].disc : make_float4(1.f, 0.f, 1.f, 0.f);
@@ -1173,7 +1198,7 @@ __device__ void price_warp_task(const EngineParams &p, const WarpTask &task)
             if (rn == ev) sum_n1 = acc;
         }
     }
-    const Scales<S> sc = tree_scales<S>(t, sum_m1, sum_n1, p);
+    const Scales<S> sc = tree_scales<S, Mode::kSizingDiscounts>(t, sum_m1, sum_n1, p);
 
     // ---- backward sweep from each tree's own height; rows of trees that have not
     // started yet are put back to the face value after every step.
@@ -1289,7 +1314,7 @@ __device__ void price_block_tree(const EngineParams &p, const Tree &t, const Gro
             if (row == t.n - 1) sum_n1 = tot;
         }
     }
-    const Scales<S> sc = tree_scales<S>(t, sum_m1, sum_n1, p);
+    const Scales<S> sc = tree_scales<S, Mode::kSizingDiscounts>(t, sum_m1, sum_n1, p);
 
     sl.setup_backward(t, k0);
     R base = Mode::kFlux ? (R)100 : (R)0;
