@@ -487,7 +487,10 @@ hwt_ctx *hwt_create(int device, const char *tune_cache)
         memset(&t, 0, sizeof(t));
         t.mode = m;
         t.block_size = m == HWT_BATCHED_FP64 ? kDefaultBlockFP64 : kDefaultBlockFloat;
-        t.big_threshold = wide_rows(m) ? kDefaultBig : kMaxWarpWidth;  // float rows fit 512 per warp
+        // widest warp-task tree: float rows fit 1,024 per warp (K = 32, coefficients in
+        // shared memory), which pays for FP32 rows; mixed rows measured faster with
+        // trees above 512 in warp groups (the autotuner chooses per batch)
+        t.big_threshold = wide_rows(m) ? kDefaultBig : (m == HWT_BATCHED_MIXED ? 512 : kMaxWarpWidth);
         t.warp_k_mask = resolve_k_mask(m, 0, nullptr);
         t.use_graph = 1;
     }
@@ -712,7 +715,7 @@ int hwt_autotune(hwt_ctx *c, const hwt_options *o, const hwt_yield *y, int mode,
     if (o->n == 0) return fail(c, HWT_EINVAL, "autotune needs a non-empty batch");
     std::vector<double> out(o->n);
     const int blocks[] = {64, 128, 256, 512};
-    const int bigs[] = {128, 256, 384, 512};
+    const int bigs[] = {128, 256, 384, 512, 1024};
     // the mode's default K set and a denser one (better fit, larger code footprint)
     const int kmasks[] = {resolve_k_mask(mode, 0, nullptr),
                           resolve_k_mask(mode, mode == HWT_BATCHED_FP64 ? kKMaskFP64Alt

@@ -36,6 +36,7 @@
 #include <float.h>
 #include <stdio.h>
 
+#include <atomic>
 #include <type_traits>
 
 #include "hwt_df64.cuh"
@@ -125,7 +126,7 @@ __device__ __forceinline__ df64 gather3(df64 a, df64 x, df64 b, df64 y, df64 c, 
 __device__ __forceinline__ int cls_K(int cls)
 {
     const int k = cls / kNumL;
-    return k < 8 ? k + 1 : (k == 8 ? 12 : 16);
+    return k < 8 ? k + 1 : (k == 8 ? 12 : (k == 9 ? 16 : 32));
 }
 
 // Named barrier `id` over the `nthreads` threads of one tree's warp group (id 0
@@ -142,17 +143,17 @@ struct Group {
 };
 __device__ __forceinline__ int cls_L(int cls) { return 1 << (cls % kNumL); }
 
-// A warp task's class word: K index q and L index l as q * kNumL + l (bits 0-5),
-// top-edge slot ts (bits 6-9).  Its sort-key slot packs the same triple densely:
+// A warp task's class word: K index q and L index l as q * kNumL + l (bits 0-6),
+// top-edge slot ts (bits 7-11).  Its sort-key slot packs the same triple densely:
 // kNumL * (sum of the K values before K_q) + ts * kNumL + l, so slot % kNumL = l.
 __device__ __forceinline__ int class_slot_base(int q)
 {
-    // kNumL x prefix sums of {1, 2, ..., 8, 12, 16}
-    return kNumL * (q <= 8 ? q * (q + 1) / 2 : 48);
+    // kNumL x prefix sums of {1, 2, ..., 8, 12, 16, 32}
+    return kNumL * (q <= 8 ? q * (q + 1) / 2 : (q == 9 ? 48 : (q == 10 ? 64 : 96)));
 }
 __device__ __forceinline__ int class_slot(int cls)
 {
-    const int q = (cls & 63) / kNumL, l = (cls & 63) % kNumL, ts = (cls >> 6) & 15;
+    const int q = (cls & kClsMask) / kNumL, l = (cls & kClsMask) % kNumL, ts = (cls >> kTsShift) & 31;
     return class_slot_base(q) + ts * kNumL + l;
 }
 __device__ __forceinline__ int slot_class(int slot)
@@ -161,7 +162,7 @@ __device__ __forceinline__ int slot_class(int slot)
 #pragma unroll
     for (int t = 1; t < kNumK; ++t) q += slot >= class_slot_base(t);
     const int rest = slot - class_slot_base(q);
-    return (q * kNumL + rest % kNumL) | ((rest / kNumL) << 6);
+    return (q * kNumL + rest % kNumL) | ((rest / kNumL) << kTsShift);
 }
 
 // Smallest L*K >= width with K in the allowed set (bits of k_mask over
@@ -171,9 +172,12 @@ __device__ __forceinline__ int slot_class(int slot)
 // 1, 2, 4, 8 and 16 by default; double rows (FP64-pipe-bound) use 1 .. 8.
 __host__ __device__ int pick_warp_class(int width, int k_mask)
 {
-    const int ks[kNumK] = {1, 2, 3, 4, 5, 6, 7, 8, 12, 16};  // the K values of kWarpK
+    const int ks[kNumK] = {1, 2, 3, 4, 5, 6, 7, 8, 12, 16, 32};  // the K values of kWarpK
     int best = -1, best_slots = 1 << 30;
-    for (int q = kNumK - 1; q >= 0; --q) {
+    // K = 32 last: it wins only where nothing else fits (coefficients in shared
+    // memory cost more than in registers)
+    for (int i = 0; i < kNumK; ++i) {
+        const int q = i < kNumK - 1 ? kNumK - 2 - i : kNumK - 1;
         const int K = ks[q];
         if (!((k_mask >> q) & 1)) continue;
         for (int l = 0; l < kNumL; ++l) {
@@ -272,11 +276,15 @@ __global__ void size_kernel(EngineParams p)
             if (tier == kWarpTier) {
                 cls = pick_warp_class(s.width, p.warp_k_mask);
                 const int top = s.edges ? (s.width - 1) % cls_K(cls) : 0;  // slot of node W-1
-                cls |= top << 6;
+                cls |= top << kTsShift;
             }
             // group tiers: one tree per task, by work (4 buckets per octave); warp
             // tier: trees of one class in lockstep, by height (8 per octave, <= 9% apart)
-            const int bucket = sort_bucket(p.sort, tier == kWarpTier, s.n, s.width, (long long)s.nodes);
+            // (a K = 32 task costs about twice a K = 16 one of the same height: it is
+            // ordered as one twice as tall, so that it starts early enough)
+            const int hw = (tier == kWarpTier && cls_K(cls) == kWideK) ? 2 * s.n : s.n;
+            const int bucket = sort_bucket(p.sort, tier == kWarpTier, p.sort == 0 || p.sort == '-' ? hw : s.n, s.width,
+                                           (long long)s.nodes);
             if (tier == kWarpTier) key = kWarpTier * kBuckets + bucket * kClassSlots + class_slot(cls);
             else key = tier * kBuckets + bucket;
             p.s.keys[i] = key;
@@ -364,30 +372,33 @@ __global__ void __launch_bounds__(kScanBlock) scan_kernel(EngineParams p)
     __syncthreads();
     if (threadIdx.x == 0) s_last = atomicAdd(&p.s.status->scan_blocks_done, 1) == kScanBlocks - 1;
     __syncthreads();
-    if (!s_last || warp != 0) return;
-    // last block: exclusive scan of the block totals (<= 64, two per lane)
+    if (!s_last) return;
+    // last block: exclusive scan of the block totals, one per thread
     __threadfence();
-    const int *tb = p.s.bin_start + kScanOffsets, *tt = p.s.task_start + kScanOffsets;
-    const int a0 = lane < kScanBlocks ? __ldcg(tb + lane) : 0, a1 = lane + 32 < kScanBlocks ? __ldcg(tb + lane + 32) : 0;
-    const int t0 = lane < kScanBlocks ? __ldcg(tt + lane) : 0, t1 = lane + 32 < kScanBlocks ? __ldcg(tt + lane + 32) : 0;
-    const int ia0 = warp_inclusive_scan(a0, lane), ia1 = warp_inclusive_scan(a1, lane);
-    const int it0 = warp_inclusive_scan(t0, lane), it1 = warp_inclusive_scan(t1, lane);
-    const int sa0 = __shfl_sync(FULL, ia0, 31), st0 = __shfl_sync(FULL, it0, 31);
-    if (lane < kScanBlocks) {
-        p.s.bin_start[kScanOffsets + lane] = ia0 - a0;
-        p.s.task_start[kScanOffsets + lane] = it0 - t0;
+    const int x = threadIdx.x;
+    const int ba = x < kScanBlocks ? __ldcg(p.s.bin_start + kScanOffsets + x) : 0;
+    const int bt = x < kScanBlocks ? __ldcg(p.s.task_start + kScanOffsets + x) : 0;
+    const int ja = warp_inclusive_scan(ba, lane), jt = warp_inclusive_scan(bt, lane);
+    if (lane == 31) { s_a[warp] = ja; s_b[warp] = jt; }
+    __syncthreads();
+    if (warp == 0) {
+        const int a = s_a[lane], y = s_b[lane];
+        const int xa = warp_inclusive_scan(a, lane), xt = warp_inclusive_scan(y, lane);
+        s_a[lane] = xa - a;
+        s_b[lane] = xt - y;
+        if (lane == 31) p.s.status->n_warp_tasks = xt;
     }
-    if (lane + 32 < kScanBlocks) {
-        p.s.bin_start[kScanOffsets + lane + 32] = sa0 + ia1 - a1;
-        p.s.task_start[kScanOffsets + lane + 32] = st0 + it1 - t1;
+    __syncthreads();
+    if (x < kScanBlocks) {
+        p.s.bin_start[kScanOffsets + x] = s_a[warp] + ja - ba;
+        p.s.task_start[kScanOffsets + x] = s_b[warp] + jt - bt;
     }
-    if (lane == 31) p.s.status->n_warp_tasks = st0 + it1;
     // tier boundaries: the group tiers' bins all lie in scan block 0 (offset 0)
     static_assert((kGroupTiers + 1) * kBuckets <= kScanBlock, "tier bins in the first scan block");
-    if (lane < kGroupTiers) {
-        const int a = __ldcg(p.s.bin_start + lane * kBuckets), e = __ldcg(p.s.bin_start + (lane + 1) * kBuckets);
-        p.s.status->tier_start[lane] = a;
-        p.s.status->tier_count[lane] = e - a;
+    if (x < kGroupTiers) {
+        const int a = __ldcg(p.s.bin_start + x * kBuckets), e = __ldcg(p.s.bin_start + (x + 1) * kBuckets);
+        p.s.status->tier_start[x] = a;
+        p.s.status->tier_count[x] = e - a;
     }
 }
 
@@ -447,6 +458,7 @@ struct Nodes<float, K, true> {
     float2 v[H];
     __device__ __forceinline__ float &operator[](int s) { return s < H ? v[s].x : v[s - H].y; }
     __device__ __forceinline__ const float &operator[](int s) const { return s < H ? v[s].x : v[s - H].y; }
+    __device__ __forceinline__ float2 pair(int q) const { return v[q]; }
 };
 
 // One double-float node inside the paired storage (its hi and lo sit in two pairs).
@@ -506,13 +518,62 @@ __device__ __forceinline__ void fma_lane(df64x2 &v, df64 d, df64 s)
     }
 }
 
+// The switch cases on the top edge's slot, 0..31 (cases a slice cannot reach stay
+// empty: see kTopSlot).
+#define HWT_TOP_CASES(X)                                                                          \
+    X(0) X(1) X(2) X(3) X(4) X(5) X(6) X(7) X(8) X(9) X(10) X(11) X(12) X(13) X(14) X(15) X(16) \
+    X(17) X(18) X(19) X(20) X(21) X(22) X(23) X(24) X(25) X(26) X(27) X(28) X(29) X(30) X(31)
+
+// Coefficients of a K = 32 slice in shared memory (three arrays of 32 x 32 floats
+// would not fit in registers beside the row): pair q of a lane at base[q * 32],
+// base offset by the lane, so a warp's access to pair q is 256 contiguous bytes.
+struct SmemPairs {
+    float2 *base;
+    __device__ __forceinline__ float2 &operator[](int q) const { return base[q * 32]; }
+};
+template <int K>
+struct SmemNodes {
+    static constexpr bool kPaired = true;
+    static constexpr int H = K / 2;
+    SmemPairs v;
+    __device__ __forceinline__ float &operator[](int s) const { return s < H ? v[s].x : v[s - H].y; }
+    // A step's read of pair q: a volatile shared load, so the compiler cannot keep
+    // the constant coefficients in registers across the step loop (which is what
+    // their place in shared memory is for)
+    __device__ __forceinline__ float2 pair(int q) const
+    {
+        float2 c;
+        const unsigned a = (unsigned)__cvta_generic_to_shared(v.base + q * 32);
+        asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(c.x), "=f"(c.y) : "r"(a) : "memory");
+        return c;
+    }
+};
+template <typename R, int K>
+struct CoefStore {
+    typedef Nodes<R, K> type;
+};
+template <>
+struct CoefStore<float, kWideK> {
+    typedef SmemNodes<kWideK> type;
+};
+
 template <class Mode, int K>
 struct Slice {
     typedef typename Mode::Row R;
     typedef typename Mode::Scal S;
 
-    Nodes<R, K> r;           // current row, nodes k0 .. k0+K-1
-    Nodes<R, K> c0, c1, c2;  // FP64: fa/fb/fc or ba/bb/bc.  Flux: up, -down of the next node, g.
+    Nodes<R, K> r;                            // current row, nodes k0 .. k0+K-1
+    typename CoefStore<R, K>::type c0, c1, c2;  // FP64: fa/fb/fc or ba/bb/bc.  Flux: up, -down of the next node, g.
+
+    // K = 32: the warp's shared-memory region for the coefficients (kWideWarpFloat2).
+    __device__ __forceinline__ void bind_coefficients(float2 *warp_region, int lane)
+    {
+        if constexpr (K == kWideK && std::is_same<R, float>::value) {
+            c0.v.base = warp_region + lane;
+            c1.v.base = warp_region + (K / 2) * 32 + lane;
+            c2.v.base = warp_region + 2 * (K / 2) * 32 + lane;
+        }
+    }
     R cl, cd0;              // flux: up of node k0-1, -down of node k0
     // Edge jumps (+-jmax branch two nodes away).  Nodes 0 and 2 sit at compile-time
     // slots (0 and 2 % K) and their terms are part of the step loop; node W-1 sits
@@ -677,22 +738,10 @@ struct Slice {
     __device__ __forceinline__ void top_values(const Halo<R> &h, R &w1, R &w3, R &w1b) const
     {
         switch (ts) {
-            case 0: save_top<0>(h, w1, w3, w1b); break;
-            case 1: save_top<1>(h, w1, w3, w1b); break;
-            case 2: save_top<2>(h, w1, w3, w1b); break;
-            case 3: save_top<3>(h, w1, w3, w1b); break;
-            case 4: save_top<4>(h, w1, w3, w1b); break;
-            case 5: save_top<5>(h, w1, w3, w1b); break;
-            case 6: save_top<6>(h, w1, w3, w1b); break;
-            case 7: save_top<7>(h, w1, w3, w1b); break;
-            case 8: save_top<8>(h, w1, w3, w1b); break;
-            case 9: save_top<9>(h, w1, w3, w1b); break;
-            case 10: save_top<10>(h, w1, w3, w1b); break;
-            case 11: save_top<11>(h, w1, w3, w1b); break;
-            case 12: save_top<12>(h, w1, w3, w1b); break;
-            case 13: save_top<13>(h, w1, w3, w1b); break;
-            case 14: save_top<14>(h, w1, w3, w1b); break;
-            case 15: save_top<15>(h, w1, w3, w1b); break;
+#define HWT_SAVE_TOP(T) \
+    case T: save_top<T>(h, w1, w3, w1b); break;
+            HWT_TOP_CASES(HWT_SAVE_TOP)
+#undef HWT_SAVE_TOP
             default: break;
         }
     }
@@ -730,22 +779,10 @@ struct Slice {
     __device__ __forceinline__ void top_fixes(R w1, R w3, R w1b)
     {
         switch (ts) {
-            case 0: top_fix<0, FWD>(w1, w3, w1b); break;
-            case 1: top_fix<1, FWD>(w1, w3, w1b); break;
-            case 2: top_fix<2, FWD>(w1, w3, w1b); break;
-            case 3: top_fix<3, FWD>(w1, w3, w1b); break;
-            case 4: top_fix<4, FWD>(w1, w3, w1b); break;
-            case 5: top_fix<5, FWD>(w1, w3, w1b); break;
-            case 6: top_fix<6, FWD>(w1, w3, w1b); break;
-            case 7: top_fix<7, FWD>(w1, w3, w1b); break;
-            case 8: top_fix<8, FWD>(w1, w3, w1b); break;
-            case 9: top_fix<9, FWD>(w1, w3, w1b); break;
-            case 10: top_fix<10, FWD>(w1, w3, w1b); break;
-            case 11: top_fix<11, FWD>(w1, w3, w1b); break;
-            case 12: top_fix<12, FWD>(w1, w3, w1b); break;
-            case 13: top_fix<13, FWD>(w1, w3, w1b); break;
-            case 14: top_fix<14, FWD>(w1, w3, w1b); break;
-            case 15: top_fix<15, FWD>(w1, w3, w1b); break;
+#define HWT_TOP_FIX(T) \
+    case T: top_fix<T, FWD>(w1, w3, w1b); break;
+            HWT_TOP_CASES(HWT_TOP_FIX)
+#undef HWT_TOP_FIX
             default: break;
         }
     }
@@ -765,9 +802,7 @@ struct Slice {
             save_top<T>(h, w1, w3, w1b);                 \
         }                                                \
         break;
-            HWT_FIX_NEXT(0) HWT_FIX_NEXT(1) HWT_FIX_NEXT(2) HWT_FIX_NEXT(3) HWT_FIX_NEXT(4) HWT_FIX_NEXT(5)
-            HWT_FIX_NEXT(6) HWT_FIX_NEXT(7) HWT_FIX_NEXT(8) HWT_FIX_NEXT(9) HWT_FIX_NEXT(10) HWT_FIX_NEXT(11)
-            HWT_FIX_NEXT(12) HWT_FIX_NEXT(13) HWT_FIX_NEXT(14) HWT_FIX_NEXT(15)
+            HWT_TOP_CASES(HWT_FIX_NEXT)
 #undef HWT_FIX_NEXT
             default: break;
         }
@@ -820,11 +855,11 @@ struct Slice {
             const float2 m1 = make_float2(-1.f, -1.f);
             // pair H-1's right neighbours are node H (pair 0's second) and the halo
             const float2 e_last =
-                __ffma2_rn(c0.v[H - 1], r.v[H - 1], __fmul2_rn(c1.v[H - 1], make_float2(r.v[0].y, h.r1)));
+                __ffma2_rn(c0.pair(H - 1), r.v[H - 1], __fmul2_rn(c1.pair(H - 1), make_float2(r.v[0].y, h.r1)));
             float2 ep = make_float2(fma(cl, h.l1, cd0 * r[0]), e_last.x);  // links k0-1 and k0+H-1
 #pragma unroll
             for (int q = 0; q < H; ++q) {
-                const float2 e = (q == H - 1) ? e_last : __ffma2_rn(c0.v[q], r.v[q], __fmul2_rn(c1.v[q], r.v[q + 1]));
+                const float2 e = (q == H - 1) ? e_last : __ffma2_rn(c0.pair(q), r.v[q], __fmul2_rn(c1.pair(q), r.v[q + 1]));
                 float2 v = __fadd2_rn(r.v[q], __ffma2_rn(e, m1, ep));
                 if (edge_live) {  // a constant in the step loops: no dead fix-ups
                     if (q == 0) v.x = fma(-jout, r.v[0].x, v.x);
@@ -833,7 +868,7 @@ struct Slice {
                         else v.y = fma(jin, src2, v.y);
                     }
                 }
-                r.v[q] = __ffma2_rn(c2.v[q], v, v);
+                r.v[q] = __ffma2_rn(c2.pair(q), v, v);
                 ep = e;
             }
         } else {
@@ -899,10 +934,10 @@ struct Slice {
 #pragma unroll
             for (int q = 0; q < H; ++q) {
                 const float2 d = (q == H - 1) ? d_last : __ffma2_rn(r.v[q], m1, r.v[q + 1]);
-                const float2 nd = (q == 0) ? make_float2(cd0, c1.v[H - 1].x) : c1.v[q - 1];
-                float2 v = __fadd2_rn(r.v[q], __ffma2_rn(c0.v[q], d, __fmul2_rn(nd, dp)));
+                const float2 nd = (q == 0) ? make_float2(cd0, c1.pair(H - 1).x) : c1.pair(q - 1);
+                float2 v = __fadd2_rn(r.v[q], __ffma2_rn(c0.pair(q), d, __fmul2_rn(nd, dp)));
                 if (edge_live && q == 0) v.x = fma(j0, o2 - r.v[0].x, v.x);
-                r.v[q] = __ffma2_rn(c2.v[q], __fadd2_rn(v, b2), v);
+                r.v[q] = __ffma2_rn(c2.pair(q), __fadd2_rn(v, b2), v);
                 dp = d;
             }
         } else {
@@ -959,14 +994,44 @@ struct Slice {
     __device__ __forceinline__ void payoff(S kappa, R base, double X, int type)
     {
         if constexpr (kPairScal<S>) {
-            // the bond value and the strike nearly cancel: the difference is taken
-            // in double-float and rounded to the row's float once
+            // Float rows, double-precision scalars, in few operations (the payoff is
+            // code every task runs once; unrolled over K nodes, a longer form
+            // pushed the step loops of other warps out of the instruction cache):
+            //   s = base + r exactly (FastTwoSum: |r| <= base = 100 before the payoff)
+            //   c = kappa s as kh sh + [exact error of kh sh] + kl sh + kh sl
+            //   X - c = (xh - kh sh) + ((xl - err) - cross)
+            // xh - kh sh is exact where X and c are close (Sterbenz), the only case
+            // where the difference needs the low parts; the omitted kl sl is below
+            // u^2 |c| (4e-13 per 100 face).
             const df64 x(X);
+            if constexpr (Nodes<R, K>::kPaired) {
+                constexpr int H = K / 2;
+                const float2 b2 = make_float2(base, base), kh = make_float2(kappa.hi, kappa.hi),
+                             kl = make_float2(kappa.lo, kappa.lo), xh = make_float2(x.hi, x.hi),
+                             xl = make_float2(x.lo, x.lo);
 #pragma unroll
-            for (int s = 0; s < K; ++s) {
-                const float d = diff_to_float(x, kappa * exact_sum(base, r[s]));
-                const float p = (type == 1) ? d : -d;
-                r[s] = p < 0.f ? 0.f : p;
+                for (int q = 0; q < H; ++q) {
+                    const float2 sh = __fadd2_rn(b2, r.v[q]);
+                    const float2 sl = sub2(r.v[q], sub2(sh, b2));
+                    const float2 ph = __fmul2_rn(kh, sh);
+                    const float2 pl = __ffma2_rn(kh, sh, make_float2(-ph.x, -ph.y));
+                    const float2 cr = __ffma2_rn(kl, sh, __fmul2_rn(kh, sl));
+                    const float2 d = __fadd2_rn(sub2(xh, ph), sub2(sub2(xl, pl), cr));
+                    const float px = (type == 1) ? d.x : -d.x, py = (type == 1) ? d.y : -d.y;
+                    r.v[q] = make_float2(px < 0.f ? 0.f : px, py < 0.f ? 0.f : py);
+                }
+            } else {
+#pragma unroll
+                for (int s = 0; s < K; ++s) {
+                    const float sh = __fadd_rn(base, r[s]);
+                    const float sl = __fsub_rn(r[s], __fsub_rn(sh, base));
+                    const float ph = __fmul_rn(kappa.hi, sh);
+                    const float pl = __fmaf_rn(kappa.hi, sh, -ph);
+                    const float cr = __fmaf_rn(kappa.lo, sh, __fmul_rn(kappa.hi, sl));
+                    const float d = __fadd_rn(__fsub_rn(x.hi, ph), __fsub_rn(__fsub_rn(x.lo, pl), cr));
+                    const float p = (type == 1) ? d : -d;
+                    r[s] = p < 0.f ? 0.f : p;
+                }
             }
         } else {
 #pragma unroll
@@ -1122,13 +1187,13 @@ __device__ __forceinline__ bool pays_at(const Tree &t) { return t.m >= 0 && t.m 
 // Small trees: 32/L trees per warp, L lanes x K nodes each.
 // ---------------------------------------------------------------------------
 template <class Mode, int K>
-__device__ void price_warp_task(const EngineParams &p, const WarpTask &task)
+__device__ void price_warp_task(const EngineParams &p, const WarpTask &task, float2 *wide)
 {
     typedef typename Mode::Row R;
     typedef typename Mode::Scal S;
     constexpr unsigned NONE = 0x7fffffffu;
     const int lane = threadIdx.x & 31;
-    const int L = cls_L(task.cls & 63);
+    const int L = cls_L(task.cls & kClsMask);
     const int g = lane / L, lis = lane & (L - 1);
     const bool valid = g < task.count;
     Tree t;
@@ -1145,8 +1210,9 @@ __device__ void price_warp_task(const EngineParams &p, const WarpTask &task)
     // ---- forward sweep: rows 1 .. n-1; the sums of rows m-1 and n-1 are kept.
     // Rows of trees that are done keep being updated (their segment is isolated by
     // the width-L shuffles), so the step loop carries no per-tree predicates.
+    sl.bind_coefficients(wide, lane);
     sl.setup_forward(t, k0);
-    sl.ts = (task.cls >> 6) & 15;  // the warp's common top-edge slot
+    sl.ts = (task.cls >> kTsShift) & 31;  // the warp's common top-edge slot
     // While the edge jumps are live the second neighbours (l2, r2) are read only
     // when node W-1 sits in slot 0 or 1 (node W-3 in the previous lane) or K < 3;
     // otherwise float rows skip the step's two extra shuffles (double-float rows
@@ -1274,6 +1340,15 @@ __device__ void price_warp_task(const EngineParams &p, const WarpTask &task)
     }
 }
 
+// K = 32 tasks in a function of their own: inlined into the kernel, their code
+// changed the register allocation of the K = 16 path (mixed rows 4% slower even
+// with no K = 32 task in the batch).
+template <class Mode>
+__device__ __noinline__ void price_wide_task(const EngineParams &p, const WarpTask &task, float2 *wide)
+{
+    price_warp_task<Mode, kWideK>(p, task, wide);
+}
+
 // ---------------------------------------------------------------------------
 // Wide trees: one whole block per tree, K nodes per thread.
 // ---------------------------------------------------------------------------
@@ -1399,25 +1474,31 @@ __global__ void __launch_bounds__(kPricingThreads, 1) price_kernel(EngineParams 
     // Warp tier: warp tasks, each warp on its own.
     const int n_tasks = p.s.status->n_warp_tasks;
     const int lane = threadIdx.x & 31;
+    // this warp's coefficient region for K = 32 tasks (float rows: the kernel is
+    // launched with kWideSmemBytes of dynamic shared memory)
+    extern __shared__ float2 wide_coef[];
+    float2 *wide = wide_coef + (threadIdx.x >> 5) * kWideWarpFloat2;
     for (;;) {
         int tsk = 0;
         if (lane == 0) tsk = atomicAdd(&p.s.status->warp_counter, 1);
         tsk = __shfl_sync(FULL, tsk, 0);
         if (tsk >= n_tasks) break;
         const WarpTask wt = p.s.tasks[tsk];
-        switch (cls_K(wt.cls & 63)) {
-            case 1: price_warp_task<Mode, 1>(p, wt); break;
-            case 2: price_warp_task<Mode, 2>(p, wt); break;
-            case 3: price_warp_task<Mode, 3>(p, wt); break;
-            case 4: price_warp_task<Mode, 4>(p, wt); break;
-            case 5: price_warp_task<Mode, 5>(p, wt); break;
-            case 6: price_warp_task<Mode, 6>(p, wt); break;
-            case 7: price_warp_task<Mode, 7>(p, wt); break;
-            case 8: price_warp_task<Mode, 8>(p, wt); break;
+        switch (cls_K(wt.cls & kClsMask)) {
+            case 1: price_warp_task<Mode, 1>(p, wt, wide); break;
+            case 2: price_warp_task<Mode, 2>(p, wt, wide); break;
+            case 3: price_warp_task<Mode, 3>(p, wt, wide); break;
+            case 4: price_warp_task<Mode, 4>(p, wt, wide); break;
+            case 5: price_warp_task<Mode, 5>(p, wt, wide); break;
+            case 6: price_warp_task<Mode, 6>(p, wt, wide); break;
+            case 7: price_warp_task<Mode, 7>(p, wt, wide); break;
+            case 8: price_warp_task<Mode, 8>(p, wt, wide); break;
             default:
                 if constexpr (Mode::kFlux) {
-                    if (cls_K(wt.cls & 63) == 12) price_warp_task<Mode, 12>(p, wt);
-                    else price_warp_task<Mode, 16>(p, wt);
+                    const int k = cls_K(wt.cls & kClsMask);
+                    if (k == 12) price_warp_task<Mode, 12>(p, wt, wide);
+                    else if (k == 16) price_warp_task<Mode, 16>(p, wt, wide);
+                    else price_wide_task<Mode>(p, wt, wide);
                 }
                 break;
         }
@@ -1485,12 +1566,31 @@ cudaError_t launch_pricing(const EngineParams &p, int mode, int grid, cudaStream
 {
     switch (mode) {
         case MODE_BATCHED_FP64: price_kernel<ModeF64><<<grid, kPricingThreads, 0, stream>>>(p); break;
-        case MODE_BATCHED_FP32: price_kernel<ModeF32><<<grid, kPricingThreads, 0, stream>>>(p); break;
-        case MODE_BATCHED_MIXED: price_kernel<ModeMix><<<grid, kPricingThreads, 0, stream>>>(p); break;
+        case MODE_BATCHED_FP32: price_kernel<ModeF32><<<grid, kPricingThreads, kWideSmemBytes, stream>>>(p); break;
+        case MODE_BATCHED_MIXED: price_kernel<ModeMix><<<grid, kPricingThreads, kWideSmemBytes, stream>>>(p); break;
         case MODE_BATCHED_DF64: price_kernel<ModeDF64><<<grid, kPricingThreads, 0, stream>>>(p); break;
         default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
+}
+
+// Float rows' kernels take kWideSmemBytes of dynamic shared memory (K = 32
+// coefficients); the attribute is set once per device, before any launch or
+// occupancy query (every launch path asks for the occupancy first).  Setting it
+// twice from two threads is harmless.
+static bool wide_smem_enabled()
+{
+    static std::atomic<int> done[64];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return false;
+    if (done[dev].load()) return true;
+    const bool ok =
+        cudaFuncSetAttribute(price_kernel<ModeF32>, cudaFuncAttributeMaxDynamicSharedMemorySize, kWideSmemBytes) ==
+            cudaSuccess &&
+        cudaFuncSetAttribute(price_kernel<ModeMix>, cudaFuncAttributeMaxDynamicSharedMemorySize, kWideSmemBytes) ==
+            cudaSuccess;
+    if (ok) done[dev].store(1);
+    return ok;
 }
 
 int pricing_blocks_per_sm(int mode)
@@ -1498,10 +1598,14 @@ int pricing_blocks_per_sm(int mode)
     const int block_threads = kPricingThreads;
     int nb = 0;
     cudaError_t e = cudaErrorInvalidValue;
+    if ((mode == MODE_BATCHED_FP32 || mode == MODE_BATCHED_MIXED) && !wide_smem_enabled()) {
+        cudaGetLastError();
+        return 0;
+    }
     switch (mode) {
         case MODE_BATCHED_FP64: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, price_kernel<ModeF64>, block_threads, 0); break;
-        case MODE_BATCHED_FP32: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, price_kernel<ModeF32>, block_threads, 0); break;
-        case MODE_BATCHED_MIXED: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, price_kernel<ModeMix>, block_threads, 0); break;
+        case MODE_BATCHED_FP32: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, price_kernel<ModeF32>, block_threads, kWideSmemBytes); break;
+        case MODE_BATCHED_MIXED: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, price_kernel<ModeMix>, block_threads, kWideSmemBytes); break;
         case MODE_BATCHED_DF64: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, price_kernel<ModeDF64>, block_threads, 0); break;
         default: break;
     }

@@ -107,16 +107,6 @@ __device__ __forceinline__ df64 operator/(df64 x, df64 y)
     return fast_two_sum(q1, __fdiv_rn(rem, y.hi));
 }
 
-// x - y rounded to float, accurate when the two nearly cancel: the leading parts'
-// difference is taken exactly (TwoSum), so the result is within an ulp of the
-// exact difference plus about 2 u^2 |x|.
-__device__ __forceinline__ float diff_to_float(df64 x, df64 y)
-{
-    float e;
-    const float s = two_sum(x.hi, -y.hi, e);
-    return __fadd_rn(s, __fadd_rn(e, __fsub_rn(x.lo, y.lo)));
-}
-
 // fma for every row type.  Declaring the df64 overload in this namespace hides the
 // global fma from unqualified calls here, so the float and double ones are
 // restated as exact-match overloads that forward to the C functions.

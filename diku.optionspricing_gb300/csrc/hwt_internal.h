@@ -55,18 +55,24 @@ struct WarpTask {
 };
 
 // Warp classes: L lanes per tree (power of two), K nodes per lane; L*K >= width.
-// class = index of K in kWarpK * kNumL + log2(L); FP64 rows stop at K = 8.  A
-// call may restrict the K values used with a mask over kWarpK's indices.
-constexpr int kWarpK[] = {1, 2, 3, 4, 5, 6, 7, 8, 12, 16};
-constexpr int kNumK = 10;
+// class = index of K in kWarpK * kNumL + log2(L); FP64 rows stop at K = 8; K = 32
+// (float rows only, trees of 513..1024 nodes) keeps its coefficients in shared
+// memory.  A call may restrict the K values used with a mask over kWarpK's indices.
+constexpr int kWarpK[] = {1, 2, 3, 4, 5, 6, 7, 8, 12, 16, 32};
+constexpr int kNumK = 11;
 constexpr int kKMaskFP64 = 0xFF;      // default K set of double rows: 1 .. 8
 constexpr int kKMaskFP64Alt = 0xAF;   // autotuner's alternative: 1, 2, 3, 4, 6, 8
-constexpr int kKMaskFloat = 0x28B;    // default K set of float rows: 1, 2, 4, 8, 16
-constexpr int kKMaskFloatAlt = 0x3AF; // autotuner's alternative: 1, 2, 3, 4, 6, 8, 12, 16
-constexpr int kKMaskAll = 0x3FF;
+constexpr int kKMaskFloat = 0x68B;    // default K set of float rows: 1, 2, 4, 8, 16, 32
+constexpr int kKMaskFloatAlt = 0x7AF; // autotuner's alternative: 1, 2, 3, 4, 6, 8, 12, 16, 32
+constexpr int kKMaskAll = 0x7FF;
 constexpr int kNumL = 6;                       // L = 1, 2, 4, 8, 16, 32
 constexpr int kNumWarpClasses = kNumK * kNumL;
-constexpr int kMaxWarpWidth = 32 * 16;         // wider trees go to warp groups or whole blocks
+constexpr int kClsMask = 127;                  // class word: K and L indices in bits 0-6,
+constexpr int kTsShift = 7;                    // the top edge's slot (0..31) from bit 7
+constexpr int kMaxWarpWidth = 32 * 32;         // wider trees go to warp groups or whole blocks
+constexpr int kWideK = 32;                     // warp tasks of this K read coefficients from shared memory
+constexpr int kWideWarpFloat2 = 3 * (kWideK / 2) * 32;  // float2 per warp: up, -down, g pairs
+constexpr int kWideSmemBytes = (512 / 32) * kWideWarpFloat2 * 8;  // 192 KB per 512-thread block
 constexpr int kMaxBlockK = 8;                  // nodes per thread for whole-block trees
 constexpr int kMaxGroupKFloat = 16;            // nodes per thread for warp-group trees, float rows
 constexpr int kPricingThreads = 512;           // threads of every pricing block
@@ -76,20 +82,20 @@ constexpr int kMaxTreeWidth = kMaxBlockK * kPricingThreads;  // widest tree acce
 // the whole block, halves, quarters, eighths): bins [t kBuckets, (t+1) kBuckets),
 // by work.  Warp tier (small trees packed into warp tasks): kWarpTier kBuckets +
 // height bucket * kClassSlots + class slot, one slot per warp class (K, L) and
-// slot ts < K of the top edge node: 6 (L values) x (1+2+...+8+12+16) = 384 slots.
+// slot ts < K of the top edge node: 6 (L values) x (1+2+...+8+12+16+32) = 576 slots.
 // Descending inside a tier.
 constexpr int kGroupTiers = 4;
 constexpr int kWarpTier = kGroupTiers;
 constexpr int kBuckets = 128;
-constexpr int kClassSlots = 384;
+constexpr int kClassSlots = kNumL * 96;
 constexpr int kKeyBinsUsed = kWarpTier * kBuckets + kBuckets * kClassSlots;  // keys are below this
 constexpr int kScanBlock = 1024;  // bins per block of the histogram scan
 constexpr int kScanBlocks = (kKeyBinsUsed + kScanBlock - 1) / kScanBlock;
 // bin_start / task_start hold the starts within each scan block for bins below
 // kScanOffsets and each scan block's offset at kScanOffsets + block
 constexpr int kScanOffsets = kScanBlocks * kScanBlock;
-constexpr int kKeyBins = kScanOffsets + 64;  // counters per array, padded with empty bins
-static_assert(kScanBlocks <= 64 && kKeyBins % 4 == 0 && kClassSlots % kNumL == 0, "bin layout");
+constexpr int kKeyBins = kScanOffsets + (kScanBlocks + 63) / 64 * 64;  // counters per array
+static_assert(kScanBlocks <= kScanBlock && kKeyBins % 4 == 0 && kClassSlots % kNumL == 0, "bin layout");
 
 // Per-run status written by the device (read back after each run).
 struct RunStatus {

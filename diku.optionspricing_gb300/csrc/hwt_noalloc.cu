@@ -131,7 +131,7 @@ extern "C" int hwt_price_device_noalloc(const hwt_options *dev_opts, const hwt_y
     p.warp_k_mask = resolve_k_mask(mode, 0, &p.max_warp_k);
     p.max_group_k = mode == HWT_BATCHED_FP64 ? kMaxBlockK : kMaxGroupKFloat;
     p.sort = 0;
-    p.big_threshold = 32 * p.max_warp_k;
+    p.big_threshold = 32 * (p.max_warp_k < 16 ? p.max_warp_k : 16);  // warp tasks up to 512 nodes
     p.record_busy = 0;
     p.curve_discounts = mode == HWT_BATCHED_MIXED ? 1 : 0;
 

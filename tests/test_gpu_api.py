@@ -255,5 +255,24 @@ def test_warp_k_sets(pkg, pricer, uneven):
         assert_fp64(pricer.price(opts, y, pkg.BATCHED_FP64, warp_k_mask=mask), ref, f"fp64 mask {mask:#x}")
     for mask in (0xFF, 0x01):
         assert_fp64(pricer.price(opts, y, pkg.BATCHED_DF64, warp_k_mask=mask), ref, f"df64 mask {mask:#x}")
-    for mask in (0x3AF, 0x3FF, 0x01, 0x200):
+    for mask in (0x3AF, 0x3FF, 0x01, 0x200, 0x400, 0x7FF):
         assert_lowp(pricer.price(opts, y, pkg.BATCHED_MIXED, warp_k_mask=mask), ref, f"mixed mask {mask:#x}")
+
+
+@pytest.mark.parametrize("mode", ["BATCHED_MIXED", "BATCHED_FP32"])
+def test_wide_warp_tasks(pkg, pricer, uneven, mode):
+    """Trees of 513..1,024 nodes as single-warp tasks of 32 nodes per lane (their
+    coefficients in shared memory) instead of warp groups: no group-tier trees are
+    left in the uneven batch, and the prices stay within 1e-4 of the oracle and
+    within float rounding of the warp-group path."""
+    opts, y, ref = uneven
+    m = getattr(pkg, mode)
+    wide = pricer.price(opts, y, m, big_threshold=1024)
+    assert pricer.last_stats.n_block_trees == 0
+    assert_lowp(wide, ref, f"{mode} K=32")
+    groups = pricer.price(opts, y, m, big_threshold=512)
+    assert pricer.last_stats.n_block_trees > 0
+    assert np.max(np.abs(wide - groups)) < 5e-5
+    # 32 nodes per lane only: every tree up to 1,024 nodes, however narrow, on 32-node lanes
+    only = pricer.price(opts, y, m, big_threshold=1024, warp_k_mask=0x400)
+    assert_lowp(only, ref, f"{mode} K=32 only")
