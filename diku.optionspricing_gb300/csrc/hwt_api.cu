@@ -491,6 +491,7 @@ hwt_ctx *hwt_create(int device, const char *tune_cache)
         // shared memory), which pays for FP32 rows; mixed rows measured faster with
         // trees above 512 in warp groups (the autotuner chooses per batch)
         t.big_threshold = wide_rows(m) ? kDefaultBig : (m == HWT_BATCHED_MIXED ? 512 : kMaxWarpWidth);
+        // (mixed rows: K = 32 is not in their K set, so 512 is their widest warp task)
         t.warp_k_mask = resolve_k_mask(m, 0, nullptr);
         t.use_graph = 1;
     }

@@ -52,24 +52,28 @@ struct ModeF64 {
     typedef double Row;
     typedef double Scal;
     static constexpr bool kSizingDiscounts = false;  // P(n dt), P(m dt) from the sizing pass
+    static constexpr bool kWide = false;  // K = 32 warp tasks (coefficients in shared memory)
     static constexpr bool kFlux = false;
 };
 struct ModeF32 {
     typedef float Row;
     typedef float Scal;
     static constexpr bool kSizingDiscounts = false;  // P(n dt), P(m dt) from the sizing pass
+    static constexpr bool kWide = true;  // K = 32 warp tasks (coefficients in shared memory)
     static constexpr bool kFlux = true;
 };
 struct ModeMix {
     typedef float Row;
     typedef df64 Scal;    // double precision without the FP64 pipe (GB300 issues it at 1/64 of FP32)
     static constexpr bool kSizingDiscounts = true;  // P(n dt), P(m dt) from the sizing pass
+    static constexpr bool kWide = false;  // K = 32 warp tasks (coefficients in shared memory)
     static constexpr bool kFlux = true;
 };
 struct ModeDF64 {
     typedef df64 Row;     // gather form like double rows, arithmetic on the FP32 pipes
     typedef double Scal;
     static constexpr bool kSizingDiscounts = true;  // P(n dt), P(m dt) from the sizing pass
+    static constexpr bool kWide = false;  // K = 32 warp tasks (coefficients in shared memory)
     static constexpr bool kFlux = false;
 };
 
@@ -1497,8 +1501,8 @@ __global__ void __launch_bounds__(kPricingThreads, 1) price_kernel(EngineParams 
                 if constexpr (Mode::kFlux) {
                     const int k = cls_K(wt.cls & kClsMask);
                     if (k == 12) price_warp_task<Mode, 12>(p, wt, wide);
-                    else if (k == 16) price_warp_task<Mode, 16>(p, wt, wide);
-                    else price_wide_task<Mode>(p, wt, wide);
+                    else if (k == 16 || !Mode::kWide) price_warp_task<Mode, 16>(p, wt, wide);
+                    else if constexpr (Mode::kWide) price_wide_task<Mode>(p, wt, wide);
                 }
                 break;
         }
@@ -1518,7 +1522,9 @@ __global__ void __launch_bounds__(kPricingThreads, 1) price_kernel(EngineParams 
 int resolve_k_mask(int mode, int requested, int *max_k)
 {
     const bool dbl = mode == MODE_BATCHED_FP64 || mode == MODE_BATCHED_DF64;  // 64-bit rows: K <= 8
-    const int allowed = dbl ? kKMaskFP64 : kKMaskAll;
+    // K = 32 (coefficients in shared memory) only for FP32 rows: mixed rows measured
+    // no gain from it, and its code cost them instruction-cache hits
+    const int allowed = dbl ? kKMaskFP64 : (mode == MODE_BATCHED_FP32 ? kKMaskAll : kKMaskAll & ~(1 << (kNumK - 1)));
     int m = requested & allowed;
     // defaults: every K for the FP64-pipe-bound double rows; the issue-bound
     // double-float rows, like float rows, do better with fewer K (less code)
@@ -1567,7 +1573,7 @@ cudaError_t launch_pricing(const EngineParams &p, int mode, int grid, cudaStream
     switch (mode) {
         case MODE_BATCHED_FP64: price_kernel<ModeF64><<<grid, kPricingThreads, 0, stream>>>(p); break;
         case MODE_BATCHED_FP32: price_kernel<ModeF32><<<grid, kPricingThreads, kWideSmemBytes, stream>>>(p); break;
-        case MODE_BATCHED_MIXED: price_kernel<ModeMix><<<grid, kPricingThreads, kWideSmemBytes, stream>>>(p); break;
+        case MODE_BATCHED_MIXED: price_kernel<ModeMix><<<grid, kPricingThreads, 0, stream>>>(p); break;
         case MODE_BATCHED_DF64: price_kernel<ModeDF64><<<grid, kPricingThreads, 0, stream>>>(p); break;
         default: return cudaErrorInvalidValue;
     }
@@ -1586,9 +1592,7 @@ static bool wide_smem_enabled()
     if (done[dev].load()) return true;
     const bool ok =
         cudaFuncSetAttribute(price_kernel<ModeF32>, cudaFuncAttributeMaxDynamicSharedMemorySize, kWideSmemBytes) ==
-            cudaSuccess &&
-        cudaFuncSetAttribute(price_kernel<ModeMix>, cudaFuncAttributeMaxDynamicSharedMemorySize, kWideSmemBytes) ==
-            cudaSuccess;
+        cudaSuccess;
     if (ok) done[dev].store(1);
     return ok;
 }
@@ -1598,14 +1602,14 @@ int pricing_blocks_per_sm(int mode)
     const int block_threads = kPricingThreads;
     int nb = 0;
     cudaError_t e = cudaErrorInvalidValue;
-    if ((mode == MODE_BATCHED_FP32 || mode == MODE_BATCHED_MIXED) && !wide_smem_enabled()) {
+    if (mode == MODE_BATCHED_FP32 && !wide_smem_enabled()) {
         cudaGetLastError();
         return 0;
     }
     switch (mode) {
         case MODE_BATCHED_FP64: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, price_kernel<ModeF64>, block_threads, 0); break;
         case MODE_BATCHED_FP32: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, price_kernel<ModeF32>, block_threads, kWideSmemBytes); break;
-        case MODE_BATCHED_MIXED: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, price_kernel<ModeMix>, block_threads, kWideSmemBytes); break;
+        case MODE_BATCHED_MIXED: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, price_kernel<ModeMix>, block_threads, 0); break;
         case MODE_BATCHED_DF64: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, price_kernel<ModeDF64>, block_threads, 0); break;
         default: break;
     }
