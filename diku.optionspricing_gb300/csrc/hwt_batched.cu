@@ -1536,15 +1536,6 @@ int resolve_k_mask(int mode, int requested, int *max_k)
     return m;
 }
 
-int warp_class_of(int width, int *K, int *L)
-{
-    const int c = pick_warp_class(width, kKMaskFloat);
-    if (c < 0) return -1;
-    if (K) *K = kWarpK[c / kNumL];
-    if (L) *L = 1 << (c % kNumL);
-    return c;
-}
-
 int sizing_launches() { return 4; }
 
 cudaError_t launch_sizing(const EngineParams &p, cudaStream_t stream)

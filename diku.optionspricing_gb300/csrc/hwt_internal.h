@@ -66,7 +66,6 @@ constexpr int kKMaskFloat = 0x68B;    // default K set of float rows: 1, 2, 4, 8
 constexpr int kKMaskFloatAlt = 0x7AF; // autotuner's alternative: 1, 2, 3, 4, 6, 8, 12, 16, 32
 constexpr int kKMaskAll = 0x7FF;
 constexpr int kNumL = 6;                       // L = 1, 2, 4, 8, 16, 32
-constexpr int kNumWarpClasses = kNumK * kNumL;
 constexpr int kClsMask = 127;                  // class word: K and L indices in bits 0-6,
 constexpr int kTsShift = 7;                    // the top edge's slot (0..31) from bit 7
 constexpr int kMaxWarpWidth = 32 * 32;         // wider trees go to warp groups or whole blocks
@@ -151,7 +150,6 @@ cudaError_t launch_pricing(const EngineParams &p, int mode, int grid, cudaStream
 int pricing_blocks_per_sm(int mode);
 cudaError_t launch_plain(const EngineParams &p, int max_width, int max_height, cudaStream_t stream);
 size_t plain_smem_bytes(int max_width, int max_height);
-int warp_class_of(int width, int *K, int *L);
 int sizing_launches();
 
 }  // namespace hwt
