@@ -1563,7 +1563,11 @@ cudaError_t launch_pricing(const EngineParams &p, int mode, int grid, cudaStream
 {
     switch (mode) {
         case MODE_BATCHED_FP64: price_kernel<ModeF64><<<grid, kPricingThreads, 0, stream>>>(p); break;
-        case MODE_BATCHED_FP32: price_kernel<ModeF32><<<grid, kPricingThreads, kWideSmemBytes, stream>>>(p); break;
+        case MODE_BATCHED_FP32:
+            // the K = 32 coefficient space only when trees above 512 nodes may be warp
+            // tasks (otherwise the L1 keeps that shared-memory carve-out)
+            price_kernel<ModeF32><<<grid, kPricingThreads, p.big_threshold > 512 ? kWideSmemBytes : 0, stream>>>(p);
+            break;
         case MODE_BATCHED_MIXED: price_kernel<ModeMix><<<grid, kPricingThreads, 0, stream>>>(p); break;
         case MODE_BATCHED_DF64: price_kernel<ModeDF64><<<grid, kPricingThreads, 0, stream>>>(p); break;
         default: return cudaErrorInvalidValue;
