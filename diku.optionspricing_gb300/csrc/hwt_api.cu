@@ -335,7 +335,7 @@ int run_batch(hwt_ctx *c, const DevOptions &dopt, double *dev_out, const hwt_con
     p.s.status = c->d_status;
     p.out = dev_out;
     p.group_threads = cfg.block_size;
-    p.warp_k_mask = resolve_k_mask(cfg.mode, cfg.warp_k_mask, &p.max_warp_k);
+    p.warp_k_mask = run_k_mask(cfg.mode, cfg.warp_k_mask, cfg.big_threshold, &p.max_warp_k);
     p.max_group_k = wide_rows(cfg.mode) ? kMaxBlockK : kMaxGroupKFloat;
     p.sort = cfg.sort;
     p.big_threshold = std::min(cfg.big_threshold, 32 * p.max_warp_k);
@@ -420,6 +420,7 @@ int finish(hwt_ctx *c, const hwt_config &cfg, hwt_stats *stats, int launches, in
         stats->busy_max_ms = mx * 1e-6;
         stats->busy_mean_ms = sum / grid_hint * 1e-6;
     }
+    if (st.wide_smem_missing) return fail(c, HWT_ECUDA, "internal: a 32-node-per-lane task met a launch without its shared memory");
     if (st.bad_count > 0) return fail(c, HWT_EINVAL, bad_option_message(st));
     return HWT_OK;
 }
@@ -488,10 +489,8 @@ hwt_ctx *hwt_create(int device, const char *tune_cache)
         t.mode = m;
         t.block_size = m == HWT_BATCHED_FP64 ? kDefaultBlockFP64 : kDefaultBlockFloat;
         // widest warp-task tree: float rows fit 1,024 per warp (K = 32, coefficients in
-        // shared memory), which pays for FP32 rows; mixed rows measured faster with
-        // trees above 512 in warp groups (the autotuner chooses per batch)
-        t.big_threshold = wide_rows(m) ? kDefaultBig : (m == HWT_BATCHED_MIXED ? 512 : kMaxWarpWidth);
-        // (mixed rows: K = 32 is not in their K set, so 512 is their widest warp task)
+        // shared memory); the autotuner chooses per batch
+        t.big_threshold = wide_rows(m) ? kDefaultBig : kMaxWarpWidth;
         t.warp_k_mask = resolve_k_mask(m, 0, nullptr);
         t.use_graph = 1;
     }

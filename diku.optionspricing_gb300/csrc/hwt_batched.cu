@@ -53,6 +53,7 @@ struct ModeF64 {
     typedef double Scal;
     static constexpr bool kSizingDiscounts = false;  // P(n dt), P(m dt) from the sizing pass
     static constexpr bool kWide = false;  // K = 32 warp tasks (coefficients in shared memory)
+    static constexpr bool kScratchPayoff = false;
     static constexpr bool kFlux = false;
 };
 struct ModeF32 {
@@ -60,13 +61,15 @@ struct ModeF32 {
     typedef float Scal;
     static constexpr bool kSizingDiscounts = false;  // P(n dt), P(m dt) from the sizing pass
     static constexpr bool kWide = true;  // K = 32 warp tasks (coefficients in shared memory)
+    static constexpr bool kScratchPayoff = false;
     static constexpr bool kFlux = true;
 };
 struct ModeMix {
     typedef float Row;
     typedef df64 Scal;    // double precision without the FP64 pipe (GB300 issues it at 1/64 of FP32)
     static constexpr bool kSizingDiscounts = true;  // P(n dt), P(m dt) from the sizing pass
-    static constexpr bool kWide = false;  // K = 32 warp tasks (coefficients in shared memory)
+    static constexpr bool kWide = true;  // K = 32 warp tasks (coefficients in shared memory)
+    static constexpr bool kScratchPayoff = true;  // payoff through shared-memory scratch
     static constexpr bool kFlux = true;
 };
 struct ModeDF64 {
@@ -74,6 +77,7 @@ struct ModeDF64 {
     typedef double Scal;
     static constexpr bool kSizingDiscounts = true;  // P(n dt), P(m dt) from the sizing pass
     static constexpr bool kWide = false;  // K = 32 warp tasks (coefficients in shared memory)
+    static constexpr bool kScratchPayoff = false;
     static constexpr bool kFlux = false;
 };
 
@@ -520,6 +524,26 @@ __device__ __forceinline__ void fma_lane(df64x2 &v, df64 d, df64 s)
         v.hi.y = t.hi;
         v.lo.y = t.lo;
     }
+}
+
+// One float-row node's payoff, kappa (base + r) against the strike x, in double
+// precision with float operations:
+//   s = base + r exactly (FastTwoSum: |r| <= base = 100 before the payoff)
+//   c = kappa s as kh sh + [exact error of kh sh] + kl sh + kh sl
+//   x - c = (xh - kh sh) + ((xl - err) - cross)
+// xh - kh sh is exact where x and c are close (Sterbenz), the only case where the
+// difference needs the low parts; the omitted kl sl is below u^2 |c| (4e-13 per
+// 100 face).
+__device__ __forceinline__ float payoff_value(float r, float base, df64 kappa, df64 x, int type)
+{
+    const float sh = __fadd_rn(base, r);
+    const float sl = __fsub_rn(r, __fsub_rn(sh, base));
+    const float ph = __fmul_rn(kappa.hi, sh);
+    const float pl = __fmaf_rn(kappa.hi, sh, -ph);
+    const float cr = __fmaf_rn(kappa.lo, sh, __fmul_rn(kappa.hi, sl));
+    const float d = __fadd_rn(__fsub_rn(x.hi, ph), __fsub_rn(__fsub_rn(x.lo, pl), cr));
+    const float p = (type == 1) ? d : -d;
+    return p < 0.f ? 0.f : p;
 }
 
 // The switch cases on the top edge's slot, 0..31 (cases a slice cannot reach stay
@@ -998,44 +1022,23 @@ struct Slice {
     __device__ __forceinline__ void payoff(S kappa, R base, double X, int type)
     {
         if constexpr (kPairScal<S>) {
-            // Float rows, double-precision scalars, in few operations (the payoff is
-            // code every task runs once; unrolled over K nodes, a longer form
-            // pushed the step loops of other warps out of the instruction cache):
-            //   s = base + r exactly (FastTwoSum: |r| <= base = 100 before the payoff)
-            //   c = kappa s as kh sh + [exact error of kh sh] + kl sh + kh sl
-            //   X - c = (xh - kh sh) + ((xl - err) - cross)
-            // xh - kh sh is exact where X and c are close (Sterbenz), the only case
-            // where the difference needs the low parts; the omitted kl sl is below
-            // u^2 |c| (4e-13 per 100 face).
+            // Through the thread's shared-memory scratch (16 floats, stride 32): the
+            // row out, one rolled loop over the nodes, the row back; the code is that
+            // of one node whatever K (unrolled over K, the per-node arithmetic cost
+            // the step loops of other warps their instruction-cache lines: mixed rows
+            // ran 3-12% slower than float rows beside K = 32 tasks)
+            extern __shared__ float payoff_scratch[];
+            float *scr = payoff_scratch + (threadIdx.x >> 5) * (32 * kPayoffScratch) + (threadIdx.x & 31);
             const df64 x(X);
-            if constexpr (Nodes<R, K>::kPaired) {
-                constexpr int H = K / 2;
-                const float2 b2 = make_float2(base, base), kh = make_float2(kappa.hi, kappa.hi),
-                             kl = make_float2(kappa.lo, kappa.lo), xh = make_float2(x.hi, x.hi),
-                             xl = make_float2(x.lo, x.lo);
+            constexpr int HALF = K < kPayoffScratch ? K : kPayoffScratch;
 #pragma unroll
-                for (int q = 0; q < H; ++q) {
-                    const float2 sh = __fadd2_rn(b2, r.v[q]);
-                    const float2 sl = sub2(r.v[q], sub2(sh, b2));
-                    const float2 ph = __fmul2_rn(kh, sh);
-                    const float2 pl = __ffma2_rn(kh, sh, make_float2(-ph.x, -ph.y));
-                    const float2 cr = __ffma2_rn(kl, sh, __fmul2_rn(kh, sl));
-                    const float2 d = __fadd2_rn(sub2(xh, ph), sub2(sub2(xl, pl), cr));
-                    const float px = (type == 1) ? d.x : -d.x, py = (type == 1) ? d.y : -d.y;
-                    r.v[q] = make_float2(px < 0.f ? 0.f : px, py < 0.f ? 0.f : py);
-                }
-            } else {
+            for (int h0 = 0; h0 < K; h0 += HALF) {
 #pragma unroll
-                for (int s = 0; s < K; ++s) {
-                    const float sh = __fadd_rn(base, r[s]);
-                    const float sl = __fsub_rn(r[s], __fsub_rn(sh, base));
-                    const float ph = __fmul_rn(kappa.hi, sh);
-                    const float pl = __fmaf_rn(kappa.hi, sh, -ph);
-                    const float cr = __fmaf_rn(kappa.lo, sh, __fmul_rn(kappa.hi, sl));
-                    const float d = __fadd_rn(__fsub_rn(x.hi, ph), __fsub_rn(__fsub_rn(x.lo, pl), cr));
-                    const float p = (type == 1) ? d : -d;
-                    r[s] = p < 0.f ? 0.f : p;
-                }
+                for (int s = 0; s < HALF; ++s) scr[s * 32] = r[h0 + s];
+#pragma unroll 1
+                for (int s = 0; s < HALF; ++s) scr[s * 32] = payoff_value(scr[s * 32], base, kappa, x, type);
+#pragma unroll
+                for (int s = 0; s < HALF; ++s) r[h0 + s] = scr[s * 32];
             }
         } else {
 #pragma unroll
@@ -1481,7 +1484,12 @@ __global__ void __launch_bounds__(kPricingThreads, 1) price_kernel(EngineParams 
     // this warp's coefficient region for K = 32 tasks (float rows: the kernel is
     // launched with kWideSmemBytes of dynamic shared memory)
     extern __shared__ float2 wide_coef[];
-    float2 *wide = wide_coef + (threadIdx.x >> 5) * kWideWarpFloat2;
+    float2 *wide = wide_coef + (Mode::kScratchPayoff ? kScratchSmemBytes / 8 : 0) + (threadIdx.x >> 5) * kWideWarpFloat2;
+    // a K = 32 task runs only if this launch has its coefficient space (a task in a
+    // launch without it is skipped and reported, never run out of bounds)
+    unsigned dyn_bytes;
+    asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(dyn_bytes));
+    const bool wide_ok = dyn_bytes >= (unsigned)((Mode::kScratchPayoff ? kScratchSmemBytes : 0) + kWideSmemBytes);
     for (;;) {
         int tsk = 0;
         if (lane == 0) tsk = atomicAdd(&p.s.status->warp_counter, 1);
@@ -1502,7 +1510,10 @@ __global__ void __launch_bounds__(kPricingThreads, 1) price_kernel(EngineParams 
                     const int k = cls_K(wt.cls & kClsMask);
                     if (k == 12) price_warp_task<Mode, 12>(p, wt, wide);
                     else if (k == 16 || !Mode::kWide) price_warp_task<Mode, 16>(p, wt, wide);
-                    else if constexpr (Mode::kWide) price_wide_task<Mode>(p, wt, wide);
+                    else if constexpr (Mode::kWide) {
+                        if (wide_ok) price_wide_task<Mode>(p, wt, wide);
+                        else if (lane == 0) atomicExch(&p.s.status->wide_smem_missing, 1);
+                    }
                 }
                 break;
         }
@@ -1522,9 +1533,7 @@ __global__ void __launch_bounds__(kPricingThreads, 1) price_kernel(EngineParams 
 int resolve_k_mask(int mode, int requested, int *max_k)
 {
     const bool dbl = mode == MODE_BATCHED_FP64 || mode == MODE_BATCHED_DF64;  // 64-bit rows: K <= 8
-    // K = 32 (coefficients in shared memory) only for FP32 rows: mixed rows measured
-    // no gain from it, and its code cost them instruction-cache hits
-    const int allowed = dbl ? kKMaskFP64 : (mode == MODE_BATCHED_FP32 ? kKMaskAll : kKMaskAll & ~(1 << (kNumK - 1)));
+    const int allowed = dbl ? kKMaskFP64 : kKMaskAll;
     int m = requested & allowed;
     // defaults: every K for the FP64-pipe-bound double rows; the issue-bound
     // double-float rows, like float rows, do better with fewer K (less code)
@@ -1534,6 +1543,28 @@ int resolve_k_mask(int mode, int requested, int *max_k)
         if ((m >> q) & 1) mk = kWarpK[q];
     if (max_k) *max_k = mk;
     return m;
+}
+
+int run_k_mask(int mode, int requested, int big_threshold, int *max_k)
+{
+    int m = resolve_k_mask(mode, requested, max_k);
+    const int k32 = 1 << (kNumK - 1);
+    if ((m & k32) && (m & ~k32) && big_threshold <= 512) {
+        m &= ~k32;
+        int mk = 1;
+        for (int q = 0; q < kNumK; ++q)
+            if ((m >> q) & 1) mk = kWarpK[q];
+        if (max_k) *max_k = mk;
+    }
+    return m;
+}
+
+int pricing_smem_bytes(int mode, int k_mask)
+{
+    const bool wide = (k_mask >> (kNumK - 1)) & 1;
+    if (mode == MODE_BATCHED_FP32) return wide ? kWideSmemBytes : 0;
+    if (mode == MODE_BATCHED_MIXED) return kScratchSmemBytes + (wide ? kWideSmemBytes : 0);
+    return 0;
 }
 
 int sizing_launches() { return 4; }
@@ -1564,11 +1595,13 @@ cudaError_t launch_pricing(const EngineParams &p, int mode, int grid, cudaStream
     switch (mode) {
         case MODE_BATCHED_FP64: price_kernel<ModeF64><<<grid, kPricingThreads, 0, stream>>>(p); break;
         case MODE_BATCHED_FP32:
-            // the K = 32 coefficient space only when trees above 512 nodes may be warp
-            // tasks (otherwise the L1 keeps that shared-memory carve-out)
-            price_kernel<ModeF32><<<grid, kPricingThreads, p.big_threshold > 512 ? kWideSmemBytes : 0, stream>>>(p);
+            // the K = 32 coefficient space only when the run's K mask allows K = 32
+            // (otherwise the L1 keeps that shared-memory carve-out)
+            price_kernel<ModeF32><<<grid, kPricingThreads, pricing_smem_bytes(mode, p.warp_k_mask), stream>>>(p);
             break;
-        case MODE_BATCHED_MIXED: price_kernel<ModeMix><<<grid, kPricingThreads, 0, stream>>>(p); break;
+        case MODE_BATCHED_MIXED:
+            price_kernel<ModeMix><<<grid, kPricingThreads, pricing_smem_bytes(mode, p.warp_k_mask), stream>>>(p);
+            break;
         case MODE_BATCHED_DF64: price_kernel<ModeDF64><<<grid, kPricingThreads, 0, stream>>>(p); break;
         default: return cudaErrorInvalidValue;
     }
@@ -1587,7 +1620,9 @@ static bool wide_smem_enabled()
     if (done[dev].load()) return true;
     const bool ok =
         cudaFuncSetAttribute(price_kernel<ModeF32>, cudaFuncAttributeMaxDynamicSharedMemorySize, kWideSmemBytes) ==
-        cudaSuccess;
+            cudaSuccess &&
+        cudaFuncSetAttribute(price_kernel<ModeMix>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             kScratchSmemBytes + kWideSmemBytes) == cudaSuccess;
     if (ok) done[dev].store(1);
     return ok;
 }
@@ -1597,14 +1632,17 @@ int pricing_blocks_per_sm(int mode)
     const int block_threads = kPricingThreads;
     int nb = 0;
     cudaError_t e = cudaErrorInvalidValue;
-    if (mode == MODE_BATCHED_FP32 && !wide_smem_enabled()) {
+    if ((mode == MODE_BATCHED_FP32 || mode == MODE_BATCHED_MIXED) && !wide_smem_enabled()) {
         cudaGetLastError();
         return 0;
     }
     switch (mode) {
         case MODE_BATCHED_FP64: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, price_kernel<ModeF64>, block_threads, 0); break;
         case MODE_BATCHED_FP32: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, price_kernel<ModeF32>, block_threads, kWideSmemBytes); break;
-        case MODE_BATCHED_MIXED: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, price_kernel<ModeMix>, block_threads, 0); break;
+        case MODE_BATCHED_MIXED:
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, price_kernel<ModeMix>, block_threads,
+                                                              kScratchSmemBytes + kWideSmemBytes);
+            break;
         case MODE_BATCHED_DF64: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, price_kernel<ModeDF64>, block_threads, 0); break;
         default: break;
     }

@@ -72,6 +72,10 @@ constexpr int kMaxWarpWidth = 32 * 32;         // wider trees go to warp groups 
 constexpr int kWideK = 32;                     // warp tasks of this K read coefficients from shared memory
 constexpr int kWideWarpFloat2 = 3 * (kWideK / 2) * 32;  // float2 per warp: up, -down, g pairs
 constexpr int kWideSmemBytes = (512 / 32) * kWideWarpFloat2 * 8;  // 192 KB per 512-thread block
+// Mixed rows compute the payoff in a rolled loop through 16 floats of shared-memory
+// scratch per thread (32 KB per block), ahead of the K = 32 coefficients.
+constexpr int kPayoffScratch = 16;
+constexpr int kScratchSmemBytes = 512 * kPayoffScratch * 4;
 constexpr int kMaxBlockK = 8;                  // nodes per thread for whole-block trees
 constexpr int kMaxGroupKFloat = 16;            // nodes per thread for warp-group trees, float rows
 constexpr int kPricingThreads = 512;           // threads of every pricing block
@@ -109,6 +113,7 @@ struct RunStatus {
     int32_t max_width;            // widest / tallest valid tree
     int32_t max_height;
     int32_t scan_blocks_done;     // histogram scan blocks finished (the last one adds the offsets)
+    int32_t wide_smem_missing;    // a K = 32 task met a launch without its shared memory (skipped)
 };
 
 struct Scratch {
@@ -143,6 +148,12 @@ struct EngineParams {
 // Resolves a requested K mask for `mode` (0 = the mode's default) and the largest
 // K it allows.
 int resolve_k_mask(int mode, int requested, int *max_k);
+// The K mask a run uses: the resolved one without K = 32 when the widest warp-task
+// tree is at most 512 nodes and another K is allowed (K = 32 then has no tree to
+// take, and the launch needs no coefficient space in shared memory).
+int run_k_mask(int mode, int requested, int big_threshold, int *max_k);
+// Dynamic shared memory a pricing launch of `mode` with this K mask needs.
+int pricing_smem_bytes(int mode, int k_mask);
 
 // Launchers (hwt_batched.cu / hwt_plain.cu).  All enqueue on `stream`; none syncs.
 cudaError_t launch_sizing(const EngineParams &p, cudaStream_t stream);

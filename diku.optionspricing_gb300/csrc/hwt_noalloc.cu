@@ -128,7 +128,7 @@ extern "C" int hwt_price_device_noalloc(const hwt_options *dev_opts, const hwt_y
     p.out = dev_out_prices;
     p.max_width = kMaxTreeWidth;
     p.group_threads = mode == HWT_BATCHED_FP64 ? 128 : 64;
-    p.warp_k_mask = resolve_k_mask(mode, 0, &p.max_warp_k);
+    p.warp_k_mask = run_k_mask(mode, 0, 512, &p.max_warp_k);
     p.max_group_k = mode == HWT_BATCHED_FP64 ? kMaxBlockK : kMaxGroupKFloat;
     p.sort = 0;
     p.big_threshold = 32 * (p.max_warp_k < 16 ? p.max_warp_k : 16);  // warp tasks up to 512 nodes
@@ -150,5 +150,6 @@ extern "C" int hwt_price_device_noalloc(const hwt_options *dev_opts, const hwt_y
     if ((e = cudaMemcpyAsync(&status, p.s.status, sizeof(RunStatus), cudaMemcpyDeviceToHost, st)) != cudaSuccess)
         return fail_cuda(e);
     if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return fail_cuda(e);
+    if (status.wide_smem_missing) return HWT_ECUDA;
     return status.bad_count > 0 ? HWT_EINVAL : HWT_OK;
 }

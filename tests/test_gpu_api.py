@@ -257,19 +257,19 @@ def test_warp_k_sets(pkg, pricer, uneven):
         assert_fp64(pricer.price(opts, y, pkg.BATCHED_DF64, warp_k_mask=mask), ref, f"df64 mask {mask:#x}")
     for mask in (0x3AF, 0x3FF, 0x01, 0x200, 0x400, 0x7FF):
         assert_lowp(pricer.price(opts, y, pkg.BATCHED_MIXED, warp_k_mask=mask), ref, f"mixed mask {mask:#x}")
+    # K = 32 alone at a 512-node threshold: every warp task takes 32 nodes per lane,
+    # and the launch must carry their shared-memory coefficients
+    for mode in (pkg.BATCHED_FP32, pkg.BATCHED_MIXED):
+        assert_lowp(pricer.price(opts, y, mode, warp_k_mask=0x400, big_threshold=512), ref, f"{mode} K=32 only")
 
 
-def test_wide_warp_tasks(pkg, pricer, uneven):
-    """FP32 rows: trees of 513..1,024 nodes as single-warp tasks of 32 nodes per lane
+@pytest.mark.parametrize("mode", ["BATCHED_MIXED", "BATCHED_FP32"])
+def test_wide_warp_tasks(pkg, pricer, uneven, mode):
+    """Float rows: trees of 513..1,024 nodes as single-warp tasks of 32 nodes per lane
     (their coefficients in shared memory) instead of warp groups: no group-tier trees
     are left in the uneven batch, and the prices stay within 1e-4 of the oracle and
-    within float rounding of the warp-group path.  Mixed rows do not take K = 32:
-    their wide trees stay in warp groups whatever the threshold."""
+    within float rounding of the warp-group path."""
     opts, y, ref = uneven
-    mode = "BATCHED_FP32"
-    mixed = pricer.price(opts, y, pkg.BATCHED_MIXED, big_threshold=1024, warp_k_mask=0x7FF)
-    assert pricer.last_stats.n_block_trees > 0
-    assert_lowp(mixed, ref, "mixed, K = 32 requested")
     m = getattr(pkg, mode)
     wide = pricer.price(opts, y, m, big_threshold=1024)
     assert pricer.last_stats.n_block_trees == 0
