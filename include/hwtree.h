@@ -97,13 +97,14 @@ typedef struct hwt_config {
                               that holds it at 8 (FP64 rows) or 16 (float rows) nodes per thread */
     int32_t sort;          /* HWT_SORT_* schedule order (0 = HWT_SORT_NONE) */
     int32_t big_threshold; /* widths above this leave warp tasks for warp groups (<= 256 for
-                              FP64 rows, <= 512 for float rows) */
+                              double rows, <= 1024 for float rows; 0 = the default) */
     int32_t use_graph;     /* 1 = replay a captured CUDA graph (default), 0 = direct launches */
     int32_t record_busy;   /* 1 = record per-block busy time for the tail-imbalance stat */
     int32_t warp_k_mask;   /* nodes-per-lane values warp tasks may use: bit q allows the q-th of
-                              {1, 2, 3, 4, 5, 6, 7, 8, 12, 16}; 12 and 16 apply to float rows
-                              only; 0 = the mode's default (FP64: 1..8; double-float: 1, 2, 3, 4, 6, 8;
-                              float rows: 1, 2, 4, 8, 16) */
+                              {1, 2, 3, 4, 5, 6, 7, 8, 12, 16, 32}; 12, 16 and 32 apply to float
+                              rows only (32: trees of up to 1,024 nodes on one warp, coefficients
+                              in shared memory); 0 = the mode's default (FP64: 1..8; double-float:
+                              1, 2, 3, 4, 6, 8; float rows: 1, 2, 4, 8, 16, 32) */
 } hwt_config;
 
 /* Run statistics, filled when a non-NULL pointer is passed.  Times are CUDA-event
