@@ -739,7 +739,10 @@ int hwt_autotune(hwt_ctx *c, const hwt_options *o, const hwt_yield *y, int mode,
                 if (k > 0) t = std::min(t, st.sizing_ms + st.pricing_ms);
             }
             if (r == HWT_EUNSUPPORTED) continue;
-            if (t < best_ms) { best_ms = t; best_cfg = cfg; }
+            // a later (larger) configuration has to win by more than 1%: where the
+            // sizes tie (a batch without warp-group trees makes the group size moot)
+            // the smaller groups, better for other batches, are kept
+            if (t < 0.99 * best_ms || best_ms == 1e300) { best_ms = t; best_cfg = cfg; }
           }
         }
     }
