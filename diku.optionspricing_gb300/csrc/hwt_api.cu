@@ -420,7 +420,7 @@ int finish(hwt_ctx *c, const hwt_config &cfg, hwt_stats *stats, int launches, in
         stats->busy_max_ms = mx * 1e-6;
         stats->busy_mean_ms = sum / grid_hint * 1e-6;
     }
-    if (st.wide_smem_missing) return fail(c, HWT_ECUDA, "internal: a 32-node-per-lane task met a launch without its shared memory");
+    if (st.wide_smem_missing) return fail(c, HWT_ECUDA, "internal: a pricing launch lacked the shared memory its work needs");
     if (st.bad_count > 0) return fail(c, HWT_EINVAL, bad_option_message(st));
     return HWT_OK;
 }

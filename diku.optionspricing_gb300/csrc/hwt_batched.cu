@@ -1452,6 +1452,17 @@ __global__ void __launch_bounds__(kPricingThreads, 1) price_kernel(EngineParams 
     __shared__ int sh_task[16];  // one per group of every group tier
     unsigned long long t_start = 0;
     if (p.record_busy && threadIdx.x == 0) asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t_start));
+    // dynamic shared memory of this launch: mixed rows need their payoff scratch
+    // (a launch without it does no work and is reported), K = 32 tasks their
+    // coefficients (checked per task below)
+    unsigned dyn_bytes;
+    asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(dyn_bytes));
+    if constexpr (Mode::kScratchPayoff) {
+        if (dyn_bytes < (unsigned)kScratchSmemBytes) {
+            if (threadIdx.x == 0) atomicExch(&p.s.status->wide_smem_missing, 1);
+            return;
+        }
+    }
 
     // Group tiers, heaviest first: tier t prices one tree per group of 512 >> t
     // threads.  Group g of tier t uses named barrier and task slot 2^t - 1 + g
@@ -1487,8 +1498,6 @@ __global__ void __launch_bounds__(kPricingThreads, 1) price_kernel(EngineParams 
     float2 *wide = wide_coef + (Mode::kScratchPayoff ? kScratchSmemBytes / 8 : 0) + (threadIdx.x >> 5) * kWideWarpFloat2;
     // a K = 32 task runs only if this launch has its coefficient space (a task in a
     // launch without it is skipped and reported, never run out of bounds)
-    unsigned dyn_bytes;
-    asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(dyn_bytes));
     const bool wide_ok = dyn_bytes >= (unsigned)((Mode::kScratchPayoff ? kScratchSmemBytes : 0) + kWideSmemBytes);
     for (;;) {
         int tsk = 0;

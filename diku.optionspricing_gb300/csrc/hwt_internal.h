@@ -113,7 +113,7 @@ struct RunStatus {
     int32_t max_width;            // widest / tallest valid tree
     int32_t max_height;
     int32_t scan_blocks_done;     // histogram scan blocks finished (the last one adds the offsets)
-    int32_t wide_smem_missing;    // a K = 32 task met a launch without its shared memory (skipped)
+    int32_t wide_smem_missing;    // a launch lacked the shared memory its work needs (work skipped)
 };
 
 struct Scratch {
