@@ -4,7 +4,8 @@
  * A plain-C restatement of the reference's CPU pricer for the batch pricing path
  * (seq/Seq.hpp:24-190 with common/OptionConstants.hpp:29-53 and
  * common/Domain.hpp:11-169).  Only tests/, the smoke check and bench.py's CPU
- * baseline load it, always as the checker or the timed CPU reference; the GPU
+ * baseline load it, always to check results against or as the timed CPU
+ * reference; the GPU
  * product never calls it and has no CPU fallback.
  *
  * Pinned against the reference's own golden vectors (data/out/*.out for the

@@ -3,7 +3,8 @@
 ctypes wrapper over liboracle.so, the plain-C restatement of the reference's CPU
 pricer (oracle/hwt_seq.c: seq/Seq.hpp:24-190, common/OptionConstants.hpp:29-53,
 common/Domain.hpp:11-169).  Used only by tests/, __graft_entry__.smoke() and
-bench.py's CPU baseline, always as the checker or the timed CPU reference.
+bench.py's CPU baseline, always to check results against or as the timed CPU
+reference.
 """
 from __future__ import annotations
 

@@ -15,7 +15,7 @@ REF_SETS = ["book", "options-1000", "0_UNIFORM_1000", "1_RAND_1000", "2_RANDCONS
                 "5_SKEWEDCONSTHEIGHT", "6_SKEWEDCONSTWIDTH")]
 SYN_SETS = ["uniform_1k", "uneven_2k", "skewed_512", "book_100", "edge"]
 
-# Parity bars (the benchmark spec's tolerances, written here once):
+# Parity bars (the required tolerances, written here once):
 #   FP64 paths: |p - p_ref| <= 1e-10 * |p_ref| + 1e-12   (relative 1e-10; the
 #               absolute floor covers prices that are zero up to rounding)
 #   FP32 / mixed paths: |p - p_ref| <= 1e-4 (absolute, per 100 face)
