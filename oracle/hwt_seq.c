@@ -5,8 +5,7 @@
  * (seq/Seq.hpp:24-190 with common/OptionConstants.hpp:29-53 and
  * common/Domain.hpp:11-169).  Only tests/, the smoke check and bench.py's CPU
  * baseline load it, always to check results against or as the timed CPU
- * reference; the GPU
- * product never calls it and has no CPU fallback.
+ * reference; the GPU product never calls it and has no CPU fallback.
  *
  * Pinned against the reference's own golden vectors (data/out/*.out for the
  * double build, data/out32/*.out for the float build, copied under tests/golden/)
