@@ -118,6 +118,8 @@ _SIGNATURES = {
     "hwt_shape": (ctypes.c_int, [ctypes.POINTER(_Options), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                  ctypes.c_void_p]),
     "hwt_active_nodes": (ctypes.c_int64, [ctypes.c_int32, ctypes.c_int32]),
+    "hwt_warp_layout": (ctypes.c_int, [ctypes.c_int, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                       ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]),
     "hwt_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(_Options), ctypes.POINTER(_Yield), ctypes.c_int,
                                     ctypes.c_int, ctypes.POINTER(Config)]),
     "hwt_get_config": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(Config)]),
@@ -356,6 +358,16 @@ def shape(options: Options) -> dict:
                          out["width"].ctypes.data, out["maturity_step"].ctypes.data)
     out["status"] = rc
     return out
+
+
+def warp_layout(mode: int, width: int, warp_k_mask: int = 0, big_threshold: int = 0) -> tuple[int, int]:
+    """(nodes per lane, lanes) of the warp task the batched engine gives a tree of
+    `width` nodes, or (0, 0) when the tree goes to a warp group (host only)."""
+    k, l = ctypes.c_int32(), ctypes.c_int32()
+    rc = lib().hwt_warp_layout(mode, width, warp_k_mask, big_threshold, ctypes.byref(k), ctypes.byref(l))
+    if rc != HWT_OK:
+        raise InvalidInput(rc, f"no warp layout for mode {mode}, width {width}")
+    return k.value, l.value
 
 
 def active_nodes(height, jmax) -> np.ndarray:

@@ -698,6 +698,24 @@ int hwt_shape(const hwt_options *o, int32_t *jmax, int32_t *height, int32_t *wid
 
 int64_t hwt_active_nodes(int32_t height, int32_t jmax) { return active_nodes(height, jmax); }
 
+int hwt_warp_layout(int mode, int32_t width, int32_t warp_k_mask, int32_t big_threshold, int32_t *K, int32_t *L)
+{
+    if (mode < HWT_BATCHED_FP64 || mode >= kNumModes || width < 1 || width > kMaxTreeWidth || !K || !L)
+        return HWT_EINVAL;
+    const int big = big_threshold > 0 ? big_threshold : (wide_rows(mode) ? kDefaultBig : kMaxWarpWidth);
+    int max_k = 1;
+    const int mask = run_k_mask(mode, warp_k_mask, big, &max_k);
+    *K = 0;
+    *L = 0;
+    // the sizing kernel's split: warp tasks up to min(threshold, 32 x largest K)
+    if (width > std::min(big, 32 * max_k)) return HWT_OK;
+    int k = 0, l = 0;
+    if (warp_layout(width, mask, &k, &l)) return HWT_OK;
+    *K = k;
+    *L = l;
+    return HWT_OK;
+}
+
 int hwt_get_config(const hwt_ctx *c, int mode, hwt_config *cfg)
 {
     if (!c || !cfg || mode < 0 || mode >= kNumModes) return HWT_EINVAL;

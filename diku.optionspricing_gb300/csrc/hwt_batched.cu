@@ -1568,6 +1568,15 @@ int run_k_mask(int mode, int requested, int big_threshold, int *max_k)
     return m;
 }
 
+int warp_layout(int width, int k_mask, int *K, int *L)
+{
+    const int c = pick_warp_class(width, k_mask);
+    if (c < 0) return -1;
+    *K = kWarpK[c / kNumL];
+    *L = 1 << (c % kNumL);
+    return 0;
+}
+
 int pricing_smem_bytes(int mode, int k_mask)
 {
     const bool wide = (k_mask >> (kNumK - 1)) & 1;

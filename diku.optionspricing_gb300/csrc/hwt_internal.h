@@ -152,6 +152,9 @@ int resolve_k_mask(int mode, int requested, int *max_k);
 // tree is at most 512 nodes and another K is allowed (K = 32 then has no tree to
 // take, and the launch needs no coefficient space in shared memory).
 int run_k_mask(int mode, int requested, int big_threshold, int *max_k);
+// Warp-task layout of a tree of `width` nodes under K mask `k_mask`: nodes per lane
+// and lanes (the sizing kernel's choice); -1 if no allowed K fits.
+int warp_layout(int width, int k_mask, int *K, int *L);
 // Dynamic shared memory a pricing launch of `mode` with this K mask needs.
 int pricing_smem_bytes(int mode, int k_mask);
 

@@ -194,6 +194,14 @@ int hwt_shape(const hwt_options *opts, int32_t *jmax, int32_t *height, int32_t *
  * the work unit of the roofline accounting. */
 int64_t hwt_active_nodes(int32_t height, int32_t jmax);
 
+/* How the batched engine lays out a tree `width` nodes wide for `mode` (a batched
+ * mode) with this K mask and widest-warp-task threshold (0 = the defaults, as a
+ * context without tuning uses them): *K nodes per lane on *L lanes of a warp task,
+ * or *K = *L = 0 when the tree goes to a warp group.  Host only, no GPU.
+ * HWT_EINVAL for a non-batched mode or a width outside 1..4096. */
+int hwt_warp_layout(int mode, int32_t width, int32_t warp_k_mask, int32_t big_threshold, int32_t *K,
+                    int32_t *L);
+
 /* Autotuner: prices the batch with each candidate configuration (block size,
  * block-tree threshold), keeps the fastest for `mode` in the context, writes it
  * to the context's tune cache (if any) and returns it in *best. */

@@ -4,6 +4,7 @@ import os
 import re
 
 import numpy as np
+import pytest
 
 from conftest import ROOT, REF_SETS, SYN_SETS, load_set
 
@@ -58,3 +59,29 @@ def test_shape_rejects_bad_records(pkg):
 
 def test_null_context_is_einval(pkg):
     assert pkg.lib().hwt_price(None, None, None, 1, None, None) == pkg.HWT_EINVAL
+
+
+def test_warp_layout_policy(pkg):
+    """How trees are laid out (the sizing kernel's choice, queried on the host):
+    the smallest K x L covering the width with ties to the larger K, K = 32 (shared
+    memory coefficients) only where no smaller K fits, the widest warp task set by
+    the threshold and the K set."""
+    lay = pkg.warp_layout
+    for mode in (pkg.BATCHED_MIXED, pkg.BATCHED_FP32):
+        assert lay(mode, 5) == (8, 1)
+        assert lay(mode, 100) == (16, 8)
+        assert lay(mode, 140) == (16, 16)
+        assert lay(mode, 512) == (16, 32)
+        assert lay(mode, 513) == (32, 32)      # default threshold 1,024: one warp
+        assert lay(mode, 1025) == (0, 0)       # warp groups
+        assert lay(mode, 600, big_threshold=512) == (0, 0)
+        assert lay(mode, 13, warp_k_mask=0x400, big_threshold=512) == (32, 1)  # K = 32 alone
+        assert lay(mode, 600, warp_k_mask=0x400, big_threshold=512) == (0, 0)
+    assert lay(pkg.BATCHED_FP64, 200) == (7, 32)   # double rows: every K in 1..8, 224 slots
+    assert lay(pkg.BATCHED_FP64, 13) == (7, 2)
+    assert lay(pkg.BATCHED_FP64, 257) == (0, 0)    # threshold 256
+    assert lay(pkg.BATCHED_FP64, 200, warp_k_mask=0x7FF) == (7, 32)  # no K above 8 for double rows
+    assert lay(pkg.BATCHED_DF64, 200) == (8, 32)   # {1, 2, 3, 4, 6, 8}
+    for bad in ((pkg.PLAIN_FP64, 10), (pkg.BATCHED_MIXED, 0), (pkg.BATCHED_MIXED, 5000)):
+        with pytest.raises(pkg.InvalidInput):
+            lay(*bad)
