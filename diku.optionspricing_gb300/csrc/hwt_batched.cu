@@ -174,10 +174,10 @@ __device__ __forceinline__ int slot_class(int slot)
 }
 
 // Smallest L*K >= width with K in the allowed set (bits of k_mask over
-// {1, 2, ..., 8, 12, 16}), L in {1..32}; ties go to the larger K (more trees per
+// {1, 2, ..., 8, 12, 16, 32}), L in {1..32}; ties go to the larger K (more trees per
 // warp, fewer shuffles per node).  Each K used adds its code to the working set
 // of the instruction cache, so float rows (whose warps are issue-bound) use only
-// 1, 2, 4, 8 and 16 by default; double rows (FP64-pipe-bound) use 1 .. 8.
+// 1, 2, 4, 8, 16 and 32 by default; double rows (FP64-pipe-bound) use 1 .. 8.
 __host__ __device__ int pick_warp_class(int width, int k_mask)
 {
     const int ks[kNumK] = {1, 2, 3, 4, 5, 6, 7, 8, 12, 16, 32};  // the K values of kWarpK

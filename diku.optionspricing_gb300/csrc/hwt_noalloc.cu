@@ -12,17 +12,20 @@
 //
 // The array is a __device__ variable: every GPU that loads the library holds it
 // (about 5 MB) until the process exits.  In host code its name is only a
-// host-side stand-in, so its device address is looked up once per device with
-// cudaGetSymbolAddress, on the first call made with that device current; make
-// that first call before any stream capture.  All calls share the array and it
-// keeps the last call's contents (the counters that must start at zero are
-// cleared by every call), so calls that overlap on the GPU - from two streams or
-// two host threads at once - race and must be serialised by the caller.
+// host-side stand-in, so every call looks up its device address with
+// cudaGetSymbolAddress, in the CUDA context current at the call (the caller's
+// device current), and passes that address to the kernels.  An address is valid
+// only in the context it was looked up in, so none is kept between calls: a
+// context created after cudaDeviceReset, or a non-primary context made current
+// by the caller, gets its own.  The first lookup in a context also loads the
+// library's device code there, so make the first call in a context before any
+// stream capture.  All calls share the array and it keeps the last call's
+// contents (the counters that must start at zero are cleared by every call), so
+// calls that overlap on the GPU - from two streams or two host threads at once -
+// race and must be serialised by the caller.
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string.h>
-
-#include <mutex>
 
 #include "../../include/hwtree.h"
 #include "hwt_internal.h"
@@ -47,18 +50,19 @@ constexpr size_t kOffBinStart = up(kOffHist + 2ull * 4 * kKeyBins);
 constexpr size_t kOffTaskStart = up(kOffBinStart + 4ull * kKeyBins);
 constexpr size_t kOffStatus = up(kOffTaskStart + 4ull * kKeyBins);
 constexpr size_t kOffRateF = up(kOffStatus + sizeof(RunStatus));
-constexpr size_t kScratchBytes = up(kOffRateF + 4ull * kNoAllocMaxYield);
+constexpr size_t kOffCurveBad = up(kOffRateF + 4ull * kNoAllocMaxYield);  // non-finite curve rates seen
+constexpr size_t kScratchBytes = up(kOffCurveBad + 4);
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_setup_mutex;
-void *g_scratch_addr[kMaxDevices] = {};
-
-__global__ void curve_to_float(const double *rate, int n, float *rate_f)
+// Float copy of the curve; *bad is raised for a rate that is not finite.
+__global__ void curve_to_float(const double *rate, int n, float *rate_f, int *bad)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) rate_f[i] = (float)rate[i];
+    if (i >= n) return;
+    const double r = rate[i];
+    if (!isfinite(r)) atomicExch(bad, 1);
+    rate_f[i] = (float)r;
 }
 
 int fail_cuda(cudaError_t e)
@@ -85,20 +89,11 @@ extern "C" int hwt_price_device_noalloc(const hwt_options *dev_opts, const hwt_y
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return fail_cuda(e);
-    if (dev < 0 || dev >= kMaxDevices) return HWT_EUNSUPPORTED;
-    unsigned char *base;
-    {
-        // set-up, once per device, with that device current
-        std::lock_guard<std::mutex> lock(g_setup_mutex);
-        if (!g_scratch_addr[dev]) {
-            void *ptr = nullptr;
-            e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
-            if (e != cudaSuccess) return fail_cuda(e);
-            g_scratch_addr[dev] = ptr;
-        }
-        base = (unsigned char *)g_scratch_addr[dev];
-    }
     cudaStream_t st = (cudaStream_t)stream;
+    // set-up: the array's device address in the current context
+    void *scratch = nullptr;
+    if ((e = cudaGetSymbolAddress(&scratch, g_noalloc_scratch)) != cudaSuccess) return fail_cuda(e);
+    unsigned char *base = (unsigned char *)scratch;
 
     EngineParams p;
     memset(&p, 0, sizeof(p));
@@ -141,15 +136,22 @@ extern "C" int hwt_price_device_noalloc(const hwt_options *dev_opts, const hwt_y
     const int per = pricing_blocks_per_sm(mode);
     if (per < 1) return HWT_EUNSUPPORTED;
 
-    curve_to_float<<<(dev_yield->n + 255) / 256, 256, 0, st>>>(dev_yield->rate, dev_yield->n, (float *)(base + kOffRateF));
+    int *curve_bad = (int *)(base + kOffCurveBad);
+    if ((e = cudaMemsetAsync(curve_bad, 0, sizeof(int), st)) != cudaSuccess) return fail_cuda(e);
+    curve_to_float<<<(dev_yield->n + 255) / 256, 256, 0, st>>>(dev_yield->rate, dev_yield->n, (float *)(base + kOffRateF),
+                                                               curve_bad);
     if ((e = cudaGetLastError()) != cudaSuccess) return fail_cuda(e);
     // launch_sizing clears the histogram, fill counters and run status itself
     if ((e = launch_sizing(p, st)) != cudaSuccess) return fail_cuda(e);
     if ((e = launch_pricing(p, mode, per * sms, st)) != cudaSuccess) return fail_cuda(e);
     RunStatus status;
+    int bad_curve = 0;
     if ((e = cudaMemcpyAsync(&status, p.s.status, sizeof(RunStatus), cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+        return fail_cuda(e);
+    if ((e = cudaMemcpyAsync(&bad_curve, curve_bad, sizeof(int), cudaMemcpyDeviceToHost, st)) != cudaSuccess)
         return fail_cuda(e);
     if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return fail_cuda(e);
     if (status.wide_smem_missing) return HWT_ECUDA;
+    if (bad_curve) return HWT_EINVAL;  // a curve rate is not finite: every price is suspect
     return status.bad_count > 0 ? HWT_EINVAL : HWT_OK;
 }

@@ -48,7 +48,8 @@ extern "C" {
 #define HWT_BATCHED_FP32 2   /* binned persistent engine, float throughout */
 #define HWT_BATCHED_MIXED 3  /* float rows; alpha-fit sums, scales, payoff, discount in double precision */
 #define HWT_BATCHED_DF64 4   /* double-float rows (hi + lo floats, ~48 bits) on the FP32 pipes,
-                                double sums, scales, payoff, discount; within 1e-10 relative of FP64 */
+                                double sums, scales, payoff, discount; within 1e-10 relative + 1e-12
+                                absolute of FP64 (the absolute floor matters only at prices near 0) */
 
 /* Sort orders of the reference's -s flag (common/Options.hpp:15-22).  They set the
  * order in which the engine schedules trees inside each of its tiers (whole-block
@@ -172,13 +173,19 @@ int hwt_price_device(hwt_ctx *ctx, const hwt_options *dev_opts, const hwt_yield 
  * synchronise the device, are not allowed): no context, no allocation of any
  * kind; the scratch the pricing kernels need lives in a static device array of
  * the library (about 5 MB on every GPU that loads it, until exit).
- *   dev_opts, dev_yield, dev_out_prices: DEVICE pointers of the current device
+ *   dev_opts, dev_yield: HOST structs whose array members are DEVICE pointers of
+ *     the current device (n is read on the host); dev_out_prices: device pointer
  *   mode: HWT_BATCHED_FP64, HWT_BATCHED_FP32 or HWT_BATCHED_MIXED
  *   stream: cudaStream_t to run on (NULL: the default stream); the call waits for it
- * At most 32768 options and 1024 curve nodes per call, else HWT_EINVAL.  The
- * first call on a device looks up the array's device address (make it before
- * any stream capture).  Calls share the array: calls that overlap on the GPU
- * race.  Returns HWT_EINVAL if an option is invalid (its price is NaN). */
+ * At most 32768 options and 1024 curve nodes per call, else HWT_EINVAL.  Every
+ * call looks up the array's device address in the CUDA context current at the
+ * call (none is kept, so a context re-created after cudaDeviceReset is safe);
+ * the first lookup in a context loads the library's device code, so make the
+ * first call in a context before any stream capture.  Calls share the array:
+ * calls that overlap on the GPU race.  Returns HWT_EINVAL if an option is
+ * invalid (its price is NaN) or a curve rate is not finite.  Warp-task layout:
+ * hwt_warp_layout(mode, width, 0, 512, ...) for the float modes and
+ * (mode, width, 0, 256, ...) for HWT_BATCHED_FP64 describe this entry point. */
 int hwt_price_device_noalloc(const hwt_options *dev_opts, const hwt_yield *dev_yield, int mode,
                              double *dev_out_prices, void *stream);
 
@@ -196,7 +203,8 @@ int64_t hwt_active_nodes(int32_t height, int32_t jmax);
 
 /* How the batched engine lays out a tree `width` nodes wide for `mode` (a batched
  * mode) with this K mask and widest-warp-task threshold (0 = the defaults, as a
- * context without tuning uses them): *K nodes per lane on *L lanes of a warp task,
+ * context without tuning uses them; hwt_price_device_noalloc uses threshold 512
+ * for the float modes and 256 for FP64): *K nodes per lane on *L lanes of a warp task,
  * or *K = *L = 0 when the tree goes to a warp group.  Host only, no GPU.
  * HWT_EINVAL for a non-batched mode or a width outside 1..4096. */
 int hwt_warp_layout(int mode, int32_t width, int32_t warp_k_mask, int32_t big_threshold, int32_t *K,

@@ -23,7 +23,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
-REF = "/root/reference"
+REF = os.environ.get("HWT_REFERENCE", "/root/reference")
 sys.path.insert(0, ROOT)
 
 import __graft_entry__ as g  # noqa: E402

@@ -29,7 +29,7 @@ def _c_options(pkg, dev, n):
     return pkg._Options(n, *(dev[k].data_ptr() for k in FIELDS))
 
 
-@pytest.mark.parametrize("mode_name", ["BATCHED_FP64", "BATCHED_MIXED"])
+@pytest.mark.parametrize("mode_name", ["BATCHED_FP64", "BATCHED_FP32", "BATCHED_MIXED"])
 def test_noalloc_matches_allocating_entry_point(pkg, mode_name):
     import torch
     mode = getattr(pkg, mode_name)
@@ -82,3 +82,19 @@ def test_noalloc_rejects_oversized_batch(pkg):
                                             pkg.BATCHED_FP64, out.data_ptr(), None)
     assert rc == pkg.HWT_OK
     assert np.all(np.isfinite(out[:32768].cpu().numpy()))
+
+
+def test_noalloc_rejects_non_finite_curve(pkg):
+    """A curve rate that is not finite makes every price suspect: HWT_EINVAL."""
+    import torch
+    opts, y, _, _ = load_set(pkg, "book")
+    dev = _device_inputs(pkg, opts)
+    rates = y.Prices.copy()
+    rates[len(rates) // 2] = np.nan
+    rate = torch.from_numpy(rates).cuda()
+    day = torch.from_numpy(y.TimeSteps).cuda()
+    out = torch.empty(opts.N, dtype=torch.float64, device="cuda")
+    c_yield = pkg._Yield(y.N, rate.data_ptr(), day.data_ptr())
+    rc = pkg.lib().hwt_price_device_noalloc(ctypes.byref(_c_options(pkg, dev, opts.N)), ctypes.byref(c_yield),
+                                            pkg.BATCHED_MIXED, out.data_ptr(), None)
+    assert rc == pkg.HWT_EINVAL
