@@ -93,6 +93,32 @@ def shard_lpt(work: np.ndarray, world: int) -> list[np.ndarray]:
     return [np.array(sorted(p), dtype=np.int64) for p in parts]
 
 
+def shard_parts(pkg, opts, world: int) -> list[np.ndarray]:
+    """The LPT split of a batch by its tree work (host shapes, no GPU)."""
+    shp = pkg.shape(opts)
+    work = FLOP_PER_NODE * pkg.active_nodes(shp["height"], shp["jmax"]).astype(np.float64)
+    return shard_lpt(work, world)
+
+
+def gather_prices(local, parts, dist, device=None):
+    """Every rank's shard prices (`local`: this rank's, in the order of its part)
+    into one float64 tensor in input order, on every rank: an all-gather of the
+    shards padded to the widest one, then a scatter by the parts' indices.  The
+    only exchange of the sharded path (options are independent)."""
+    import torch
+    world = len(parts)
+    n = int(sum(len(p) for p in parts))
+    width = max(len(p) for p in parts)
+    buf = torch.zeros(width, dtype=torch.float64, device=device)
+    buf[:local.numel()] = local
+    outs = [torch.empty_like(buf) for _ in range(world)]
+    dist.all_gather(outs, buf)
+    full = torch.empty(n, dtype=torch.float64, device=device)
+    for r, p in enumerate(parts):
+        full[torch.from_numpy(p).to(device)] = outs[r][:len(p)]
+    return full
+
+
 class ClockSampler:
     """Samples SM clocks and throttle reasons with nvidia-smi while running."""
     QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -197,10 +223,12 @@ def cpu_reference(args, rank, world):
         "impl": "reference", "metric": METRIC, "value": value, "unit": "options/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": per * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded numpy)",
-        "config": {"workload": args.workload, "options": n_total, "sample_options": sample,
-                   "implementation": "oracle/hwt_seq.c: C restatement of the reference seq/ pricer, OpenMP over options"},
+        "config": {"workload": args.workload, "options": n_total},
+        "implementation": "oracle/hwt_seq.c: C restatement of the reference seq/ pricer (pinned to the reference's "
+                          "own seq/ build and goldens), OpenMP over options",
         "cpu_baseline": {"value": value, "unit": "options/s", "cores": threads, "kind": "port",
-                         "sample": f"first {sample} options of {args.workload}, {args.steps} timed passes",
+                         "sample": f"first {sample} of the {n_total} options of {args.workload} per step, "
+                                   f"{args.steps} timed steps",
                          "single_thread": one},
         "e2e": {"value": value, "unit": "options/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -381,6 +409,32 @@ def run_ours(args, rank, world, local):
             e["x_batched_fp64"] = e["options_per_s"] / fp64_rate
             e["x_plain_fp64"] = e["options_per_s"] / plain_rate
 
+    # ---- sharded N > 1: each rank prices its LPT part of the batch, then the prices
+    # are all-gathered (the step's only exchange); the whole job is one batch
+    parts = shard_parts(pkg, opts, world) if (args.shard and world > 1) else None
+    if parts is not None:
+        mine = parts[rank]
+        sub = opts.subset(mine)
+        sub_dev = {k: torch.from_numpy(np.ascontiguousarray(v[mine])).to(dev) for k, v in fields.items()}
+        sub_ptr = {k: t.data_ptr() for k, t in sub_dev.items()}
+        sub_out = torch.empty(len(mine), dtype=torch.float64, device=dev)
+        sub_host = {k: torch.from_numpy(np.ascontiguousarray(v[mine])).pin_memory() for k, v in fields.items()}
+        sub_host_ptr = {k: t.data_ptr() for k, t in sub_host.items()}
+        sub_host_out = torch.empty(len(mine), dtype=torch.float64).pin_memory()
+        full_host = torch.empty(n, dtype=torch.float64).pin_memory()
+
+        def shard_step():
+            st_ = pricer.price_device(sub_ptr, len(mine), y, sub_out.data_ptr(), mode)
+            gather_prices(sub_out, parts, dist, dev)
+            torch.cuda.synchronize(dev)
+            return st_
+
+        def shard_step_host():
+            pricer.price_host_ptrs(sub_host_ptr, len(mine), y, sub_host_out.data_ptr(), mode)
+            full = gather_prices(sub_host_out.to(dev, non_blocking=True), parts, dist, dev)
+            full_host.copy_(full)
+            torch.cuda.synchronize(dev)
+
     # ---- timed region: K device-resident steps of the headline mode
     if dist is not None:
         dist.barrier()
@@ -391,18 +445,40 @@ def run_ours(args, rank, world, local):
     if nvtx is not None:
         nvtx.range_push("timed")
     with ClockSampler(local) as clk:
-        times, launches, st = device_steps(mode, args.steps, args.warmup)
+        if parts is None:
+            times, launches, st = device_steps(mode, args.steps, args.warmup)
+        else:
+            # host clock around price + all-gather (the pricer's call waits for its
+            # stream, the gather is synchronised), L2 flushed between steps
+            for _ in range(args.warmup):
+                shard_step()
+            times, launches, kernel = [], 0, []
+            for _ in range(args.steps):
+                flush_l2()
+                t0 = time.perf_counter()
+                st_ = shard_step()
+                times.append(1e3 * (time.perf_counter() - t0))
+                kernel.append(st_.pricing_ms)
+                launches += st_.kernel_launches
+            st = pkg.Stats.from_buffer_copy(st_)
+            st.pricing_ms = sum(kernel) / len(kernel)
         torch.cuda.synchronize(dev)
         if dist is not None:
             dist.barrier()
         # e2e through the public host-memory API (pinned buffers), host clock
         for _ in range(args.warmup):
-            pricer.price_host_ptrs(host_ptr, n, y, host_out.data_ptr(), mode)
+            if parts is None:
+                pricer.price_host_ptrs(host_ptr, n, y, host_out.data_ptr(), mode)
+            else:
+                shard_step_host()
         e2e_t = []
         for _ in range(args.steps):
             flush_l2()
             t0 = time.perf_counter()
-            pricer.price_host_ptrs(host_ptr, n, y, host_out.data_ptr(), mode)
+            if parts is None:
+                pricer.price_host_ptrs(host_ptr, n, y, host_out.data_ptr(), mode)
+            else:
+                shard_step_host()
             e2e_t.append(time.perf_counter() - t0)
     if nvtx is not None:
         nvtx.range_pop()
@@ -410,6 +486,8 @@ def run_ours(args, rank, world, local):
     ms = max_over_ranks(ms, dist, dev)
     e2e_ms = max_over_ranks(1e3 * sum(e2e_t) / len(e2e_t), dist, dev)
     pricing_ms = st.pricing_ms
+    # options the whole job prices per step: replicas price the batch once per rank
+    job_options = n if parts is not None else world * n
 
     peaks = pricer.measure_peaks()
     measured = load_json(os.path.join(ROOT, "MEASURED_PEAKS.json")) or {}
@@ -423,26 +501,30 @@ def run_ours(args, rank, world, local):
     if rank == 0:
         line = {
             "metric": METRIC,
-            "value": world * n / (ms * 1e-3),
+            "value": job_options / (ms * 1e-3),
             "unit": "options/s",
             "n_gpus": world,
             "steps": args.steps,
             "warmup": args.warmup,
             "ms_per_step": ms,
             "higher_is_better": True,
-            "scaling": "weak",
+            "scaling": "strong" if parts is not None else "weak",
             "vs_baseline": None,
             "dtype": {"mixed": "f32+f64", "fp32": "f32", "fp64": "f64", "df64": "f32x2+f64", "plain": "f64"}[args.mode],
             "data": "synthetic (seeded numpy; no public data set exists for this workload)",
-            "config": {"workload": args.workload, "options": n, "mode": pkg.MODE_NAMES[mode],
-                       "active_nodes_per_pass": nodes, "parallelism": "replicas" if world > 1 else "single",
+            "config": {"workload": args.workload, "options": n},
+            "engine": {"mode": pkg.MODE_NAMES[mode], "active_nodes_per_pass": nodes,
+                       "parallelism": ("lpt shards + all-gather" if parts is not None else "replicas")
+                       if world > 1 else "single",
                        "l2": "flushed between steps (256 MB memset), inputs 1.35 MB",
                        "block_size": st.block_size, "grid": st.grid,
                        "tuned": tuned.get(pkg.MODE_NAMES[mode], "library defaults")},
             "clocks": clk.summary(),
             "gpu_launches": launches,
-            "e2e": {"value": world * n / (e2e_ms * 1e-3), "unit": "options/s", "h2d_bytes_per_step": h2d_bytes,
-                    "d2h_bytes_per_step": 8 * n},
+            "e2e": {"value": job_options / (e2e_ms * 1e-3), "unit": "options/s",
+                    "h2d_bytes_per_step": h2d_bytes if parts is None else
+                    int(sum(t.numel() * t.element_size() for t in sub_host.values())) + 8 * len(mine),
+                    "d2h_bytes_per_step": 8 * n if parts is None else 8 * len(mine) + 8 * n},
             "roofline": {"bound": bound, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": achieved / peak, "traffic": traffic,
                          "work": f"{FLOP_PER_NODE} FLOP x {nodes} active nodes per launch; peak = FMA microbenchmark "
@@ -486,9 +568,18 @@ def main():
     ap.add_argument("--no-datasets", action="store_true", help="skip the seven thesis benchmark distributions")
     ap.add_argument("--sur-samples", type=int, default=4_000_000)
     ap.add_argument("--sur-epochs", type=int, default=24)
+    ap.add_argument("--shard", action="store_true",
+                    help="N>1: split the batch across ranks by tree work (LPT) and gather the prices, instead of "
+                         "one replica of the whole batch per GPU")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_env()
+    if args.gpus != world:
+        # one process per GPU: N > 1 runs under torchrun, which sets WORLD_SIZE
+        print(json.dumps({"error": f"--gpus {args.gpus} but WORLD_SIZE={world}: run N > 1 as "
+                                   f"python -m torch.distributed.run --nproc-per-node {args.gpus} "
+                                   f"--master-addr 127.0.0.1 bench.py --gpus {args.gpus} ..."}))
+        return 2
     if args.impl == "reference":
         return cpu_reference(args, rank, world)
     return run_ours(args, rank, world, local)

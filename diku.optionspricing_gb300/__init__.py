@@ -526,13 +526,17 @@ class Box(ctypes.Structure):
 
 class TrainConfig(ctypes.Structure):
     _fields_ = [("epochs", ctypes.c_int32), ("batch", ctypes.c_int32), ("lr", ctypes.c_double),
-                ("lr_min", ctypes.c_double), ("seed", ctypes.c_uint64)]
+                ("lr_min", ctypes.c_double), ("seed", ctypes.c_uint64), ("err_weight", ctypes.c_double),
+                ("route_tolerance", ctypes.c_double), ("holdout", ctypes.c_double)]
 
 
 class TrainStats(ctypes.Structure):
     _fields_ = [("final_loss", ctypes.c_double), ("train_ms", ctypes.c_double), ("label_ms", ctypes.c_double),
                 ("steps", ctypes.c_int64), ("samples", ctypes.c_int64), ("samples_per_s", ctypes.c_double),
-                ("y_mean", ctypes.c_double), ("y_std", ctypes.c_double)]
+                ("y_mean", ctypes.c_double), ("y_std", ctypes.c_double), ("route_threshold", ctypes.c_double),
+                ("holdout_answered", ctypes.c_double), ("holdout_max_abs", ctypes.c_double),
+                ("holdout_p99_abs", ctypes.c_double), ("holdout_all_max_abs", ctypes.c_double),
+                ("holdout", ctypes.c_int64)]
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_}
@@ -542,7 +546,8 @@ class SurrogateStats(ctypes.Structure):
     _fields_ = [("n_in_box", ctypes.c_int64), ("n_routed", ctypes.c_int64), ("n_judged", ctypes.c_int64),
                 ("fell_back", ctypes.c_int32), ("pad", ctypes.c_int32), ("judge_max_abs", ctypes.c_double), ("judge_p99_abs", ctypes.c_double),
                 ("judge_mean_abs", ctypes.c_double), ("network_ms", ctypes.c_double), ("tree_ms", ctypes.c_double),
-                ("route_ms", ctypes.c_double), ("total_ms", ctypes.c_double)]
+                ("route_ms", ctypes.c_double), ("total_ms", ctypes.c_double), ("n_flagged", ctypes.c_int64),
+                ("n_network", ctypes.c_int64)]
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_}
@@ -562,12 +567,15 @@ _SIGNATURES.update({
     "hwt_surrogate_param_count": (ctypes.c_int64, [ctypes.c_void_p]),
     "hwt_surrogate_params": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int]),
     "hwt_surrogate_forward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
+    "hwt_surrogate_forward_ex": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                                ctypes.c_int]),
     "hwt_surrogate_inject_stall": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "hwt_surrogate_loss_grads": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
-                                                ctypes.POINTER(ctypes.c_double), ctypes.c_void_p]),
+                                                ctypes.c_double, ctypes.POINTER(ctypes.c_double), ctypes.c_void_p]),
 })
 
-SURROGATE_DIMS = (8, 256, 256, 256, 256, 1)  # first fan-in: 7 features + 1 zero pad row
+# first fan-in: 7 features + 1 zero pad row; outputs: price residual, log-error estimate
+SURROGATE_DIMS = (8, 256, 256, 256, 256, 2)
 
 
 class Surrogate:
@@ -602,8 +610,11 @@ class Surrogate:
             raise (InvalidInput if rc == HWT_EINVAL else HwtError)(rc, msg.decode() if msg else "")
 
     def train(self, samples: Options, yield_: Yield, epochs: int = 1, batch: int = 8192, lr: float = 1e-3,
-              lr_min: float = 0.0, seed: int = 7) -> dict:
-        cfg = TrainConfig(epochs, batch, lr, lr_min, seed)
+              lr_min: float = 0.0, seed: int = 7, err_weight: float = 0.0, route_tolerance: float = 1e-4,
+              holdout: float = 0.05) -> dict:
+        """Labels the samples with the FP64 tree and trains; with err_weight > 0 the
+        error head is trained too and routes (held-out calibration at route_tolerance)."""
+        cfg = TrainConfig(epochs, batch, lr, lr_min, seed, err_weight, route_tolerance, holdout)
         o, y = samples._c(), yield_._c()
         self._check(lib().hwt_surrogate_train(self._s, ctypes.byref(o), ctypes.byref(y), ctypes.byref(cfg),
                                               ctypes.byref(self.train_stats)))
@@ -641,25 +652,28 @@ class Surrogate:
                                for W, b in params]).astype(np.float32)
         self._check(lib().hwt_surrogate_params(self._s, flat.ctypes.data, len(flat), 1))
 
-    def inject_stall(self, on: bool) -> None:
-        """Test hook: GEMMs wait on an mbarrier phase nothing completes (bounded),
-        so calls return HWT_ETIMEOUT; the context stays usable."""
-        self._check(lib().hwt_surrogate_inject_stall(self._s, 1 if on else 0))
+    def inject_stall(self, mode) -> None:
+        """Test hook: tensor-core kernels wait on an mbarrier phase nothing completes
+        (bounded) - mode 1 before their first MMA, 2 after their first K block's MMAs
+        (True means 1) - so calls return HWT_ETIMEOUT; the context stays usable."""
+        self._check(lib().hwt_surrogate_inject_stall(self._s, int(mode)))
 
-    def forward(self, x: np.ndarray) -> np.ndarray:
+    def forward(self, x: np.ndarray, fused: bool = True) -> np.ndarray:
+        """Network outputs [n, 2] for standardised features x [n, 7]: the fused
+        inference kernel, or the layer-by-layer training kernels."""
         x = np.ascontiguousarray(x, dtype=np.float32)
-        out = np.empty(len(x), dtype=np.float32)
-        self._check(lib().hwt_surrogate_forward(self._s, x.ctypes.data, len(x), out.ctypes.data))
+        out = np.empty((len(x), 2), dtype=np.float32)
+        self._check(lib().hwt_surrogate_forward_ex(self._s, x.ctypes.data, len(x), out.ctypes.data, 0 if fused else 1))
         return out
 
-    def loss_grads(self, x: np.ndarray, y: np.ndarray):
+    def loss_grads(self, x: np.ndarray, y: np.ndarray, err_weight: float = 0.0):
         x = np.ascontiguousarray(x, dtype=np.float32)
         y = np.ascontiguousarray(y, dtype=np.float32)
         n = lib().hwt_surrogate_param_count(self._s)
         g = np.empty(n, dtype=np.float32)
         loss = ctypes.c_double()
-        self._check(lib().hwt_surrogate_loss_grads(self._s, x.ctypes.data, y.ctypes.data, len(x), ctypes.byref(loss),
-                                                   g.ctypes.data))
+        self._check(lib().hwt_surrogate_loss_grads(self._s, x.ctypes.data, y.ctypes.data, len(x), err_weight,
+                                                   ctypes.byref(loss), g.ctypes.data))
         grads, off = [], 0
         for fi, fo in zip(SURROGATE_DIMS[:-1], SURROGATE_DIMS[1:]):
             gW = g[off:off + fi * fo].reshape(fi, fo).copy(); off += fi * fo

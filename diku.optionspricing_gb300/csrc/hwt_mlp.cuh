@@ -1,0 +1,314 @@
+// Fused surrogate network: the whole 8 -> 256 -> 256 -> 256 -> 256 -> 2 SiLU MLP
+// of a 128-row tile in one persistent kernel, activations on chip.
+//
+//   layer 0 (8 -> 256):   fp32 on the CUDA cores, one thread per row, from fp32
+//                         features (the first layer resolves strike-sized features,
+//                         which bf16 inputs or weights would move by ~1e-2 strike)
+//   layers 1-3 (256x256): tcgen05.mma kind::f16, bf16 activations in shared memory
+//                         (A operand, K-major core-matrix layout), bf16 weights
+//                         streamed from L2 (B operand), fp32 accumulator in 256
+//                         TMEM columns (M = 128, N = 256, K = 16 per instruction)
+//   layer 4 (256 -> 2):   fp32 dot products of the bf16-rounded activations with
+//                         bf16-rounded weights, in the last layer's epilogue
+//
+// Each output row is computed exactly as the layer-by-layer training path computes
+// it (same roundings, same K order of the tensor-core sums; layer 4 sums in another
+// order), so a network trained there evaluates the same here.
+//
+// Weights of the three tensor-core layers are pre-packed (the surrogate's refresh
+// kernel) into 24 blocks of [256 output rows x 32 K] in the canonical no-swizzle
+// K-major layout, 16 KB each, so one thread streams a block with a single untiled
+// bulk copy (cp.async.bulk, completion counted on an mbarrier) through a ring of
+// kStages shared-memory stages; the tensor core frees a stage by committing the
+// MMAs that read it to the stage's "empty" mbarrier.  One thread (thread 0) issues
+// copies and MMAs; all 128 threads run the epilogues (thread t owns TMEM lane t =
+// tile row t).  Two CTAs share an SM (112 KB of shared memory and 256 TMEM
+// columns each), so one CTA's epilogue overlaps the other's MMAs.
+//
+// Every mbarrier wait is bounded.  A CTA whose wait runs out raises *err, stops
+// issuing, waits (bounded) for the copies and MMAs it already issued, frees its
+// TMEM and returns; if that drain wait runs out as well the tensor core or the copy
+// engine has stopped completing work, and the CTA frees its TMEM and returns anyway
+// with *err raised.  test_stall injects a wait that nothing completes: 1 before any
+// copy or MMA, 2 after the first weight block's MMAs were committed.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+#include "hwt_umma.cuh"
+
+namespace hwt {
+namespace mlp {
+
+constexpr int kRows = 128;      // rows per tile (the MMA's M, one per thread)
+constexpr int kHidden = 256;
+constexpr int kIn = 8;          // 7 standardised features + a zero pad
+constexpr int kOut = 2;         // price residual, log-error estimate
+constexpr int kKB = 32;         // K per streamed weight block
+constexpr int kBlocksPerLayer = kHidden / kKB;  // 8
+constexpr int kTcLayers = 3;
+constexpr int kBlocks = kTcLayers * kBlocksPerLayer;  // 24 per tile
+constexpr int kStages = 3;
+constexpr int kThreads = 128;
+constexpr int kActBytes = kRows * kHidden * 2;       // 64 KB
+constexpr int kWBlockElems = kHidden * kKB;           // 8192
+constexpr int kWBlockBytes = kWBlockElems * 2;        // 16 KB
+constexpr int kSmemBytes = kActBytes + kStages * kWBlockBytes + 128;
+constexpr int kTmemCols = 256;
+
+struct MlpArgs {
+    const float *X;            // [n][8] standardised features
+    int n;
+    const float *W0, *b0;      // fp32 [8][256], [256]
+    const __nv_bfloat16 *Wp;   // packed blocks of layers 1-3 (see pack_offset)
+    const float *b1, *b2, *b3; // [256] biases of layers 1-3
+    const float *W4r;          // [256][2] bf16-rounded weights of layer 4, as float
+    const float *b4;           // [2]
+    float *out;                // [n][2]
+    int *err;
+    int test_stall;
+};
+
+// Element offset of (output row nrow, k) inside a packed [256 x 32] weight block:
+// 8 x 8 core matrices of 128 contiguous bytes, K-adjacent ones 128 bytes apart,
+// row-adjacent ones 512 bytes apart.
+__host__ __device__ __forceinline__ int pack_offset(int nrow, int k)
+{
+    return ((((nrow >> 3) * (kKB / 8)) + (k >> 3)) << 6) + ((nrow & 7) << 3) + (k & 7);
+}
+
+// Element offset of (row r, k) in the 128 x 256 activation tile: four 64-wide K
+// blocks of the same core-matrix layout (16 KB each), as the GEMM stages use.
+__device__ __forceinline__ int act_offset(int r, int k) { return (k >> 6) * (kRows * 64) + umma::core_offset(r, k & 63); }
+
+// Layer 0 of one row for output columns [n0, n0 + 8): z = b0 + x W0 (fp32, k in
+// order), shared by the fused kernel and the training path.
+__device__ __forceinline__ void layer0_chunk(const float (&x)[kIn], const float *__restrict__ W0,
+                                             const float *__restrict__ b0, int n0, float (&z)[8])
+{
+    const float4 *b4 = reinterpret_cast<const float4 *>(b0 + n0);
+    const float4 ba = __ldg(b4), bb = __ldg(b4 + 1);
+    z[0] = ba.x; z[1] = ba.y; z[2] = ba.z; z[3] = ba.w;
+    z[4] = bb.x; z[5] = bb.y; z[6] = bb.z; z[7] = bb.w;
+#pragma unroll
+    for (int k = 0; k < kIn; ++k) {
+        const float4 *w4 = reinterpret_cast<const float4 *>(W0 + k * kHidden + n0);
+        const float4 wa = __ldg(w4), wb = __ldg(w4 + 1);
+        z[0] = fmaf(x[k], wa.x, z[0]); z[1] = fmaf(x[k], wa.y, z[1]);
+        z[2] = fmaf(x[k], wa.z, z[2]); z[3] = fmaf(x[k], wa.w, z[3]);
+        z[4] = fmaf(x[k], wb.x, z[4]); z[5] = fmaf(x[k], wb.y, z[5]);
+        z[6] = fmaf(x[k], wb.z, z[6]); z[7] = fmaf(x[k], wb.w, z[7]);
+    }
+}
+
+__device__ __forceinline__ uint32_t pack_bf16x2(float a, float b)
+{
+    const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<const uint32_t *>(&h);
+}
+
+__device__ __forceinline__ void bulk_copy_g2s(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(bar)
+                 : "memory");
+}
+
+__global__ void __launch_bounds__(kThreads, 2) mlp_forward_kernel(MlpArgs p)
+{
+    extern __shared__ __align__(1024) unsigned char smem[];
+    __nv_bfloat16 *act = reinterpret_cast<__nv_bfloat16 *>(smem);
+    unsigned char *wst = smem + kActBytes;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + kActBytes + kStages * kWBlockBytes);
+    // bars: full[3], empty[3], acc, never; then the TMEM address and the abort word
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * kStages + 2);
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const uint32_t full0 = umma::smem_u32(&bars[0]), empty0 = umma::smem_u32(&bars[kStages]);
+    const uint32_t acc_bar = umma::smem_u32(&bars[2 * kStages]), never_bar = umma::smem_u32(&bars[2 * kStages + 1]);
+    constexpr uint32_t IDESC = umma::make_idesc(kHidden);
+
+    if (tid == 0) {
+        for (int s = 0; s < 2 * kStages + 2; ++s) umma::mbar_init(umma::smem_u32(&bars[s]), 1);
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) umma::tmem_alloc(umma::smem_u32(tmem_slot), kTmemCols);
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    const uint32_t tmem = *tmem_slot;
+    const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);  // this warp's TMEM lane quarter
+
+    uint32_t ld = 0, mm = 0, acc_uses = 0;  // blocks copied, blocks consumed, accumulator completions (thread 0)
+    bool ok = true;                          // thread 0: no wait ran out
+    int stall = p.test_stall;
+    const int ntiles = (p.n + kRows - 1) / kRows;
+
+    // Thread 0: copy weight block `ld` (global block ld % kBlocks) into its stage,
+    // once the MMAs that last read that stage have completed.
+    auto load_next = [&]() -> bool {
+        const uint32_t s = ld % kStages;
+        if (ld >= (uint32_t)kStages && !umma::mbar_wait(empty0 + 8 * s, ((ld - kStages) / kStages) & 1)) return false;
+        bulk_copy_g2s(umma::smem_u32(wst + s * kWBlockBytes), p.Wp + (size_t)(ld % kBlocks) * kWBlockElems,
+                      kWBlockBytes, full0 + 8 * s);
+        ++ld;
+        return true;
+    };
+
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int row = tile * kRows + tid;
+        // ---- layer 0 on the CUDA cores: this thread's row -> activation tile
+        {
+            float x[kIn];
+            if (row < p.n) {
+                const float4 *xr = reinterpret_cast<const float4 *>(p.X + (size_t)row * kIn);
+                const float4 xa = __ldg(xr), xb = __ldg(xr + 1);
+                x[0] = xa.x; x[1] = xa.y; x[2] = xa.z; x[3] = xa.w;
+                x[4] = xb.x; x[5] = xb.y; x[6] = xb.z; x[7] = xb.w;
+            } else {
+#pragma unroll
+                for (int k = 0; k < kIn; ++k) x[k] = 0.f;
+            }
+#pragma unroll 1
+            for (int n0 = 0; n0 < kHidden; n0 += 8) {
+                float z[8];
+                layer0_chunk(x, p.W0, p.b0, n0, z);
+                uint4 v;
+                v.x = pack_bf16x2(umma::silu_f(z[0]), umma::silu_f(z[1]));
+                v.y = pack_bf16x2(umma::silu_f(z[2]), umma::silu_f(z[3]));
+                v.z = pack_bf16x2(umma::silu_f(z[4]), umma::silu_f(z[5]));
+                v.w = pack_bf16x2(umma::silu_f(z[6]), umma::silu_f(z[7]));
+                *reinterpret_cast<uint4 *>(act + act_offset(tid, n0)) = v;
+            }
+        }
+        float o0 = 0.f, o1 = 0.f;
+#pragma unroll 1
+        for (int l = 0; l < kTcLayers; ++l) {
+            if (tid == 0 && !ok) *abort_flag = 1;  // a prefetch wait ran out
+            umma::fence_proxy_async();  // activation writes -> visible to the tensor core
+            umma::fence_before_sync();
+            __syncthreads();
+            umma::fence_after_sync();
+            if (*abort_flag) break;
+            if (tid == 0) {
+                // blocks of this layer: mm .. mm + 7; at most kStages copies ahead
+                const uint32_t end = mm + kBlocksPerLayer;
+                while (ok && ld < end && ld < mm + kStages) ok = load_next();
+                for (int kb = 0; ok && kb < kBlocksPerLayer; ++kb) {
+                    const uint32_t s = mm % kStages;
+                    if (stall == 1) {  // injected: a phase nothing completes, before any MMA
+                        ok = umma::mbar_wait(never_bar, 0);
+                        stall = 0;
+                        if (!ok) break;
+                    }
+                    if (!umma::mbar_wait(full0 + 8 * s, (mm / kStages) & 1)) { ok = false; break; }
+                    umma::fence_after_sync();
+                    const uint32_t a0 = umma::smem_u32(act), b0 = umma::smem_u32(wst + s * kWBlockBytes);
+#pragma unroll
+                    for (int kk = 0; kk < kKB / 16; ++kk) {
+                        const int ks = kb * (kKB / 16) + kk;  // 16-wide K step in the layer
+                        const uint64_t ad = umma::make_desc(a0 + (ks >> 2) * (kRows * 64 * 2) + (ks & 3) * 256, 128, 1024);
+                        const uint64_t bd = umma::make_desc(b0 + kk * 256, 128, (kKB / 8) * 128);
+                        umma::mma_bf16(tmem, ad, bd, IDESC, (kb > 0 || kk > 0) ? 1u : 0u);
+                    }
+                    umma::mma_commit(empty0 + 8 * s);
+                    ++mm;
+                    if (stall == 2) {  // injected: after this block's MMAs were committed
+                        ok = umma::mbar_wait(never_bar, 0);
+                        stall = 0;
+                        if (!ok) break;
+                    }
+                    // refill the stage block mm - 2 used (its MMAs are one block behind)
+                    if (ld < end && ld < mm + kStages - 1) ok = load_next();
+                }
+                if (ok) umma::mma_commit(acc_bar);
+                else *abort_flag = 1;
+            }
+            __syncthreads();
+            if (*abort_flag) break;
+            // every MMA of the layer has completed once acc_bar's phase does
+            if (!umma::mbar_wait(acc_bar, acc_uses & 1)) {
+                *abort_flag = 1;
+                ok = false;
+            }
+            ++acc_uses;
+            umma::fence_after_sync();
+            if (__syncthreads_or(*abort_flag)) break;
+            // the stages are free: prefetch the next layer's (or the next tile's) first blocks
+            if (tid == 0) {
+                const bool more = l + 1 < kTcLayers || tile + (int)gridDim.x < ntiles;
+                while (ok && more && ld < mm + kStages) ok = load_next();  // a failure is seen at the next barrier
+            }
+            // ---- epilogue: accumulator + bias -> SiLU -> bf16 (next layer's A) or layer 4
+            const float *bias = l == 0 ? p.b1 : (l == 1 ? p.b2 : p.b3);
+#pragma unroll 1
+            for (int c = 0; c < kHidden; c += 16) {
+                float v[16];
+                umma::tmem_ld16(trow + (uint32_t)c, v);
+                const float4 *b4 = reinterpret_cast<const float4 *>(bias + c);
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const float4 b = __ldg(b4 + q);
+                    v[4 * q] += b.x; v[4 * q + 1] += b.y; v[4 * q + 2] += b.z; v[4 * q + 3] += b.w;
+                }
+                if (l + 1 < kTcLayers) {
+                    uint4 lo, hi;
+                    lo.x = pack_bf16x2(umma::silu_f(v[0]), umma::silu_f(v[1]));
+                    lo.y = pack_bf16x2(umma::silu_f(v[2]), umma::silu_f(v[3]));
+                    lo.z = pack_bf16x2(umma::silu_f(v[4]), umma::silu_f(v[5]));
+                    lo.w = pack_bf16x2(umma::silu_f(v[6]), umma::silu_f(v[7]));
+                    hi.x = pack_bf16x2(umma::silu_f(v[8]), umma::silu_f(v[9]));
+                    hi.y = pack_bf16x2(umma::silu_f(v[10]), umma::silu_f(v[11]));
+                    hi.z = pack_bf16x2(umma::silu_f(v[12]), umma::silu_f(v[13]));
+                    hi.w = pack_bf16x2(umma::silu_f(v[14]), umma::silu_f(v[15]));
+                    *reinterpret_cast<uint4 *>(act + act_offset(tid, c)) = lo;
+                    *reinterpret_cast<uint4 *>(act + act_offset(tid, c + 8)) = hi;
+                } else {
+                    const float4 *w4 = reinterpret_cast<const float4 *>(p.W4r + 2 * c);
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) {
+                        const float4 w = __ldg(w4 + q);  // rows c + 2q, c + 2q + 1, two outputs each
+                        const float h0 = __bfloat162float(__float2bfloat16_rn(umma::silu_f(v[2 * q])));
+                        const float h1 = __bfloat162float(__float2bfloat16_rn(umma::silu_f(v[2 * q + 1])));
+                        o0 = fmaf(h0, w.x, o0); o1 = fmaf(h0, w.y, o1);
+                        o0 = fmaf(h1, w.z, o0); o1 = fmaf(h1, w.w, o1);
+                    }
+                }
+            }
+        }
+        if (__syncthreads_or((tid == 0 && !ok) || *abort_flag)) {
+            if (tid == 0) *abort_flag = 1;
+            break;
+        }
+        if (row < p.n) {
+            float2 r;
+            r.x = o0 + __ldg(p.b4);
+            r.y = o1 + __ldg(p.b4 + 1);
+            *reinterpret_cast<float2 *>(p.out + (size_t)row * kOut) = r;
+        }
+    }
+
+    __syncthreads();
+    if (tid == 0) {
+        if (*abort_flag || !ok) {
+            // drain: copies in flight land, committed MMAs complete (bounded)
+            bool drained = true;
+            for (uint32_t b = mm; b < ld; ++b) drained = umma::mbar_wait(full0 + 8 * (b % kStages), (b / kStages) & 1) && drained;
+            if (mm > 0) drained = umma::mbar_wait(empty0 + 8 * ((mm - 1) % kStages), ((mm - 1) / kStages) & 1) && drained;
+            (void)drained;
+            if (p.err) atomicExch(p.err, 1);
+        }
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) {
+        umma::fence_after_sync();
+        umma::tmem_dealloc(tmem, kTmemCols);
+    }
+}
+
+}  // namespace mlp
+}  // namespace hwt

@@ -1,12 +1,18 @@
-// Learned surrogate: a 7 -> 256 -> 256 -> 256 -> 256 -> 1 SiLU MLP that maps
-// standardised option parameters to price / forward bond price.  Weights are
-// kept as fp32 masters with bf16 copies for the tcgen05 tensor-core GEMMs
-// (hwt_umma.cuh); activations between layers are bf16, accumulation fp32 in
-// tensor memory.
-// Training: Adam with cosine decay on labels priced by the batched FP64 tree.
-// Inference: options inside the training box go through the network, the rest
-// to the tree; a random sample of the in-box options is re-priced by the tree
-// as the judge of every batch.
+// Learned surrogate: an 8 -> 256 -> 256 -> 256 -> 256 -> 2 SiLU MLP that maps
+// standardised option parameters (7 features and a zero pad) to
+//   output 0: (price - Hull-White closed-form price) / forward bond price,
+//             standardised (or price / forward bond price with residual = 0), and
+//   output 1: an estimate of log |output-0 error| (the error head), which routes
+//             the options it does not trust to the tree.
+// Layer 0 runs in fp32 on the CUDA cores from fp32 features; layers 1-4 keep fp32
+// master weights with bf16 copies for the tcgen05 tensor cores, bf16 activations
+// and fp32 accumulation.
+// Training: Adam with cosine decay on labels priced by the batched FP64 tree, the
+// layer-by-layer tensor-core GEMMs of hwt_umma.cuh, one CUDA graph per step; a
+// held-out slice of the samples calibrates the error head's routing threshold.
+// Inference: the fused network kernel of hwt_mlp.cuh; options outside the training
+// box and options the error head flags go to the tree, and a random sample of the
+// network's answers is re-priced by the tree as the judge of every batch.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <math.h>
@@ -14,13 +20,15 @@
 #include <string.h>
 
 #include <algorithm>
+#include <cmath>
 #include <string>
 #include <vector>
 
 #include "../../include/hwtree.h"
 #include "hwt_internal.h"
-#include "hwt_umma.cuh"
+#include "hwt_mlp.cuh"
 #include "hwt_model.cuh"
+#include "hwt_umma.cuh"
 
 using namespace hwt;
 using namespace hwt::umma;
@@ -28,13 +36,14 @@ using namespace hwt::umma;
 namespace {
 
 constexpr int kLayers = 5;
-constexpr int kIn = 7, kInPad = 8, kHidden = 256;
+constexpr int kIn = 7, kInPad = mlp::kIn, kHidden = mlp::kHidden, kOut = mlp::kOut;
 const int kFanIn[kLayers] = {kInPad, kHidden, kHidden, kHidden, kHidden};
-const int kFanOut[kLayers] = {kHidden, kHidden, kHidden, kHidden, 1};
-constexpr int kChunk = 65536;  // samples per inference pass
+const int kFanOut[kLayers] = {kHidden, kHidden, kHidden, kHidden, kOut};
+constexpr float kErrEps = 1e-3f;  // floor of the error head's target log(|r| + eps), standardised units
+constexpr int kMaxCurve = 4096;
 
 struct FeatureNorm {
-    float mean[kIn], inv_std[kIn];
+    double mean[kIn], inv_std[kIn];
 };
 
 // ---------------------------------------------------------------------------
@@ -53,9 +62,9 @@ __device__ double hw_closed_form(double t, double T, double X, double a, double 
     return type == 1 ? strike * normcdf(-h + sp) - bond * normcdf(-h) : bond * normcdf(h) - strike * normcdf(h - sp);
 }
 
-// Features, forward bond price, control-variate price and in-box flag of each option.
-__global__ void features_kernel(DevOptions o, DevYield yc, hwt_box box, FeatureNorm fn, __nv_bfloat16 *X,
-                                double *F, double *base, uint8_t *inbox)
+// fp32 features, forward bond price, control-variate price and in-box flag of each option.
+__global__ void features_kernel(DevOptions o, DevYield yc, hwt_box box, FeatureNorm fn, float *X, double *F,
+                                double *base, uint8_t *inbox)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= o.n) return;
@@ -68,9 +77,13 @@ __global__ void features_kernel(DevOptions o, DevYield yc, hwt_box box, FeatureN
     const double a = o.a[i], sg = o.sigma[i];
     const int steps = o.term_steps[i];
     const double v[kIn] = {t, T, mny, a, sg, (double)steps, (double)o.type[i]};
+    float x[kInPad];
 #pragma unroll
-    for (int q = 0; q < kIn; ++q) X[(size_t)i * kInPad + q] = __float2bfloat16(((float)v[q] - fn.mean[q]) * fn.inv_std[q]);
-    X[(size_t)i * kInPad + kIn] = __float2bfloat16(0.f);
+    for (int q = 0; q < kIn; ++q) x[q] = (float)((v[q] - fn.mean[q]) * fn.inv_std[q]);
+    x[kIn] = 0.f;
+    float4 *xr = reinterpret_cast<float4 *>(X + (size_t)i * kInPad);
+    xr[0] = make_float4(x[0], x[1], x[2], x[3]);
+    xr[1] = make_float4(x[4], x[5], x[6], x[7]);
     F[i] = fwd;
     base[i] = box.residual ? hw_closed_form(t, T, o.strike[i], a, sg, Pt, PT, o.type[i]) : 0.0;
     const double span = T - t;
@@ -81,17 +94,66 @@ __global__ void features_kernel(DevOptions o, DevYield yc, hwt_box box, FeatureN
     inbox[i] = in ? 1 : 0;
 }
 
-// r = out - y; dZ = r / n (bf16 operand of the backward GEMMs); loss += 0.5 r^2 / n
-__global__ void loss_kernel(const float *out, const float *y, int n, __nv_bfloat16 *dZ, float *dZf, double *loss)
+// Layer 0 of the training path: Z0 = X W0 + b0 (fp32) and H1 = bf16(silu(Z0)),
+// one warp per row (eight columns per lane), with the fused kernel's arithmetic.
+__global__ void layer0_kernel(const float *X, const float *W0, const float *b0, int n, float *Z0, __nv_bfloat16 *H1)
+{
+    const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+    const int row = gt >> 5, n0 = (gt & 31) * 8;
+    if (row >= n) return;
+    const float4 *xr = reinterpret_cast<const float4 *>(X + (size_t)row * kInPad);
+    const float4 xa = xr[0], xb = xr[1];
+    const float x[kInPad] = {xa.x, xa.y, xa.z, xa.w, xb.x, xb.y, xb.z, xb.w};
+    float z[8];
+    mlp::layer0_chunk(x, W0, b0, n0, z);
+    float4 *zr = reinterpret_cast<float4 *>(Z0 + (size_t)row * kHidden + n0);
+    zr[0] = make_float4(z[0], z[1], z[2], z[3]);
+    zr[1] = make_float4(z[4], z[5], z[6], z[7]);
+    uint4 h;
+    h.x = mlp::pack_bf16x2(silu_f(z[0]), silu_f(z[1]));
+    h.y = mlp::pack_bf16x2(silu_f(z[2]), silu_f(z[3]));
+    h.z = mlp::pack_bf16x2(silu_f(z[4]), silu_f(z[5]));
+    h.w = mlp::pack_bf16x2(silu_f(z[6]), silu_f(z[7]));
+    *reinterpret_cast<uint4 *>(H1 + (size_t)row * kHidden + n0) = h;
+}
+
+// dW0[k][c] += sum over rows of X[r][k] dZ0[r][c] (fp32), a slice of rows per block.
+__global__ void dw0_kernel(const float *X, const float *dZ, int n, float *dW0)
+{
+    const int c = threadIdx.x;  // kHidden threads
+    const int per = (n + gridDim.x - 1) / gridDim.x;
+    const int r0 = blockIdx.x * per, r1 = min(n, r0 + per);
+    float acc[kInPad] = {};
+    for (int r = r0; r < r1; ++r) {
+        const float d = dZ[(size_t)r * kHidden + c];
+        const float4 *xr = reinterpret_cast<const float4 *>(X + (size_t)r * kInPad);
+        const float4 xa = __ldg(xr), xb = __ldg(xr + 1);
+        acc[0] = fmaf(xa.x, d, acc[0]); acc[1] = fmaf(xa.y, d, acc[1]);
+        acc[2] = fmaf(xa.z, d, acc[2]); acc[3] = fmaf(xa.w, d, acc[3]);
+        acc[4] = fmaf(xb.x, d, acc[4]); acc[5] = fmaf(xb.y, d, acc[5]);
+        acc[6] = fmaf(xb.z, d, acc[6]); acc[7] = fmaf(xb.w, d, acc[7]);
+    }
+    if (r1 > r0)
+        for (int k = 0; k < kInPad; ++k) atomicAdd(dW0 + k * kHidden + c, acc[k]);
+}
+
+// Outputs [n][2] against targets y: r = o0 - y; error-head target g = log(|r| + eps)
+// (held constant); loss += 0.5 r^2 / n + 0.5 lam (o1 - g)^2 / n; dZ = its gradient.
+__global__ void loss_kernel(const float *out, const float *y, int n, float lam, __nv_bfloat16 *dZ, float *dZf,
+                            double *loss)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double l = 0.0;
     if (i < n) {
-        const float r = out[i] - y[i];
-        const float d = r / (float)n;
-        dZ[i] = __float2bfloat16(d);
-        dZf[i] = d;
-        l = 0.5 * (double)r * (double)r / n;
+        const float r = out[2 * i] - y[i];
+        const float g = logf(fabsf(r) + kErrEps);
+        const float r1 = out[2 * i + 1] - g;
+        const float d0 = r / (float)n, d1 = lam * r1 / (float)n;
+        dZ[2 * i] = __float2bfloat16(d0);
+        dZ[2 * i + 1] = __float2bfloat16(d1);
+        dZf[2 * i] = d0;
+        dZf[2 * i + 1] = d1;
+        l = (0.5 * (double)r * r + 0.5 * (double)lam * (double)r1 * r1) / n;
     }
     for (int off = 16; off > 0; off >>= 1) l += __shfl_xor_sync(0xffffffffu, l, off);
     if ((threadIdx.x & 31) == 0 && l != 0.0) atomicAdd(loss, l);
@@ -148,13 +210,15 @@ __global__ void step_begin_kernel(StepState *st, double lr0, double lr_min, long
 }
 
 // Batch `cur` of the shuffled samples into the fixed input and target buffers.
-__global__ void batch_copy_kernel(const __nv_bfloat16 *Xs, const float *ys, const StepState *st, int batch,
-                                  __nv_bfloat16 *X, float *y)
+__global__ void batch_copy_kernel(const float *Xs, const float *ys, const StepState *st, int batch, float *X, float *y)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= batch) return;
     const size_t row = (size_t)st->cur * batch + i;
-    *reinterpret_cast<uint4 *>(X + (size_t)i * kInPad) = *reinterpret_cast<const uint4 *>(Xs + row * kInPad);
+    const float4 *src = reinterpret_cast<const float4 *>(Xs + row * kInPad);
+    float4 *dst = reinterpret_cast<float4 *>(X + (size_t)i * kInPad);
+    dst[0] = src[0];
+    dst[1] = src[1];
     y[i] = ys[row];
 }
 
@@ -176,25 +240,32 @@ __global__ void adam_kernel(AdamArgs a, const StepState *st)
     a.w[i] -= a.lr * (m / a.c1) / (sqrtf(v / a.c2) + a.eps);
 }
 
-// bf16 copies of W[in][out]: Wt[out][in_pad] (forward operand) and Wb[in_pad][out]
-__global__ void refresh_kernel(const float *W, int in, int in_pad, int out, __nv_bfloat16 *Wt, __nv_bfloat16 *Wb)
+// bf16 copies of W[in][out] (layers 1-4): Wt[out][in] (forward operand), Wb[in][out]
+// (backward-data operand), the fused kernel's packed blocks (layers 1-3) and the
+// bf16-rounded values as float (layer 4).
+__global__ void refresh_kernel(const float *W, int in, int out, __nv_bfloat16 *Wt, __nv_bfloat16 *Wb,
+                               __nv_bfloat16 *Wp, float *Wr)
 {
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= in_pad * out) return;
+    if (idx >= in * out) return;
     const int k = idx / out, n = idx % out;
-    const __nv_bfloat16 v = __float2bfloat16(k < in ? W[(size_t)k * out + n] : 0.f);
-    Wt[(size_t)n * in_pad + k] = v;
+    const __nv_bfloat16 v = __float2bfloat16(W[(size_t)k * out + n]);
+    Wt[(size_t)n * in + k] = v;
     Wb[(size_t)k * out + n] = v;
+    if (Wp) Wp[(size_t)(k / mlp::kKB) * mlp::kWBlockElems + mlp::pack_offset(n, k % mlp::kKB)] = v;
+    if (Wr) Wr[(size_t)k * out + n] = __bfloat162float(v);
 }
 
-__global__ void gather_rows_kernel(const __nv_bfloat16 *X, const float *y, const int32_t *perm, int n,
-                                   __nv_bfloat16 *Xo, float *yo)
+__global__ void gather_rows_kernel(const float *X, const float *y, const int32_t *perm, int n, float *Xo, float *yo)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int s = perm[i];
-    *reinterpret_cast<uint4 *>(Xo + (size_t)i * kInPad) = *reinterpret_cast<const uint4 *>(X + (size_t)s * kInPad);
-    yo[i] = y[s];
+    const float4 *src = reinterpret_cast<const float4 *>(X + (size_t)s * kInPad);
+    float4 *dst = reinterpret_cast<float4 *>(Xo + (size_t)i * kInPad);
+    dst[0] = src[0];
+    dst[1] = src[1];
+    if (y) yo[i] = y[s];
 }
 
 __global__ void targets_kernel(const double *price, const double *F, const double *base, int n, double ymean,
@@ -202,14 +273,6 @@ __global__ void targets_kernel(const double *price, const double *F, const doubl
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) y[i] = (float)(((price[i] - base[i]) / F[i] - ymean) * yinv);
-}
-
-// Price from the network output for in-box options.
-__global__ void decode_kernel(const float *out, const double *F, const double *base, const uint8_t *inbox, int n,
-                              double ymean, double ystd, double *price)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n && inbox[i]) price[i] = base[i] + F[i] * ((double)out[i] * ystd + ymean);
 }
 
 __device__ __forceinline__ unsigned long long mix64(unsigned long long x)
@@ -220,30 +283,68 @@ __device__ __forceinline__ unsigned long long mix64(unsigned long long x)
     return x ^ (x >> 31);
 }
 
-// Tree work list: out-of-box options, and in-box options drawn for the judge.
-// kind: 1 = routed, 2 = judged.
-__global__ void route_kernel(const uint8_t *inbox, int n, unsigned long long seed, unsigned long long thresh,
-                             int32_t *list, uint8_t *kind, int32_t *count)
+// Kinds of an option in a priced batch.
+enum Kind : uint8_t {
+    KIND_NETWORK = 0,  // answered by the network
+    KIND_OUTSIDE = 1,  // outside the training box: tree
+    KIND_JUDGED = 2,   // answered by the network and re-priced by the tree (the judge's sample)
+    KIND_FLAGGED = 3,  // inside the box, but the error head does not trust the network: tree
+};
+
+// Decodes the network's answers and builds the tree's work list: out-of-box and
+// flagged options (the tree answers them), and the judge's draw among the network's
+// answers.  counts[k] = options of kind k (k = 1..3).
+__global__ void decode_route_kernel(const float *out, const double *F, const double *base, const uint8_t *inbox,
+                                    int n, double ymean, double ystd, float log_tau_over_ystd,
+                                    unsigned long long seed, unsigned long long thresh, double *price,
+                                    uint8_t *kind, int32_t *list, int32_t *counts)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    uint8_t k = 0;
-    if (!inbox[i]) k = 1;
-    else if (mix64(seed ^ (unsigned long long)i) < thresh) k = 2;
+    uint8_t k = KIND_NETWORK;
+    if (!inbox[i]) {
+        k = KIND_OUTSIDE;
+    } else {
+        const float2 o = reinterpret_cast<const float2 *>(out)[i];
+        price[i] = base[i] + F[i] * ((double)o.x * ystd + ymean);
+        // predicted |price error| = exp(o1) ystd F > tau  <=>  o1 > log(tau / ystd) - log(F)
+        if (o.y > log_tau_over_ystd - logf((float)F[i])) k = KIND_FLAGGED;
+        else if (mix64(seed ^ (unsigned long long)i) < thresh) k = KIND_JUDGED;
+    }
     kind[i] = k;
-    if (k) list[atomicAdd(count, 1)] = i;
+    if (k != KIND_NETWORK) {
+        list[atomicAdd(counts, 1)] = i;
+        atomicAdd(counts + k, 1);
+    }
 }
 
-__global__ void gather_options_kernel(DevOptions src, const int32_t *list, const int32_t *count, DevOptions dst_mut,
-                                      double *strike, double *bm, double *om, uint16_t *tu, uint16_t *ts, double *a,
-                                      double *sg, int8_t *ty)
+// Network answers of kind KIND_NETWORK into the list (the whole-batch fallback).
+__global__ void network_list_kernel(const uint8_t *kind, int n, int32_t *list, int32_t *count)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && kind[i] == KIND_NETWORK) list[atomicAdd(count, 1)] = i;
+}
+
+__global__ void gather_options_kernel(DevOptions src, const int32_t *list, int m, double *strike, double *bm,
+                                      double *om, uint16_t *tu, uint16_t *ts, double *a, double *sg, int8_t *ty)
 {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= *count) return;
+    if (j >= m) return;
     const int i = list[j];
     strike[j] = src.strike[i]; bm[j] = src.bond_maturity[i]; om[j] = src.option_maturity[i];
     tu[j] = src.term_unit[i]; ts[j] = src.term_steps[i]; a[j] = src.a[i]; sg[j] = src.sigma[i]; ty[j] = src.type[i];
-    (void)dst_mut;
+}
+
+// Tree prices back into the batch; the judge's |network - tree| (else -1) per entry.
+__global__ void scatter_tree_kernel(const int32_t *list, int m, const double *tree, const uint8_t *kind, double *price,
+                                    double *err)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= m) return;
+    const int i = list[j];
+    const double t = tree[j];
+    err[j] = kind[i] == KIND_JUDGED ? fabs(price[i] - t) : -1.0;
+    price[i] = t;
 }
 
 }  // namespace
@@ -251,364 +352,9 @@ __global__ void gather_options_kernel(DevOptions src, const int32_t *list, const
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
-struct hwt_surrogate {
-    hwt_ctx *ctx = nullptr;
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    hwt_box box;
-    FeatureNorm fn;
-    double ymean = 0.0, ystd = 1.0;
-    int trained = 0;
-    std::string err;
-    // parameters (fp32 masters) and Adam state, one flat buffer each
-    size_t n_params = 0;
-    float *d_w = nullptr, *d_m = nullptr, *d_v = nullptr, *d_g = nullptr;
-    size_t w_off[kLayers], b_off[kLayers];
-    __nv_bfloat16 *d_wt[kLayers] = {}, *d_wb[kLayers] = {};
-    long adam_t = 0;
-    // activations for one batch / chunk
-    int act_cap = 0;
-    __nv_bfloat16 *d_h[kLayers + 1] = {};  // h[0] = X, h[l+1] = silu(z_l) for l < 4
-    float *d_z[kLayers] = {};              // pre-activations (z[4] = output)
-    __nv_bfloat16 *d_dz = nullptr, *d_dz2 = nullptr;
-    float *d_dzf = nullptr;
-    double *d_loss = nullptr;
-    float *d_y = nullptr;
-    int *d_gemm_err = nullptr;  // raised by a GEMM whose mbarrier wait ran out
-    int stall = 0;              // fault injection for tests (hwt_surrogate_inject_stall)
-};
-
 namespace {
 
-int sfail(hwt_surrogate *s, int code, const std::string &m)
-{
-    s->err = m;
-    return code;
-}
-
-#define SCUDA(s, call, what)                                                                      \
-    do {                                                                                          \
-        cudaError_t e_ = (call);                                                                  \
-        if (e_ != cudaSuccess) {                                                                  \
-            cudaGetLastError();                                                                   \
-            return sfail((s), e_ == cudaErrorMemoryAllocation ? HWT_ENOMEM : HWT_ECUDA,           \
-                         std::string(what) + ": " + cudaGetErrorString(e_));                      \
-        }                                                                                         \
-    } while (0)
-
-int ensure_act(hwt_surrogate *s, int rows)
-{
-    if (rows <= s->act_cap) return HWT_OK;
-    for (int l = 0; l <= kLayers; ++l) { cudaFree(s->d_h[l]); s->d_h[l] = nullptr; }
-    for (int l = 0; l < kLayers; ++l) { cudaFree(s->d_z[l]); s->d_z[l] = nullptr; }
-    cudaFree(s->d_dz); cudaFree(s->d_dz2); cudaFree(s->d_dzf); cudaFree(s->d_y);
-    SCUDA(s, cudaMalloc(&s->d_h[0], sizeof(__nv_bfloat16) * (size_t)rows * kInPad), "alloc X");
-    for (int l = 1; l < kLayers; ++l) SCUDA(s, cudaMalloc(&s->d_h[l], sizeof(__nv_bfloat16) * (size_t)rows * kHidden), "alloc H");
-    for (int l = 0; l < kLayers; ++l) SCUDA(s, cudaMalloc(&s->d_z[l], sizeof(float) * (size_t)rows * kFanOut[l]), "alloc Z");
-    SCUDA(s, cudaMalloc(&s->d_dz, sizeof(__nv_bfloat16) * (size_t)rows * kHidden), "alloc dZ");
-    SCUDA(s, cudaMalloc(&s->d_dz2, sizeof(__nv_bfloat16) * (size_t)rows * kHidden), "alloc dZ");
-    SCUDA(s, cudaMalloc(&s->d_dzf, sizeof(float) * (size_t)rows * kHidden), "alloc dZf");
-    SCUDA(s, cudaMalloc(&s->d_y, sizeof(float) * (size_t)rows), "alloc y");
-    s->act_cap = rows;
-    return HWT_OK;
-}
-
-template <bool TA, bool TB, int BN>
-cudaError_t gemm_bn(const GemmArgs &a, int splits, cudaStream_t st)
-{
-    auto kern = umma_gemm_kernel<TA, TB, BN>;
-    dim3 grid((a.N + BN - 1) / BN, (a.M + BM - 1) / BM, splits);
-    kern<<<grid, THREADS, smem_bytes(BN), st>>>(a);
-    return cudaGetLastError();
-}
-
-// Dynamic shared memory above 48 KB for every GEMM instantiation, once at set-up
-// (outside any stream capture).
-cudaError_t gemm_attributes()
-{
-    cudaError_t e = cudaSuccess;
-    auto set = [&](auto kern, int bn) {
-        if (e == cudaSuccess) e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes(bn));
-    };
-    set(umma_gemm_kernel<false, false, 16>, 16);
-    set(umma_gemm_kernel<false, false, 64>, 64);
-    set(umma_gemm_kernel<false, false, 128>, 128);
-    set(umma_gemm_kernel<true, true, 16>, 16);
-    set(umma_gemm_kernel<true, true, 64>, 64);
-    set(umma_gemm_kernel<true, true, 128>, 128);
-    return e;
-}
-
-// Tile width: the output width rounded up to 16 (one tile for the 1-wide output
-// layer), at most 128 so that a 256-wide layer spreads over two column tiles.
-template <bool TA, bool TB>
-cudaError_t gemm(const GemmArgs &a, int splits, cudaStream_t st)
-{
-    if (a.N <= 16) return gemm_bn<TA, TB, 16>(a, splits, st);
-    if (a.N <= 64) return gemm_bn<TA, TB, 64>(a, splits, st);
-    return gemm_bn<TA, TB, 128>(a, splits, st);
-}
-
-GemmArgs gargs(const hwt_surrogate *s, const __nv_bfloat16 *A, const __nv_bfloat16 *B, int M, int N, int K, int lda,
-               int ldb, int epi)
-{
-    GemmArgs g;
-    memset(&g, 0, sizeof(g));
-    g.A = A; g.B = B; g.M = M; g.N = N; g.K = K; g.lda = lda; g.ldb = ldb; g.epi = epi;
-    g.k_chunk = (K + BK - 1) / BK * BK;
-    g.err = s->d_gemm_err;
-    g.test_stall = s->stall;
-    return g;
-}
-
-// HWT_ETIMEOUT (and the flag cleared) if a GEMM gave up waiting since the last check.
-int gemm_status(hwt_surrogate *s)
-{
-    int flag = 0;
-    SCUDA(s, cudaMemcpy(&flag, s->d_gemm_err, sizeof(int), cudaMemcpyDeviceToHost), "GEMM status");
-    if (flag == 0) return HWT_OK;
-    SCUDA(s, cudaMemset(s->d_gemm_err, 0, sizeof(int)), "GEMM status");
-    return sfail(s, HWT_ETIMEOUT, "tensor-core GEMM: an mbarrier wait ran out");
-}
-
-// Forward through all layers for `rows` samples already in d_h[0].  Output
-// (normalised) in d_z[4].
-int forward(hwt_surrogate *s, int rows)
-{
-    for (int l = 0; l < kLayers; ++l) {
-        const bool last = l == kLayers - 1;
-        GemmArgs g = gargs(s, s->d_h[l], s->d_wt[l], rows, kFanOut[l], kFanIn[l], kFanIn[l], kFanIn[l],
-                           last ? EPI_BIAS : EPI_BIAS_SILU);
-        g.bias = s->d_w + s->b_off[l];
-        g.Cf = s->d_z[l];
-        g.ldc = kFanOut[l];
-        g.Cb = last ? nullptr : s->d_h[l + 1];
-        g.ldcb = kFanOut[l];
-        SCUDA(s, (gemm<false, false>(g, 1, s->stream)), "forward gemm");
-    }
-    return HWT_OK;
-}
-
-// Loss and gradients (into d_g) for `rows` samples in d_h[0] with targets d_y.
-int backward(hwt_surrogate *s, int rows, bool zero_loss)
-{
-    SCUDA(s, cudaMemsetAsync(s->d_g, 0, sizeof(float) * s->n_params, s->stream), "zero grads");
-    if (zero_loss) SCUDA(s, cudaMemsetAsync(s->d_loss, 0, sizeof(double), s->stream), "zero loss");
-    loss_kernel<<<(rows + 255) / 256, 256, 0, s->stream>>>(s->d_z[kLayers - 1], s->d_y, rows, s->d_dz, s->d_dzf, s->d_loss);
-    SCUDA(s, cudaGetLastError(), "loss kernel");
-    __nv_bfloat16 *dz = s->d_dz, *dz_next = s->d_dz2;
-    const int splits = std::max(1, std::min(64, rows / 512));
-    int kc = (rows + splits - 1) / splits;
-    kc = (kc + BK - 1) / BK * BK;
-    for (int l = kLayers - 1; l >= 0; --l) {
-        const int in = kFanIn[l], out = kFanOut[l];
-        // dW_l[in][out] = H_l^T dZ_l   (split-K over the batch)
-        GemmArgs gw = gargs(s, s->d_h[l], dz, in, out, rows, in, out, EPI_ATOMIC);
-        gw.Cf = s->d_g + s->w_off[l];
-        gw.ldc = out;
-        gw.k_chunk = kc;
-        SCUDA(s, (gemm<true, true>(gw, (rows + kc - 1) / kc, s->stream)), "dW gemm");
-        // db_l = column sums of dZ_l (fp32 copy in d_dzf)
-        dim3 cg((out + 255) / 256, std::max(1, std::min(256, rows / 32)));
-        colsum_kernel<<<cg, 256, 0, s->stream>>>(s->d_dzf, rows, out, out, s->d_g + s->b_off[l]);
-        SCUDA(s, cudaGetLastError(), "db kernel");
-        if (l == 0) break;
-        // dZ_{l-1} = (dZ_l W_l^T) * silu'(Z_{l-1})
-        GemmArgs gd = gargs(s, dz, s->d_wb[l], rows, in, out, out, out, EPI_DSILU);
-        gd.Zin = s->d_z[l - 1];
-        gd.Cf = s->d_dzf;
-        gd.ldc = in;
-        gd.Cb = dz_next;
-        gd.ldcb = in;
-        SCUDA(s, (gemm<false, false>(gd, 1, s->stream)), "dX gemm");
-        std::swap(dz, dz_next);
-    }
-    return HWT_OK;
-}
-
-int refresh(hwt_surrogate *s)
-{
-    for (int l = 0; l < kLayers; ++l) {
-        const int in = l == 0 ? kIn : kFanIn[l];
-        const int tot = kFanIn[l] * kFanOut[l];
-        refresh_kernel<<<(tot + 255) / 256, 256, 0, s->stream>>>(s->d_w + s->w_off[l], in, kFanIn[l], kFanOut[l],
-                                                               s->d_wt[l], s->d_wb[l]);
-        SCUDA(s, cudaGetLastError(), "refresh kernel");
-    }
-    return HWT_OK;
-}
-
-// One training step on the batch the step state names, everything from device
-// state: the body of the captured training graph.
-int train_step(hwt_surrogate *s, const __nv_bfloat16 *Xs, const float *ys, StepState *st, int batch, double lr0,
-               double lr_min, long long total)
-{
-    step_begin_kernel<<<1, 1, 0, s->stream>>>(st, lr0, lr_min, total);
-    SCUDA(s, cudaGetLastError(), "step kernel");
-    batch_copy_kernel<<<(batch + 255) / 256, 256, 0, s->stream>>>(Xs, ys, st, batch, s->d_h[0], s->d_y);
-    SCUDA(s, cudaGetLastError(), "batch kernel");
-    int r = forward(s, batch);
-    if (!r) r = backward(s, batch, false);
-    if (r) return r;
-    AdamArgs a;
-    a.w = s->d_w; a.m = s->d_m; a.v = s->d_v; a.g = s->d_g; a.n = (int)s->n_params;
-    a.lr = 0.f; a.b1 = 0.9f; a.b2 = 0.999f; a.eps = 1e-8f; a.c1 = 1.f; a.c2 = 1.f;
-    adam_kernel<<<((int)s->n_params + 255) / 256, 256, 0, s->stream>>>(a, st);
-    SCUDA(s, cudaGetLastError(), "adam kernel");
-    return refresh(s);
-}
-
-void box_norm(const hwt_box &b, FeatureNorm &fn)
-{
-    const double lo[kIn] = {b.t_min, b.t_min + b.span_min, b.moneyness_min, b.a_min, b.sigma_min, (double)b.steps_min, 0.0};
-    const double hi[kIn] = {b.t_max, b.t_max + b.span_max, b.moneyness_max, b.a_max, b.sigma_max, (double)b.steps_max, 1.0};
-    for (int q = 0; q < kIn; ++q) {
-        const double w = std::max(hi[q] - lo[q], 1e-12);
-        fn.mean[q] = (float)(0.5 * (lo[q] + hi[q]));
-        fn.inv_std[q] = (float)(1.0 / (w / sqrt(12.0)));
-    }
-}
-
-}  // namespace
-
-extern "C" {
-
-hwt_surrogate *hwt_surrogate_create(hwt_ctx *ctx, const hwt_box *box, uint64_t seed)
-{
-    if (!ctx || !box) return nullptr;
-    hwt_surrogate *s = new hwt_surrogate();
-    s->ctx = ctx;
-    s->box = *box;
-    box_norm(*box, s->fn);
-    cudaGetDevice(&s->device);
-    bool ok = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) == cudaSuccess;
-    size_t off = 0;
-    for (int l = 0; l < kLayers; ++l) {
-        s->w_off[l] = off; off += (size_t)kFanIn[l] * kFanOut[l];
-        s->b_off[l] = off; off += kFanOut[l];
-    }
-    s->n_params = off;
-    ok = ok && cudaMalloc(&s->d_w, 4 * off) == cudaSuccess && cudaMalloc(&s->d_m, 4 * off) == cudaSuccess &&
-         cudaMalloc(&s->d_v, 4 * off) == cudaSuccess && cudaMalloc(&s->d_g, 4 * off) == cudaSuccess &&
-         cudaMalloc(&s->d_loss, sizeof(double)) == cudaSuccess &&
-         cudaMalloc(&s->d_gemm_err, sizeof(int)) == cudaSuccess && cudaMemset(s->d_gemm_err, 0, sizeof(int)) == cudaSuccess;
-    for (int l = 0; l < kLayers && ok; ++l) {
-        ok = cudaMalloc(&s->d_wt[l], 2 * (size_t)kFanIn[l] * kFanOut[l]) == cudaSuccess &&
-             cudaMalloc(&s->d_wb[l], 2 * (size_t)kFanIn[l] * kFanOut[l]) == cudaSuccess;
-    }
-    if (ok) {
-        // He initialisation from a seeded host generator (splitmix64 + Box-Muller)
-        std::vector<float> w(off, 0.f);
-        unsigned long long st = seed ? seed : 0x1234567ull;
-        auto next = [&]() {
-            st += 0x9e3779b97f4a7c15ull;
-            unsigned long long z = st;
-            z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
-            z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
-            return (double)((z ^ (z >> 31)) >> 11) * (1.0 / 9007199254740992.0);
-        };
-        for (int l = 0; l < kLayers; ++l) {
-            const int in = l == 0 ? kIn : kFanIn[l];
-            const double sd = sqrt(2.0 / in) * (l == kLayers - 1 ? 0.1 : 1.0);
-            for (int k = 0; k < in; ++k)
-                for (int n = 0; n < kFanOut[l]; ++n) {
-                    const double u1 = std::max(next(), 1e-300), u2 = next();
-                    w[s->w_off[l] + (size_t)k * kFanOut[l] + n] = (float)(sd * sqrt(-2.0 * log(u1)) * cos(6.283185307179586 * u2));
-                }
-        }
-        ok = cudaMemcpy(s->d_w, w.data(), 4 * off, cudaMemcpyHostToDevice) == cudaSuccess &&
-             cudaMemset(s->d_m, 0, 4 * off) == cudaSuccess && cudaMemset(s->d_v, 0, 4 * off) == cudaSuccess;
-        ok = ok && gemm_attributes() == cudaSuccess;
-        ok = ok && refresh(s) == HWT_OK && cudaStreamSynchronize(s->stream) == cudaSuccess;
-    }
-    if (!ok) {
-        cudaGetLastError();
-        hwt_surrogate_destroy(s);
-        return nullptr;
-    }
-    return s;
-}
-
-void hwt_surrogate_destroy(hwt_surrogate *s)
-{
-    if (!s) return;
-    if (s->stream) cudaStreamSynchronize(s->stream);
-    cudaFree(s->d_w); cudaFree(s->d_m); cudaFree(s->d_v); cudaFree(s->d_g); cudaFree(s->d_loss); cudaFree(s->d_gemm_err);
-    for (int l = 0; l < kLayers; ++l) { cudaFree(s->d_wt[l]); cudaFree(s->d_wb[l]); cudaFree(s->d_z[l]); }
-    for (int l = 0; l <= kLayers; ++l) cudaFree(s->d_h[l]);
-    cudaFree(s->d_dz); cudaFree(s->d_dz2); cudaFree(s->d_dzf); cudaFree(s->d_y);
-    if (s->stream) cudaStreamDestroy(s->stream);
-    delete s;
-}
-
-const char *hwt_surrogate_last_error(const hwt_surrogate *s) { return s ? s->err.c_str() : "no surrogate"; }
-
-int hwt_surrogate_inject_stall(hwt_surrogate *s, int on)
-{
-    if (!s) return HWT_EINVAL;
-    s->stall = on ? 1 : 0;
-    return HWT_OK;
-}
-
-int64_t hwt_surrogate_param_count(const hwt_surrogate *s) { return s ? (int64_t)s->n_params : 0; }
-
-int hwt_surrogate_params(hwt_surrogate *s, float *buf, int64_t n, int set)
-{
-    if (!s || !buf || n != (int64_t)s->n_params) return HWT_EINVAL;
-    if (set) {
-        SCUDA(s, cudaMemcpy(s->d_w, buf, 4 * n, cudaMemcpyHostToDevice), "set params");
-        int r = refresh(s);
-        if (r) return r;
-        SCUDA(s, cudaStreamSynchronize(s->stream), "refresh");
-    } else {
-        SCUDA(s, cudaMemcpy(buf, s->d_w, 4 * n, cudaMemcpyDeviceToHost), "get params");
-    }
-    return HWT_OK;
-}
-
-int hwt_surrogate_forward(hwt_surrogate *s, const float *x, int n, float *out)
-{
-    if (!s || !x || !out || n <= 0) return HWT_EINVAL;
-    int r = ensure_act(s, n);
-    if (r) return r;
-    std::vector<__nv_bfloat16> xb((size_t)n * kInPad);
-    for (int i = 0; i < n; ++i)
-        for (int q = 0; q < kInPad; ++q) xb[(size_t)i * kInPad + q] = __float2bfloat16(q < kIn ? x[(size_t)i * kIn + q] : 0.f);
-    SCUDA(s, cudaMemcpy(s->d_h[0], xb.data(), 2 * xb.size(), cudaMemcpyHostToDevice), "x H2D");
-    if ((r = forward(s, n))) return r;
-    SCUDA(s, cudaMemcpyAsync(out, s->d_z[kLayers - 1], 4 * (size_t)n, cudaMemcpyDeviceToHost, s->stream), "out D2H");
-    SCUDA(s, cudaStreamSynchronize(s->stream), "forward");
-    return gemm_status(s);
-}
-
-int hwt_surrogate_loss_grads(hwt_surrogate *s, const float *x, const float *y, int n, double *loss, float *grads)
-{
-    if (!s || !x || !y || n <= 0) return HWT_EINVAL;
-    int r = ensure_act(s, n);
-    if (r) return r;
-    std::vector<__nv_bfloat16> xb((size_t)n * kInPad);
-    for (int i = 0; i < n; ++i)
-        for (int q = 0; q < kInPad; ++q) xb[(size_t)i * kInPad + q] = __float2bfloat16(q < kIn ? x[(size_t)i * kIn + q] : 0.f);
-    SCUDA(s, cudaMemcpy(s->d_h[0], xb.data(), 2 * xb.size(), cudaMemcpyHostToDevice), "x H2D");
-    SCUDA(s, cudaMemcpy(s->d_y, y, 4 * (size_t)n, cudaMemcpyHostToDevice), "y H2D");
-    if ((r = forward(s, n))) return r;
-    if ((r = backward(s, n, true))) return r;
-    if (grads) SCUDA(s, cudaMemcpyAsync(grads, s->d_g, 4 * s->n_params, cudaMemcpyDeviceToHost, s->stream), "grads D2H");
-    double l = 0;
-    SCUDA(s, cudaMemcpyAsync(&l, s->d_loss, sizeof(double), cudaMemcpyDeviceToHost, s->stream), "loss D2H");
-    SCUDA(s, cudaStreamSynchronize(s->stream), "grads");
-    if (loss) *loss = l;
-    return gemm_status(s);
-}
-
-}  // extern "C"
-
-// ---------------------------------------------------------------------------
-// training, pricing, checkpoints
-// ---------------------------------------------------------------------------
-namespace {
-
-struct DevBatch {  // device copy of host option records
+struct DevBatch {  // device copy of option records
     double *strike = nullptr, *bm = nullptr, *om = nullptr, *a = nullptr, *sg = nullptr;
     uint16_t *tu = nullptr, *ts = nullptr;
     int8_t *ty = nullptr;
@@ -622,15 +368,22 @@ void free_batch(DevBatch &b)
     b = DevBatch();
 }
 
-bool alloc_batch(DevBatch &b, int64_t n)
+// Grows (never shrinks) the batch to n options.
+bool grow_batch(DevBatch &b, int64_t n)
 {
+    if (n <= b.cap) return true;
     free_batch(b);
     bool ok = cudaMalloc(&b.strike, 8 * n) == cudaSuccess && cudaMalloc(&b.bm, 8 * n) == cudaSuccess &&
               cudaMalloc(&b.om, 8 * n) == cudaSuccess && cudaMalloc(&b.a, 8 * n) == cudaSuccess &&
               cudaMalloc(&b.sg, 8 * n) == cudaSuccess && cudaMalloc(&b.tu, 2 * n) == cudaSuccess &&
               cudaMalloc(&b.ts, 2 * n) == cudaSuccess && cudaMalloc(&b.ty, n) == cudaSuccess;
-    b.cap = ok ? n : 0;
-    return ok;
+    if (!ok) {
+        cudaGetLastError();
+        free_batch(b);
+        return false;
+    }
+    b.cap = n;
+    return true;
 }
 
 DevOptions dev_view(const DevBatch &b, int n)
@@ -663,44 +416,530 @@ cudaError_t upload_batch(DevBatch &b, const hwt_options *o, cudaStream_t st)
     return cudaMemcpyAsync(b.ty, o->type, n, cudaMemcpyHostToDevice, st);
 }
 
-// Device copy of a host yield curve (double rates, float rates, days).
-struct DevCurve {
-    double *rate = nullptr;
-    float *rate_f = nullptr;
-    int32_t *day = nullptr;
-    int n = 0;
+// Grow-only device buffer.
+template <typename T>
+struct Buf {
+    T *p = nullptr;
+    size_t cap = 0;
+    bool grow(size_t n)
+    {
+        if (n <= cap) return true;
+        cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        if (cudaMalloc(&p, sizeof(T) * n) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        cap = n;
+        return true;
+    }
+    void release()
+    {
+        cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
 };
 
-int upload_curve(hwt_surrogate *s, DevCurve &c, const hwt_yield *y)
+}  // namespace
+
+struct hwt_surrogate {
+    hwt_ctx *ctx = nullptr;
+    int device = 0, sms = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[4] = {};
+    hwt_box box;
+    FeatureNorm fn;
+    double ymean = 0.0, ystd = 1.0;
+    double route_tau = INFINITY;  // price error the error head's routing keeps network answers under
+    int trained = 0;
+    std::string err;
+    // parameters (fp32 masters) and Adam state, one flat buffer each
+    size_t n_params = 0;
+    float *d_w = nullptr, *d_m = nullptr, *d_v = nullptr, *d_g = nullptr;
+    size_t w_off[kLayers], b_off[kLayers];
+    __nv_bfloat16 *d_wt[kLayers] = {}, *d_wb[kLayers] = {};  // layers 1-4
+    __nv_bfloat16 *d_wp = nullptr;                           // packed blocks of layers 1-3
+    float *d_w4r = nullptr;                                  // bf16-rounded layer-4 weights
+    long adam_t = 0;
+    // training activations for one batch
+    int act_cap = 0;
+    float *d_x = nullptr;                  // [rows][8] fp32 features
+    __nv_bfloat16 *d_h[kLayers] = {};      // d_h[l] = bf16 input of layer l (l >= 1)
+    float *d_z[kLayers] = {};              // pre-activations (z[4] = outputs [rows][2])
+    __nv_bfloat16 *d_dz = nullptr, *d_dz2 = nullptr;
+    float *d_dzf = nullptr;
+    double *d_loss = nullptr;
+    float *d_y = nullptr;
+    int *d_gemm_err = nullptr;  // raised by a kernel whose mbarrier wait ran out
+    int stall = 0;              // fault injection for tests (hwt_surrogate_inject_stall)
+    // pricing buffers (grow-only)
+    DevBatch opts, sub;
+    Buf<float> xf, out2;
+    Buf<double> F, base, price, tree, errs;
+    Buf<uint8_t> inbox, kind;
+    Buf<int32_t> list, counts;
+    Buf<double> crate;
+    Buf<float> crate_f;
+    Buf<int32_t> cday;
+    std::vector<double> curve_rate;  // the curve now on the device
+    std::vector<int32_t> curve_day;
+};
+
+namespace {
+
+int sfail(hwt_surrogate *s, int code, const std::string &m)
 {
-    if (!y || y->n <= 0 || !y->rate || !y->day) return sfail(s, HWT_EINVAL, "yield curve is empty or NULL");
-    std::vector<float> rf(y->n);
-    for (int i = 0; i < y->n; ++i) rf[i] = (float)y->rate[i];
-    SCUDA(s, cudaMalloc(&c.rate, 8 * y->n), "curve alloc");
-    SCUDA(s, cudaMalloc(&c.rate_f, 4 * y->n), "curve alloc");
-    SCUDA(s, cudaMalloc(&c.day, 4 * y->n), "curve alloc");
-    SCUDA(s, cudaMemcpy(c.rate, y->rate, 8 * y->n, cudaMemcpyHostToDevice), "curve H2D");
-    SCUDA(s, cudaMemcpy(c.rate_f, rf.data(), 4 * y->n, cudaMemcpyHostToDevice), "curve H2D");
-    SCUDA(s, cudaMemcpy(c.day, y->day, 4 * y->n, cudaMemcpyHostToDevice), "curve H2D");
-    c.n = y->n;
+    s->err = m;
+    return code;
+}
+
+#define SCUDA(s, call, what)                                                                      \
+    do {                                                                                          \
+        cudaError_t e_ = (call);                                                                  \
+        if (e_ != cudaSuccess) {                                                                  \
+            cudaGetLastError();                                                                   \
+            return sfail((s), e_ == cudaErrorMemoryAllocation ? HWT_ENOMEM : HWT_ECUDA,           \
+                         std::string(what) + ": " + cudaGetErrorString(e_));                      \
+        }                                                                                         \
+    } while (0)
+
+int ensure_act(hwt_surrogate *s, int rows)
+{
+    if (rows <= s->act_cap) return HWT_OK;
+    cudaFree(s->d_x); s->d_x = nullptr;
+    for (int l = 0; l < kLayers; ++l) {
+        cudaFree(s->d_h[l]); s->d_h[l] = nullptr;
+        cudaFree(s->d_z[l]); s->d_z[l] = nullptr;
+    }
+    cudaFree(s->d_dz); cudaFree(s->d_dz2); cudaFree(s->d_dzf); cudaFree(s->d_y);
+    s->d_dz = s->d_dz2 = nullptr; s->d_dzf = nullptr; s->d_y = nullptr;
+    s->act_cap = 0;
+    SCUDA(s, cudaMalloc(&s->d_x, sizeof(float) * (size_t)rows * kInPad), "alloc X");
+    for (int l = 1; l < kLayers; ++l) SCUDA(s, cudaMalloc(&s->d_h[l], sizeof(__nv_bfloat16) * (size_t)rows * kHidden), "alloc H");
+    for (int l = 0; l < kLayers; ++l) SCUDA(s, cudaMalloc(&s->d_z[l], sizeof(float) * (size_t)rows * kFanOut[l]), "alloc Z");
+    SCUDA(s, cudaMalloc(&s->d_dz, sizeof(__nv_bfloat16) * (size_t)rows * kHidden), "alloc dZ");
+    SCUDA(s, cudaMalloc(&s->d_dz2, sizeof(__nv_bfloat16) * (size_t)rows * kHidden), "alloc dZ");
+    SCUDA(s, cudaMalloc(&s->d_dzf, sizeof(float) * (size_t)rows * kHidden), "alloc dZf");
+    SCUDA(s, cudaMalloc(&s->d_y, sizeof(float) * (size_t)rows), "alloc y");
+    s->act_cap = rows;
     return HWT_OK;
 }
 
-void free_curve(DevCurve &c)
+template <bool TA, bool TB, int BN>
+cudaError_t gemm_bn(const GemmArgs &a, int splits, cudaStream_t st)
 {
-    cudaFree(c.rate); cudaFree(c.rate_f); cudaFree(c.day);
-    c = DevCurve();
+    auto kern = umma_gemm_kernel<TA, TB, BN>;
+    dim3 grid((a.N + BN - 1) / BN, (a.M + BM - 1) / BM, splits);
+    kern<<<grid, THREADS, smem_bytes(BN), st>>>(a);
+    return cudaGetLastError();
 }
 
-// Forward pass of `rows` samples whose bf16 features start at X (row stride kInPad).
-int forward_from(hwt_surrogate *s, const __nv_bfloat16 *X, int rows)
+// Dynamic shared memory above 48 KB for every kernel that needs it, once at set-up
+// (outside any stream capture).
+cudaError_t kernel_attributes()
 {
-    __nv_bfloat16 *keep = s->d_h[0];
-    s->d_h[0] = const_cast<__nv_bfloat16 *>(X);
-    const int r = forward(s, rows);
-    s->d_h[0] = keep;
-    return r;
+    cudaError_t e = cudaSuccess;
+    auto set = [&](auto kern, int bytes) {
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    };
+    set(umma_gemm_kernel<false, false, 16>, smem_bytes(16));
+    set(umma_gemm_kernel<false, false, 64>, smem_bytes(64));
+    set(umma_gemm_kernel<false, false, 128>, smem_bytes(128));
+    set(umma_gemm_kernel<true, true, 16>, smem_bytes(16));
+    set(umma_gemm_kernel<true, true, 64>, smem_bytes(64));
+    set(umma_gemm_kernel<true, true, 128>, smem_bytes(128));
+    set(mlp::mlp_forward_kernel, mlp::kSmemBytes);
+    return e;
 }
+
+// Tile width: the output width rounded up to 16 (one tile for the 2-wide output
+// layer), at most 128 so that a 256-wide layer spreads over two column tiles.
+template <bool TA, bool TB>
+cudaError_t gemm(const GemmArgs &a, int splits, cudaStream_t st)
+{
+    if (a.N <= 16) return gemm_bn<TA, TB, 16>(a, splits, st);
+    if (a.N <= 64) return gemm_bn<TA, TB, 64>(a, splits, st);
+    return gemm_bn<TA, TB, 128>(a, splits, st);
+}
+
+GemmArgs gargs(const hwt_surrogate *s, const __nv_bfloat16 *A, const __nv_bfloat16 *B, int M, int N, int K, int lda,
+               int ldb, int epi)
+{
+    GemmArgs g;
+    memset(&g, 0, sizeof(g));
+    g.A = A; g.B = B; g.M = M; g.N = N; g.K = K; g.lda = lda; g.ldb = ldb; g.epi = epi;
+    g.k_chunk = (K + BK - 1) / BK * BK;
+    g.err = s->d_gemm_err;
+    g.test_stall = s->stall;
+    return g;
+}
+
+// HWT_ETIMEOUT (and the flag cleared) if a tensor-core kernel gave up waiting since
+// the last check.
+int gemm_status(hwt_surrogate *s)
+{
+    int flag = 0;
+    SCUDA(s, cudaMemcpy(&flag, s->d_gemm_err, sizeof(int), cudaMemcpyDeviceToHost), "tensor-core status");
+    if (flag == 0) return HWT_OK;
+    SCUDA(s, cudaMemset(s->d_gemm_err, 0, sizeof(int)), "tensor-core status");
+    return sfail(s, HWT_ETIMEOUT, "tensor-core kernel: an mbarrier wait ran out");
+}
+
+// Layer-by-layer forward (the training path) for `rows` samples in d_x; outputs in
+// d_z[4] ([rows][2]).
+int forward_layers(hwt_surrogate *s, int rows)
+{
+    layer0_kernel<<<(rows * 32 + 255) / 256, 256, 0, s->stream>>>(s->d_x, s->d_w + s->w_off[0], s->d_w + s->b_off[0],
+                                                                  rows, s->d_z[0], s->d_h[1]);
+    SCUDA(s, cudaGetLastError(), "layer 0");
+    for (int l = 1; l < kLayers; ++l) {
+        const bool last = l == kLayers - 1;
+        GemmArgs g = gargs(s, s->d_h[l], s->d_wt[l], rows, kFanOut[l], kFanIn[l], kFanIn[l], kFanIn[l],
+                           last ? EPI_BIAS : EPI_BIAS_SILU);
+        g.bias = s->d_w + s->b_off[l];
+        g.Cf = s->d_z[l];
+        g.ldc = kFanOut[l];
+        g.Cb = last ? nullptr : s->d_h[l + 1];
+        g.ldcb = kFanOut[l];
+        SCUDA(s, (gemm<false, false>(g, 1, s->stream)), "forward gemm");
+    }
+    return HWT_OK;
+}
+
+// Fused forward of `rows` samples (fp32 features X) into out [rows][2].
+int forward_fused(hwt_surrogate *s, const float *X, int rows, float *out)
+{
+    if (rows <= 0) return HWT_OK;
+    mlp::MlpArgs a;
+    a.X = X;
+    a.n = rows;
+    a.W0 = s->d_w + s->w_off[0];
+    a.b0 = s->d_w + s->b_off[0];
+    a.Wp = s->d_wp;
+    a.b1 = s->d_w + s->b_off[1];
+    a.b2 = s->d_w + s->b_off[2];
+    a.b3 = s->d_w + s->b_off[3];
+    a.W4r = s->d_w4r;
+    a.b4 = s->d_w + s->b_off[4];
+    a.out = out;
+    a.err = s->d_gemm_err;
+    a.test_stall = s->stall;
+    const int tiles = (rows + mlp::kRows - 1) / mlp::kRows;
+    const int grid = std::min(tiles, 2 * s->sms);
+    mlp::mlp_forward_kernel<<<grid, mlp::kThreads, mlp::kSmemBytes, s->stream>>>(a);
+    SCUDA(s, cudaGetLastError(), "fused network kernel");
+    return HWT_OK;
+}
+
+// Loss and gradients (into d_g) for `rows` samples in d_x with targets d_y.
+int backward(hwt_surrogate *s, int rows, float lam, bool zero_loss)
+{
+    SCUDA(s, cudaMemsetAsync(s->d_g, 0, sizeof(float) * s->n_params, s->stream), "zero grads");
+    if (zero_loss) SCUDA(s, cudaMemsetAsync(s->d_loss, 0, sizeof(double), s->stream), "zero loss");
+    loss_kernel<<<(rows + 255) / 256, 256, 0, s->stream>>>(s->d_z[kLayers - 1], s->d_y, rows, lam, s->d_dz, s->d_dzf,
+                                                           s->d_loss);
+    SCUDA(s, cudaGetLastError(), "loss kernel");
+    __nv_bfloat16 *dz = s->d_dz, *dz_next = s->d_dz2;
+    const int splits = std::max(1, std::min(64, rows / 512));
+    int kc = (rows + splits - 1) / splits;
+    kc = (kc + BK - 1) / BK * BK;
+    for (int l = kLayers - 1; l >= 1; --l) {
+        const int in = kFanIn[l], out = kFanOut[l];
+        // dW_l[in][out] = H_l^T dZ_l   (split-K over the batch)
+        GemmArgs gw = gargs(s, s->d_h[l], dz, in, out, rows, in, out, EPI_ATOMIC);
+        gw.Cf = s->d_g + s->w_off[l];
+        gw.ldc = out;
+        gw.k_chunk = kc;
+        SCUDA(s, (gemm<true, true>(gw, (rows + kc - 1) / kc, s->stream)), "dW gemm");
+        // db_l = column sums of dZ_l (fp32 copy in d_dzf)
+        dim3 cg((out + 255) / 256, std::max(1, std::min(256, rows / 32)));
+        colsum_kernel<<<cg, 256, 0, s->stream>>>(s->d_dzf, rows, out, out, s->d_g + s->b_off[l]);
+        SCUDA(s, cudaGetLastError(), "db kernel");
+        // dZ_{l-1} = (dZ_l W_l^T) * silu'(Z_{l-1})
+        GemmArgs gd = gargs(s, dz, s->d_wb[l], rows, in, out, out, out, EPI_DSILU);
+        gd.Zin = s->d_z[l - 1];
+        gd.Cf = s->d_dzf;
+        gd.ldc = in;
+        gd.Cb = dz_next;
+        gd.ldcb = in;
+        SCUDA(s, (gemm<false, false>(gd, 1, s->stream)), "dX gemm");
+        std::swap(dz, dz_next);
+    }
+    // layer 0 in fp32: dW0 = X^T dZ0, db0 = column sums of dZ0
+    dw0_kernel<<<std::max(1, std::min(256, rows / 32)), kHidden, 0, s->stream>>>(s->d_x, s->d_dzf, rows,
+                                                                                 s->d_g + s->w_off[0]);
+    SCUDA(s, cudaGetLastError(), "dW0 kernel");
+    dim3 cg(1, std::max(1, std::min(256, rows / 32)));
+    colsum_kernel<<<cg, 256, 0, s->stream>>>(s->d_dzf, rows, kHidden, kHidden, s->d_g + s->b_off[0]);
+    SCUDA(s, cudaGetLastError(), "db0 kernel");
+    return HWT_OK;
+}
+
+int refresh(hwt_surrogate *s)
+{
+    for (int l = 1; l < kLayers; ++l) {
+        const int tot = kFanIn[l] * kFanOut[l];
+        __nv_bfloat16 *wp = l <= mlp::kTcLayers ? s->d_wp + (size_t)(l - 1) * mlp::kBlocksPerLayer * mlp::kWBlockElems : nullptr;
+        refresh_kernel<<<(tot + 255) / 256, 256, 0, s->stream>>>(s->d_w + s->w_off[l], kFanIn[l], kFanOut[l], s->d_wt[l],
+                                                               s->d_wb[l], wp, l == kLayers - 1 ? s->d_w4r : nullptr);
+        SCUDA(s, cudaGetLastError(), "refresh kernel");
+    }
+    return HWT_OK;
+}
+
+// One training step on the batch the step state names, everything from device
+// state: the body of the captured training graph.
+int train_step(hwt_surrogate *s, const float *Xs, const float *ys, StepState *st, int batch, double lr0,
+               double lr_min, long long total, float lam)
+{
+    step_begin_kernel<<<1, 1, 0, s->stream>>>(st, lr0, lr_min, total);
+    SCUDA(s, cudaGetLastError(), "step kernel");
+    batch_copy_kernel<<<(batch + 255) / 256, 256, 0, s->stream>>>(Xs, ys, st, batch, s->d_x, s->d_y);
+    SCUDA(s, cudaGetLastError(), "batch kernel");
+    int r = forward_layers(s, batch);
+    if (!r) r = backward(s, batch, lam, false);
+    if (r) return r;
+    AdamArgs a;
+    a.w = s->d_w; a.m = s->d_m; a.v = s->d_v; a.g = s->d_g; a.n = (int)s->n_params;
+    a.lr = 0.f; a.b1 = 0.9f; a.b2 = 0.999f; a.eps = 1e-8f; a.c1 = 1.f; a.c2 = 1.f;
+    adam_kernel<<<((int)s->n_params + 255) / 256, 256, 0, s->stream>>>(a, st);
+    SCUDA(s, cudaGetLastError(), "adam kernel");
+    return refresh(s);
+}
+
+// Mean and 1 / std of a uniform variable on [lo, hi]; a dimension the box pins to
+// one value gets inv_std 0 (its feature is 0 inside the box).
+void box_norm(const hwt_box &b, FeatureNorm &fn)
+{
+    const double lo[kIn] = {b.t_min, b.t_min + b.span_min, b.moneyness_min, b.a_min, b.sigma_min, (double)b.steps_min, 0.0};
+    const double hi[kIn] = {b.t_max, b.t_max + b.span_max, b.moneyness_max, b.a_max, b.sigma_max, (double)b.steps_max, 1.0};
+    for (int q = 0; q < kIn; ++q) {
+        const double w = hi[q] - lo[q];
+        fn.mean[q] = 0.5 * (lo[q] + hi[q]);
+        fn.inv_std[q] = w > 1e-12 ? sqrt(12.0) / w : 0.0;
+    }
+}
+
+int upload_curve(hwt_surrogate *s, const hwt_yield *y, DevYield &yc)
+{
+    if (!y || y->n <= 0 || !y->rate || !y->day) return sfail(s, HWT_EINVAL, "yield curve is empty or NULL");
+    if (y->n > kMaxCurve) return sfail(s, HWT_EINVAL, "yield curve has more than 4096 nodes");
+    for (int i = 0; i < y->n; ++i)
+        if (!std::isfinite(y->rate[i])) return sfail(s, HWT_EINVAL, "yield curve rate is not finite");
+    if (!s->crate.grow(kMaxCurve) || !s->crate_f.grow(kMaxCurve) || !s->cday.grow(kMaxCurve))
+        return sfail(s, HWT_ENOMEM, "curve buffers");
+    const bool same = (int)s->curve_rate.size() == y->n && memcmp(s->curve_rate.data(), y->rate, 8 * y->n) == 0 &&
+                      memcmp(s->curve_day.data(), y->day, 4 * y->n) == 0;
+    if (!same) {
+        std::vector<float> rf(y->n);
+        for (int i = 0; i < y->n; ++i) rf[i] = (float)y->rate[i];
+        SCUDA(s, cudaStreamSynchronize(s->stream), "curve");  // no kernel may still read the old curve
+        SCUDA(s, cudaMemcpy(s->crate.p, y->rate, 8 * y->n, cudaMemcpyHostToDevice), "curve H2D");
+        SCUDA(s, cudaMemcpy(s->crate_f.p, rf.data(), 4 * y->n, cudaMemcpyHostToDevice), "curve H2D");
+        SCUDA(s, cudaMemcpy(s->cday.p, y->day, 4 * y->n, cudaMemcpyHostToDevice), "curve H2D");
+        s->curve_rate.assign(y->rate, y->rate + y->n);
+        s->curve_day.assign(y->day, y->day + y->n);
+    }
+    yc.n = y->n;
+    yc.rate = s->crate.p;
+    yc.rate_f = s->crate_f.p;
+    yc.day = s->cday.p;
+    return HWT_OK;
+}
+
+// Standardised host features x [n][7] into the training input buffer (fp32, padded).
+int upload_features(hwt_surrogate *s, const float *x, int n)
+{
+    int r = ensure_act(s, n);
+    if (r) return r;
+    std::vector<float> xp((size_t)n * kInPad, 0.f);
+    for (int i = 0; i < n; ++i)
+        for (int q = 0; q < kIn; ++q) xp[(size_t)i * kInPad + q] = x[(size_t)i * kIn + q];
+    SCUDA(s, cudaMemcpy(s->d_x, xp.data(), 4 * xp.size(), cudaMemcpyHostToDevice), "x H2D");
+    return HWT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+hwt_surrogate *hwt_surrogate_create(hwt_ctx *ctx, const hwt_box *box, uint64_t seed)
+{
+    if (!ctx || !box) return nullptr;
+    hwt_surrogate *s = new hwt_surrogate();
+    s->ctx = ctx;
+    s->box = *box;
+    box_norm(*box, s->fn);
+    cudaGetDevice(&s->device);
+    cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, s->device);
+    bool ok = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) == cudaSuccess;
+    for (auto &e : s->ev) ok = ok && cudaEventCreate(&e) == cudaSuccess;
+    size_t off = 0;
+    for (int l = 0; l < kLayers; ++l) {  // every block starts on a 16-byte boundary
+        s->w_off[l] = off; off += ((size_t)kFanIn[l] * kFanOut[l] + 3) / 4 * 4;
+        s->b_off[l] = off; off += ((size_t)kFanOut[l] + 3) / 4 * 4;
+    }
+    s->n_params = off;
+    ok = ok && cudaMalloc(&s->d_w, 4 * off) == cudaSuccess && cudaMalloc(&s->d_m, 4 * off) == cudaSuccess &&
+         cudaMalloc(&s->d_v, 4 * off) == cudaSuccess && cudaMalloc(&s->d_g, 4 * off) == cudaSuccess &&
+         cudaMalloc(&s->d_loss, sizeof(double)) == cudaSuccess &&
+         cudaMalloc(&s->d_gemm_err, sizeof(int)) == cudaSuccess && cudaMemset(s->d_gemm_err, 0, sizeof(int)) == cudaSuccess &&
+         cudaMalloc(&s->d_wp, 2ull * mlp::kBlocks * mlp::kWBlockElems) == cudaSuccess &&
+         cudaMalloc(&s->d_w4r, 4ull * kHidden * kOut) == cudaSuccess;
+    for (int l = 1; l < kLayers && ok; ++l) {
+        ok = cudaMalloc(&s->d_wt[l], 2 * (size_t)kFanIn[l] * kFanOut[l]) == cudaSuccess &&
+             cudaMalloc(&s->d_wb[l], 2 * (size_t)kFanIn[l] * kFanOut[l]) == cudaSuccess;
+    }
+    if (ok) {
+        // He initialisation from a seeded host generator (splitmix64 + Box-Muller);
+        // the zero pad row of layer 0 and the padding words stay zero
+        std::vector<float> w(off, 0.f);
+        unsigned long long st = seed ? seed : 0x1234567ull;
+        auto next = [&]() {
+            st += 0x9e3779b97f4a7c15ull;
+            unsigned long long z = st;
+            z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+            z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+            return (double)((z ^ (z >> 31)) >> 11) * (1.0 / 9007199254740992.0);
+        };
+        for (int l = 0; l < kLayers; ++l) {
+            const int in = l == 0 ? kIn : kFanIn[l];
+            const double sd = sqrt(2.0 / in) * (l == kLayers - 1 ? 0.1 : 1.0);
+            for (int k = 0; k < in; ++k)
+                for (int n = 0; n < kFanOut[l]; ++n) {
+                    const double u1 = std::max(next(), 1e-300), u2 = next();
+                    w[s->w_off[l] + (size_t)k * kFanOut[l] + n] = (float)(sd * sqrt(-2.0 * log(u1)) * cos(6.283185307179586 * u2));
+                }
+        }
+        ok = cudaMemcpy(s->d_w, w.data(), 4 * off, cudaMemcpyHostToDevice) == cudaSuccess &&
+             cudaMemset(s->d_m, 0, 4 * off) == cudaSuccess && cudaMemset(s->d_v, 0, 4 * off) == cudaSuccess;
+        ok = ok && kernel_attributes() == cudaSuccess;
+        ok = ok && refresh(s) == HWT_OK && cudaStreamSynchronize(s->stream) == cudaSuccess;
+    }
+    if (!ok) {
+        cudaGetLastError();
+        hwt_surrogate_destroy(s);
+        return nullptr;
+    }
+    return s;
+}
+
+void hwt_surrogate_destroy(hwt_surrogate *s)
+{
+    if (!s) return;
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    cudaFree(s->d_w); cudaFree(s->d_m); cudaFree(s->d_v); cudaFree(s->d_g); cudaFree(s->d_loss); cudaFree(s->d_gemm_err);
+    cudaFree(s->d_wp); cudaFree(s->d_w4r); cudaFree(s->d_x);
+    for (int l = 0; l < kLayers; ++l) { cudaFree(s->d_wt[l]); cudaFree(s->d_wb[l]); cudaFree(s->d_z[l]); cudaFree(s->d_h[l]); }
+    cudaFree(s->d_dz); cudaFree(s->d_dz2); cudaFree(s->d_dzf); cudaFree(s->d_y);
+    free_batch(s->opts);
+    free_batch(s->sub);
+    s->xf.release(); s->out2.release(); s->F.release(); s->base.release(); s->price.release(); s->tree.release();
+    s->errs.release(); s->inbox.release(); s->kind.release(); s->list.release(); s->counts.release();
+    s->crate.release(); s->crate_f.release(); s->cday.release();
+    for (auto &e : s->ev)
+        if (e) cudaEventDestroy(e);
+    if (s->stream) cudaStreamDestroy(s->stream);
+    delete s;
+}
+
+const char *hwt_surrogate_last_error(const hwt_surrogate *s) { return s ? s->err.c_str() : "no surrogate"; }
+
+int hwt_surrogate_inject_stall(hwt_surrogate *s, int mode)
+{
+    if (!s || mode < 0 || mode > 2) return HWT_EINVAL;
+    s->stall = mode;
+    return HWT_OK;
+}
+
+int64_t hwt_surrogate_param_count(const hwt_surrogate *s)
+{
+    if (!s) return 0;
+    int64_t n = 0;
+    for (int l = 0; l < kLayers; ++l) n += (int64_t)kFanIn[l] * kFanOut[l] + kFanOut[l];
+    return n;
+}
+
+// Parameters in the flat layout [W_0, b_0, ..., W_4, b_4] (no padding words).
+int hwt_surrogate_params(hwt_surrogate *s, float *buf, int64_t n, int set)
+{
+    if (!s || !buf || n != hwt_surrogate_param_count(s)) return HWT_EINVAL;
+    std::vector<float> w(s->n_params, 0.f);
+    if (!set) SCUDA(s, cudaMemcpy(w.data(), s->d_w, 4 * s->n_params, cudaMemcpyDeviceToHost), "get params");
+    size_t q = 0;
+    for (int l = 0; l < kLayers; ++l) {
+        const size_t nw = (size_t)kFanIn[l] * kFanOut[l], nb = kFanOut[l];
+        for (size_t i = 0; i < nw + nb; ++i, ++q) {
+            float &dst = w[(i < nw ? s->w_off[l] + i : s->b_off[l] + (i - nw))];
+            if (set) dst = buf[q];
+            else buf[q] = dst;
+        }
+    }
+    if (set) {
+        SCUDA(s, cudaMemcpy(s->d_w, w.data(), 4 * s->n_params, cudaMemcpyHostToDevice), "set params");
+        int r = refresh(s);
+        if (r) return r;
+        SCUDA(s, cudaStreamSynchronize(s->stream), "refresh");
+    }
+    return HWT_OK;
+}
+
+int hwt_surrogate_forward_ex(hwt_surrogate *s, const float *x, int n, float *out, int path)
+{
+    if (!s || !x || !out || n <= 0 || (path != 0 && path != 1)) return HWT_EINVAL;
+    int r = upload_features(s, x, n);
+    if (r) return r;
+    if (path == 0) {
+        if (!s->out2.grow((size_t)n * kOut)) return sfail(s, HWT_ENOMEM, "output buffer");
+        if ((r = forward_fused(s, s->d_x, n, s->out2.p))) return r;
+        SCUDA(s, cudaMemcpyAsync(out, s->out2.p, 4ull * n * kOut, cudaMemcpyDeviceToHost, s->stream), "out D2H");
+    } else {
+        if ((r = forward_layers(s, n))) return r;
+        SCUDA(s, cudaMemcpyAsync(out, s->d_z[kLayers - 1], 4ull * n * kOut, cudaMemcpyDeviceToHost, s->stream), "out D2H");
+    }
+    SCUDA(s, cudaStreamSynchronize(s->stream), "forward");
+    return gemm_status(s);
+}
+
+int hwt_surrogate_forward(hwt_surrogate *s, const float *x, int n, float *out)
+{
+    return hwt_surrogate_forward_ex(s, x, n, out, 0);
+}
+
+int hwt_surrogate_loss_grads(hwt_surrogate *s, const float *x, const float *y, int n, double err_weight, double *loss,
+                             float *grads)
+{
+    if (!s || !x || !y || n <= 0) return HWT_EINVAL;
+    int r = upload_features(s, x, n);
+    if (r) return r;
+    SCUDA(s, cudaMemcpy(s->d_y, y, 4 * (size_t)n, cudaMemcpyHostToDevice), "y H2D");
+    if ((r = forward_layers(s, n))) return r;
+    if ((r = backward(s, n, (float)err_weight, true))) return r;
+    std::vector<float> g(s->n_params);
+    double l = 0;
+    SCUDA(s, cudaMemcpyAsync(g.data(), s->d_g, 4 * s->n_params, cudaMemcpyDeviceToHost, s->stream), "grads D2H");
+    SCUDA(s, cudaMemcpyAsync(&l, s->d_loss, sizeof(double), cudaMemcpyDeviceToHost, s->stream), "loss D2H");
+    SCUDA(s, cudaStreamSynchronize(s->stream), "grads");
+    if (loss) *loss = l;
+    if (grads) {
+        size_t q = 0;
+        for (int lyr = 0; lyr < kLayers; ++lyr) {
+            const size_t nw = (size_t)kFanIn[lyr] * kFanOut[lyr], nb = kFanOut[lyr];
+            for (size_t i = 0; i < nw; ++i) grads[q++] = g[s->w_off[lyr] + i];
+            for (size_t i = 0; i < nb; ++i) grads[q++] = g[s->b_off[lyr] + i];
+        }
+    }
+    return gemm_status(s);
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// training, pricing, checkpoints
+// ---------------------------------------------------------------------------
+namespace {
 
 struct Scoped {
     std::vector<void *> ptrs;
@@ -709,6 +948,63 @@ struct Scoped {
         for (void *p : ptrs) cudaFree(p);
     }
 };
+
+// Features, forward prices and closed-form bases of the host options into the
+// surrogate's pricing buffers (options copied to s->opts).
+int features_for(hwt_surrogate *s, const hwt_options *o, const hwt_yield *y)
+{
+    const int n = o->n;
+    DevYield yc;
+    int r = upload_curve(s, y, yc);
+    if (r) return r;
+    if (!grow_batch(s->opts, n) || !s->xf.grow((size_t)n * kInPad) || !s->F.grow(n) || !s->base.grow(n) ||
+        !s->inbox.grow(n))
+        return sfail(s, HWT_ENOMEM, "pricing buffers");
+    SCUDA(s, upload_batch(s->opts, o, s->stream), "options H2D");
+    features_kernel<<<(n + 255) / 256, 256, 0, s->stream>>>(dev_view(s->opts, n), yc, s->box, s->fn, s->xf.p, s->F.p,
+                                                           s->base.p, s->inbox.p);
+    SCUDA(s, cudaGetLastError(), "features kernel");
+    return HWT_OK;
+}
+
+// Router threshold from held-out samples: the largest predicted error tau such that
+// every held-out sample the network would answer (predicted <= tau) has a true
+// error <= tol.  pred and err in price units.
+double calibrate_tau(const std::vector<double> &pred, const std::vector<double> &err, double tol, double *answered,
+                     double *max_answered, double *p99_answered)
+{
+    const size_t n = pred.size();
+    std::vector<size_t> idx(n);
+    for (size_t i = 0; i < n; ++i) idx[i] = i;
+    std::sort(idx.begin(), idx.end(), [&](size_t a, size_t b) { return pred[a] < pred[b]; });
+    size_t k = 0;  // answered: idx[0..k)
+    double run = 0.0;
+    while (k < n) {
+        const double e = err[idx[k]];
+        if (!(e <= tol)) break;
+        run = std::max(run, e);
+        ++k;
+    }
+    // ties: a threshold equal to the next prediction would also admit it
+    while (k > 0 && k < n && pred[idx[k]] == pred[idx[k - 1]]) --k;
+    double tau = k == 0 ? -1.0 : pred[idx[k - 1]];
+    std::vector<double> ea;
+    ea.reserve(k);
+    run = 0.0;
+    for (size_t i = 0; i < k; ++i) {
+        ea.push_back(err[idx[i]]);
+        run = std::max(run, err[idx[i]]);
+    }
+    *answered = n ? (double)k / n : 0.0;
+    *max_answered = run;
+    if (!ea.empty()) {
+        std::sort(ea.begin(), ea.end());
+        *p99_answered = ea[std::min(ea.size() - 1, (size_t)floor(0.99 * (ea.size() - 1)))];
+    } else {
+        *p99_answered = 0.0;
+    }
+    return tau;
+}
 
 }  // namespace
 
@@ -721,11 +1017,11 @@ int hwt_surrogate_train(hwt_surrogate *s, const hwt_options *samples, const hwt_
     const int n = samples->n;
     const int batch = cfg->batch > 0 ? cfg->batch : 8192;
     const int epochs = cfg->epochs > 0 ? cfg->epochs : 1;
+    const float lam = (float)std::max(cfg->err_weight, 0.0);
+    const double holdout = cfg->holdout > 0 ? std::min(cfg->holdout, 0.5) : 0.05;
+    const double route_tol = cfg->route_tolerance > 0 ? cfg->route_tolerance : 1e-4;
     if (n < batch) return sfail(s, HWT_EINVAL, "fewer samples than one batch");
     if (stats) memset(stats, 0, sizeof(*stats));
-    cudaEvent_t e0, e1;
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
 
     // 1. labels from the FP64 batched tree
     std::vector<double> price(n);
@@ -738,57 +1034,16 @@ int hwt_surrogate_train(hwt_surrogate *s, const hwt_options *samples, const hwt_
     if (r) return sfail(s, r, std::string("labelling with the tree failed: ") + hwt_last_error(s->ctx));
 
     // 2. features and targets on the device
-    DevBatch b;
-    if (!alloc_batch(b, n)) {
-        free_batch(b);
-        return sfail(s, HWT_ENOMEM, "sample buffers");
-    }
-    DevCurve cv;
-    Scoped guard;
-    if ((r = upload_curve(s, cv, y))) { free_batch(b); return r; }
-    __nv_bfloat16 *X = nullptr, *Xs = nullptr;
-    double *F = nullptr, *dprice = nullptr, *base = nullptr;
-    uint8_t *inbox = nullptr;
-    float *yv = nullptr, *ys = nullptr;
-    int32_t *perm = nullptr;
-    bool ok = cudaMalloc(&X, 2ull * n * kInPad) == cudaSuccess && cudaMalloc(&Xs, 2ull * n * kInPad) == cudaSuccess &&
-              cudaMalloc(&F, 8ull * n) == cudaSuccess && cudaMalloc(&dprice, 8ull * n) == cudaSuccess &&
-              cudaMalloc(&base, 8ull * n) == cudaSuccess &&
-              cudaMalloc(&inbox, n) == cudaSuccess && cudaMalloc(&yv, 4ull * n) == cudaSuccess &&
-              cudaMalloc(&ys, 4ull * n) == cudaSuccess && cudaMalloc(&perm, 4ull * n) == cudaSuccess;
-    guard.ptrs = {X, Xs, F, dprice, base, inbox, yv, ys, perm};
-    if (!ok) { free_batch(b); free_curve(cv); return sfail(s, HWT_ENOMEM, "training buffers"); }
-    if (upload_batch(b, samples, s->stream) != cudaSuccess) { free_batch(b); free_curve(cv); return sfail(s, HWT_ECUDA, "samples H2D"); }
-    DevYield yc;
-    yc.n = cv.n; yc.rate = cv.rate; yc.rate_f = cv.rate_f; yc.day = cv.day;
-    features_kernel<<<(n + 255) / 256, 256, 0, s->stream>>>(dev_view(b, n), yc, s->box, s->fn, X, F, base, inbox);
+    if ((r = features_for(s, samples, y))) return r;
     std::vector<double> Fh(n), bh(n);
     std::vector<uint8_t> ib(n);
-    cudaMemcpyAsync(Fh.data(), F, 8ull * n, cudaMemcpyDeviceToHost, s->stream);
-    cudaMemcpyAsync(bh.data(), base, 8ull * n, cudaMemcpyDeviceToHost, s->stream);
-    cudaMemcpyAsync(ib.data(), inbox, n, cudaMemcpyDeviceToHost, s->stream);
-    cudaError_t ce = cudaStreamSynchronize(s->stream);
-    free_batch(b);
-    free_curve(cv);
-    if (ce != cudaSuccess) return sfail(s, HWT_ECUDA, std::string("features: ") + cudaGetErrorString(ce));
-    double sum = 0, sum2 = 0;
-    int64_t nin = 0;
-    for (int i = 0; i < n; ++i) {
-        if (!ib[i]) continue;
-        const double v = (price[i] - bh[i]) / Fh[i];
-        sum += v; sum2 += v * v; ++nin;
-    }
-    if (nin < batch) return sfail(s, HWT_EINVAL, "fewer in-box samples than one batch");
-    s->ymean = sum / nin;
-    s->ystd = std::max(sqrt(std::max(sum2 / nin - s->ymean * s->ymean, 0.0)), 1e-12);
-    SCUDA(s, cudaMemcpyAsync(dprice, price.data(), 8ull * n, cudaMemcpyHostToDevice, s->stream), "prices H2D");
-    targets_kernel<<<(n + 255) / 256, 256, 0, s->stream>>>(dprice, F, base, n, s->ymean, 1.0 / s->ystd, yv);
-    SCUDA(s, cudaGetLastError(), "targets");
-    if ((r = ensure_act(s, batch))) return r;
-
-    // 3. Adam with cosine decay over the in-box samples, reshuffled every epoch
+    SCUDA(s, cudaMemcpyAsync(Fh.data(), s->F.p, 8ull * n, cudaMemcpyDeviceToHost, s->stream), "F D2H");
+    SCUDA(s, cudaMemcpyAsync(bh.data(), s->base.p, 8ull * n, cudaMemcpyDeviceToHost, s->stream), "base D2H");
+    SCUDA(s, cudaMemcpyAsync(ib.data(), s->inbox.p, n, cudaMemcpyDeviceToHost, s->stream), "box D2H");
+    SCUDA(s, cudaStreamSynchronize(s->stream), "features");
+    // in-box samples, shuffled once and split into training and held-out parts
     std::vector<int32_t> idx;
-    idx.reserve(nin);
+    idx.reserve(n);
     for (int i = 0; i < n; ++i)
         if (ib[i]) idx.push_back(i);
     unsigned long long rs = cfg->seed ? cfg->seed : 7ull;
@@ -799,21 +1054,51 @@ int hwt_surrogate_train(hwt_surrogate *s, const hwt_options *samples, const hwt_
         z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
         return z ^ (z >> 31);
     };
-    const int steps_per_epoch = (int)(nin / batch);
+    for (int64_t i = (int64_t)idx.size() - 1; i > 0; --i) std::swap(idx[i], idx[rnd() % (unsigned long long)(i + 1)]);
+    const int64_t nin = (int64_t)idx.size();
+    const int64_t nhold = (int64_t)(holdout * nin);
+    const int64_t ntrain = nin - nhold;
+    if (ntrain < batch) return sfail(s, HWT_EINVAL, "fewer in-box training samples than one batch");
+    double sum = 0, sum2 = 0;
+    for (int64_t j = 0; j < ntrain; ++j) {
+        const int i = idx[j];
+        const double v = (price[i] - bh[i]) / Fh[i];
+        sum += v; sum2 += v * v;
+    }
+    s->ymean = sum / ntrain;
+    s->ystd = std::max(sqrt(std::max(sum2 / ntrain - s->ymean * s->ymean, 0.0)), 1e-12);
+
+    Scoped guard;
+    float *yv = nullptr, *Xs = nullptr, *ys = nullptr;
+    double *dprice = nullptr;
+    int32_t *perm = nullptr;
+    StepState *dstate = nullptr;
+    bool ok = cudaMalloc(&yv, 4ull * n) == cudaSuccess && cudaMalloc(&Xs, 4ull * kInPad * nin) == cudaSuccess &&
+              cudaMalloc(&ys, 4ull * nin) == cudaSuccess && cudaMalloc(&dprice, 8ull * n) == cudaSuccess &&
+              cudaMalloc(&perm, 4ull * nin) == cudaSuccess && cudaMalloc(&dstate, sizeof(StepState)) == cudaSuccess;
+    guard.ptrs = {yv, Xs, ys, dprice, perm, dstate};
+    if (!ok) {
+        cudaGetLastError();
+        return sfail(s, HWT_ENOMEM, "training buffers");
+    }
+    SCUDA(s, cudaMemcpyAsync(dprice, price.data(), 8ull * n, cudaMemcpyHostToDevice, s->stream), "prices H2D");
+    targets_kernel<<<(n + 255) / 256, 256, 0, s->stream>>>(dprice, s->F.p, s->base.p, n, s->ymean, 1.0 / s->ystd, yv);
+    SCUDA(s, cudaGetLastError(), "targets");
+    if ((r = ensure_act(s, batch))) return r;
+
+    // 3. Adam with cosine decay over the training part, reshuffled every epoch
+    const int steps_per_epoch = (int)(ntrain / batch);
     const long total = (long)steps_per_epoch * epochs;
     const double lr0 = cfg->lr > 0 ? cfg->lr : 1e-3, lr_min = cfg->lr_min;
     long step = 0;
     double last_epoch_loss = 0;
-    // one training step captured as a CUDA graph (about 30 kernels), replayed per step
-    StepState *dstate = nullptr;
-    SCUDA(s, cudaMalloc(&dstate, sizeof(StepState)), "step state");
-    guard.ptrs.push_back(dstate);
     {
         StepState h;
         memset(&h, 0, sizeof(h));
         h.t = s->adam_t;
         SCUDA(s, cudaMemcpy(dstate, &h, sizeof(h), cudaMemcpyHostToDevice), "step state H2D");
     }
+    // one training step captured as a CUDA graph (about 30 kernels), replayed per step
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
     struct GraphGuard {
@@ -826,19 +1111,20 @@ int hwt_surrogate_train(hwt_surrogate *s, const hwt_options *samples, const hwt_
         }
     } gguard{&graph, &gexec};
     SCUDA(s, cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
-    r = train_step(s, Xs, ys, dstate, batch, lr0, lr_min, (long long)total);
+    r = train_step(s, Xs, ys, dstate, batch, lr0, lr_min, (long long)total, lam);
     {
         const cudaError_t ce2 = cudaStreamEndCapture(s->stream, &graph);
         if (r) return r;
         SCUDA(s, ce2, "end capture");
     }
     SCUDA(s, cudaGraphInstantiate(&gexec, graph, 0), "instantiate training graph");
-    cudaEventRecord(e0, s->stream);
+    std::vector<int32_t> tr(idx.begin(), idx.begin() + ntrain);
+    SCUDA(s, cudaEventRecord(s->ev[0], s->stream), "event");
     for (int ep = 0; ep < epochs; ++ep) {
-        for (int64_t i = nin - 1; i > 0; --i) std::swap(idx[i], idx[rnd() % (unsigned long long)(i + 1)]);
-        SCUDA(s, cudaMemcpyAsync(perm, idx.data(), 4ull * nin, cudaMemcpyHostToDevice, s->stream), "perm H2D");
-        gather_rows_kernel<<<(int)((nin + 255) / 256), 256, 0, s->stream>>>(X, yv, perm, (int)nin, Xs, ys);
-        SCUDA(s, cudaStreamSynchronize(s->stream), "shuffle");  // perm host buffer is rewritten next epoch
+        for (int64_t i = ntrain - 1; i > 0; --i) std::swap(tr[i], tr[rnd() % (unsigned long long)(i + 1)]);
+        SCUDA(s, cudaMemcpyAsync(perm, tr.data(), 4ull * ntrain, cudaMemcpyHostToDevice, s->stream), "perm H2D");
+        gather_rows_kernel<<<(int)((ntrain + 255) / 256), 256, 0, s->stream>>>(s->xf.p, yv, perm, (int)ntrain, Xs, ys);
+        SCUDA(s, cudaStreamSynchronize(s->stream), "shuffle");  // tr is reshuffled next epoch
         SCUDA(s, cudaMemsetAsync(s->d_loss, 0, sizeof(double), s->stream), "zero loss");
         SCUDA(s, cudaMemsetAsync(&dstate->k, 0, sizeof(int), s->stream), "epoch start");
         for (int k = 0; k < steps_per_epoch; ++k, ++step)
@@ -848,29 +1134,67 @@ int hwt_surrogate_train(hwt_surrogate *s, const hwt_options *samples, const hwt_
         SCUDA(s, cudaStreamSynchronize(s->stream), "epoch");
         last_epoch_loss = l / steps_per_epoch;
     }
-    cudaEventRecord(e1, s->stream);
-    cudaEventSynchronize(e1);
+    SCUDA(s, cudaEventRecord(s->ev[1], s->stream), "event");
+    SCUDA(s, cudaEventSynchronize(s->ev[1]), "event");
     {
         StepState h;
         SCUDA(s, cudaMemcpy(&h, dstate, sizeof(h), cudaMemcpyDeviceToHost), "step state D2H");
         s->adam_t = (long)h.t;
     }
     float ms = 0;
-    cudaEventElapsedTime(&ms, e0, e1);
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
+    cudaEventElapsedTime(&ms, s->ev[0], s->ev[1]);
+    if ((r = gemm_status(s))) return r;
+
+    // 4. router calibration on the held-out samples with the fused network
+    double answered = 1.0, max_ans = 0.0, p99_ans = 0.0, max_all = 0.0;
+    s->route_tau = INFINITY;
+    if (nhold > 0) {
+        std::vector<int32_t> hold(idx.begin() + ntrain, idx.end());
+        if (!s->out2.grow((size_t)nhold * kOut)) return sfail(s, HWT_ENOMEM, "held-out outputs");
+        SCUDA(s, cudaMemcpyAsync(perm, hold.data(), 4ull * nhold, cudaMemcpyHostToDevice, s->stream), "perm H2D");
+        gather_rows_kernel<<<(int)((nhold + 255) / 256), 256, 0, s->stream>>>(s->xf.p, nullptr, perm, (int)nhold, Xs,
+                                                                              nullptr);
+        if ((r = forward_fused(s, Xs, (int)nhold, s->out2.p))) return r;
+        std::vector<float> o((size_t)nhold * kOut);
+        SCUDA(s, cudaMemcpyAsync(o.data(), s->out2.p, 4ull * nhold * kOut, cudaMemcpyDeviceToHost, s->stream), "D2H");
+        SCUDA(s, cudaStreamSynchronize(s->stream), "held-out forward");
+        if ((r = gemm_status(s))) return r;
+        std::vector<double> pred(nhold), err(nhold);
+        for (int64_t j = 0; j < nhold; ++j) {
+            const int i = hold[j];
+            const double net = bh[i] + Fh[i] * ((double)o[2 * j] * s->ystd + s->ymean);
+            err[j] = fabs(net - price[i]);
+            if (!(err[j] <= 1e300)) err[j] = INFINITY;
+            pred[j] = exp((double)o[2 * j + 1]) * s->ystd * Fh[i];
+            max_all = std::max(max_all, err[j]);
+        }
+        if (lam > 0) {
+            s->route_tau = calibrate_tau(pred, err, route_tol, &answered, &max_ans, &p99_ans);
+        } else {
+            std::vector<double> e = err;
+            std::sort(e.begin(), e.end());
+            max_ans = e.back();
+            p99_ans = e[std::min(e.size() - 1, (size_t)floor(0.99 * (e.size() - 1)))];
+        }
+    }
     s->trained = 1;
     if (stats) {
         stats->final_loss = last_epoch_loss;
         stats->train_ms = ms;
         stats->label_ms = ts.total_ms;
         stats->steps = step;
-        stats->samples = nin;
+        stats->samples = ntrain;
         stats->samples_per_s = (double)step * batch / (ms * 1e-3);
         stats->y_mean = s->ymean;
         stats->y_std = s->ystd;
+        stats->route_threshold = s->route_tau;
+        stats->holdout_answered = answered;
+        stats->holdout_max_abs = max_ans;
+        stats->holdout_p99_abs = p99_ans;
+        stats->holdout_all_max_abs = max_all;
+        stats->holdout = nhold;
     }
-    return gemm_status(s);
+    return HWT_OK;
 }
 
 int hwt_surrogate_price(hwt_surrogate *s, const hwt_options *o, const hwt_yield *y, double judge_fraction,
@@ -878,121 +1202,109 @@ int hwt_surrogate_price(hwt_surrogate *s, const hwt_options *o, const hwt_yield 
 {
     if (!s || !o || !y || (o->n > 0 && !out)) return HWT_EINVAL;
     if (!s->trained) return sfail(s, HWT_EINVAL, "the surrogate has not been trained or loaded");
-    if (tree_mode < HWT_BATCHED_FP64 || tree_mode > HWT_BATCHED_MIXED) return sfail(s, HWT_EINVAL, "tree mode must be batched");
+    if (tree_mode < HWT_BATCHED_FP64 || tree_mode > HWT_BATCHED_DF64) return sfail(s, HWT_EINVAL, "tree mode must be batched");
     const int n = o->n;
     if (stats) memset(stats, 0, sizeof(*stats));
     if (n == 0) return HWT_OK;
-    cudaEvent_t ev[4];
-    for (auto &e : ev) cudaEventCreate(&e);
-    cudaEventRecord(ev[0], s->stream);
-    DevBatch b, sub;
-    DevCurve cv;
-    Scoped guard;
     int r;
-    if (!alloc_batch(b, n)) { free_batch(b); return sfail(s, HWT_ENOMEM, "option buffers"); }
-    if ((r = upload_curve(s, cv, y))) { free_batch(b); return r; }
-    __nv_bfloat16 *X = nullptr;
-    double *F = nullptr, *dout = nullptr, *tree_out = nullptr, *base = nullptr;
-    uint8_t *inbox = nullptr, *kind = nullptr;
-    int32_t *list = nullptr, *count = nullptr;
-    bool ok = cudaMalloc(&X, 2ull * n * kInPad) == cudaSuccess && cudaMalloc(&F, 8ull * n) == cudaSuccess &&
-              cudaMalloc(&base, 8ull * n) == cudaSuccess &&
-              cudaMalloc(&dout, 8ull * n) == cudaSuccess && cudaMalloc(&tree_out, 8ull * n) == cudaSuccess &&
-              cudaMalloc(&inbox, n) == cudaSuccess && cudaMalloc(&kind, n) == cudaSuccess &&
-              cudaMalloc(&list, 4ull * n) == cudaSuccess && cudaMalloc(&count, 4) == cudaSuccess;
-    guard.ptrs = {X, F, dout, tree_out, base, inbox, kind, list, count};
-    if (!ok) { free_batch(b); free_curve(cv); return sfail(s, HWT_ENOMEM, "pricing buffers"); }
-    if (upload_batch(b, o, s->stream) != cudaSuccess) { free_batch(b); free_curve(cv); return sfail(s, HWT_ECUDA, "options H2D"); }
-    DevYield yc;
-    yc.n = cv.n; yc.rate = cv.rate; yc.rate_f = cv.rate_f; yc.day = cv.day;
-    features_kernel<<<(n + 255) / 256, 256, 0, s->stream>>>(dev_view(b, n), yc, s->box, s->fn, X, F, base, inbox);
-    // network on every option (out-of-box rows are overwritten by the tree)
-    if ((r = ensure_act(s, std::min(n, kChunk)))) { free_batch(b); free_curve(cv); return r; }
-    for (int c0 = 0; c0 < n; c0 += kChunk) {
-        const int rows = std::min(kChunk, n - c0);
-        if ((r = forward_from(s, X + (size_t)c0 * kInPad, rows))) { free_batch(b); free_curve(cv); return r; }
-        decode_kernel<<<(rows + 255) / 256, 256, 0, s->stream>>>(s->d_z[kLayers - 1], F + c0, base + c0, inbox + c0, rows,
-                                                               s->ymean, s->ystd, dout + c0);
-    }
-    cudaEventRecord(ev[1], s->stream);
-    // route out-of-box options and the judge's sample to the tree
-    SCUDA(s, cudaMemsetAsync(count, 0, 4, s->stream), "count");
+    SCUDA(s, cudaEventRecord(s->ev[0], s->stream), "event");
+    if ((r = features_for(s, o, y))) return r;
+    if (!s->out2.grow((size_t)n * kOut) || !s->price.grow(n) || !s->kind.grow(n) || !s->list.grow(n) ||
+        !s->counts.grow(4) || !s->tree.grow(n) || !s->errs.grow(n) || !grow_batch(s->sub, n))
+        return sfail(s, HWT_ENOMEM, "pricing buffers");
+    // network on every option (rows outside the box are not used)
+    if ((r = forward_fused(s, s->xf.p, n, s->out2.p))) return r;
+    SCUDA(s, cudaMemsetAsync(s->counts.p, 0, 16, s->stream), "counts");
     const double jf = std::min(std::max(judge_fraction, 0.0), 1.0);
     const unsigned long long thresh = jf >= 1.0 ? ~0ull : (unsigned long long)(jf * 18446744073709551616.0);
-    route_kernel<<<(n + 255) / 256, 256, 0, s->stream>>>(inbox, n, seed, thresh, list, kind, count);
-    int m = 0;
-    SCUDA(s, cudaMemcpyAsync(&m, count, 4, cudaMemcpyDeviceToHost, s->stream), "count D2H");
+    // flag when exp(o1) ystd F > tau; tau = +inf: the router is off, tau <= 0: nothing is answered
+    const float log_tau = std::isinf(s->route_tau) ? INFINITY
+                          : (s->route_tau > 0 ? (float)log(s->route_tau / s->ystd) : -INFINITY);
+    decode_route_kernel<<<(n + 255) / 256, 256, 0, s->stream>>>(s->out2.p, s->F.p, s->base.p, s->inbox.p, n, s->ymean,
+                                                               s->ystd, log_tau, seed, thresh, s->price.p, s->kind.p,
+                                                               s->list.p, s->counts.p);
+    SCUDA(s, cudaGetLastError(), "decode kernel");
+    SCUDA(s, cudaEventRecord(s->ev[1], s->stream), "event");
+    int32_t cnt[4] = {0, 0, 0, 0};
+    SCUDA(s, cudaMemcpyAsync(cnt, s->counts.p, 16, cudaMemcpyDeviceToHost, s->stream), "counts D2H");
     SCUDA(s, cudaStreamSynchronize(s->stream), "route");
-    std::vector<int32_t> hl(m);
-    std::vector<double> tree_px(m);
+    if ((r = gemm_status(s))) return r;
+    const int m = cnt[0];
     double tree_ms = 0;
+    hwt_config tc;
+    memset(&tc, 0, sizeof(tc));
+    tc.mode = tree_mode;
+    tc.use_graph = 1;
     if (m > 0) {
-        if (!alloc_batch(sub, m)) { free_batch(b); free_batch(sub); free_curve(cv); return sfail(s, HWT_ENOMEM, "routed buffers"); }
-        gather_options_kernel<<<(m + 255) / 256, 256, 0, s->stream>>>(dev_view(b, n), list, count, dev_view(sub, m),
-                                                                    sub.strike, sub.bm, sub.om, sub.tu, sub.ts, sub.a,
-                                                                    sub.sg, sub.ty);
-        SCUDA(s, cudaStreamSynchronize(s->stream), "gather");
-        hwt_options so = abi_view(sub, m);
-        hwt_config tc;
-        memset(&tc, 0, sizeof(tc));
-        tc.mode = tree_mode;
-        tc.use_graph = 1;
+        gather_options_kernel<<<(m + 255) / 256, 256, 0, s->stream>>>(dev_view(s->opts, n), s->list.p, m, s->sub.strike,
+                                                                    s->sub.bm, s->sub.om, s->sub.tu, s->sub.ts, s->sub.a,
+                                                                    s->sub.sg, s->sub.ty);
+        SCUDA(s, cudaStreamSynchronize(s->stream), "gather");  // the tree runs on the context's stream
+        hwt_options so = abi_view(s->sub, m);
         hwt_stats ts;
-        r = hwt_price_device(s->ctx, &so, y, &tc, tree_out, &ts);
-        free_batch(sub);
-        if (r && r != HWT_EINVAL) { free_batch(b); free_curve(cv); return sfail(s, r, hwt_last_error(s->ctx)); }
+        r = hwt_price_device(s->ctx, &so, y, &tc, s->tree.p, &ts);
+        if (r && r != HWT_EINVAL) return sfail(s, r, hwt_last_error(s->ctx));
         tree_ms = ts.total_ms;
-        cudaMemcpy(hl.data(), list, 4ull * m, cudaMemcpyDeviceToHost);
-        cudaMemcpy(tree_px.data(), tree_out, 8ull * m, cudaMemcpyDeviceToHost);
+        scatter_tree_kernel<<<(m + 255) / 256, 256, 0, s->stream>>>(s->list.p, m, s->tree.p, s->kind.p, s->price.p,
+                                                                  s->errs.p);
+        SCUDA(s, cudaGetLastError(), "scatter kernel");
     }
-    cudaEventRecord(ev[2], s->stream);
-    SCUDA(s, cudaMemcpyAsync(out, dout, 8ull * n, cudaMemcpyDeviceToHost, s->stream), "prices D2H");
-    std::vector<uint8_t> kh(n);
-    SCUDA(s, cudaMemcpyAsync(kh.data(), kind, n, cudaMemcpyDeviceToHost, s->stream), "kind D2H");
-    cudaEventRecord(ev[3], s->stream);
+    SCUDA(s, cudaEventRecord(s->ev[2], s->stream), "event");
+    std::vector<double> errs(m);
+    if (m > 0) SCUDA(s, cudaMemcpyAsync(errs.data(), s->errs.p, 8ull * m, cudaMemcpyDeviceToHost, s->stream), "errs D2H");
+    SCUDA(s, cudaMemcpyAsync(out, s->price.p, 8ull * n, cudaMemcpyDeviceToHost, s->stream), "prices D2H");
+    SCUDA(s, cudaEventRecord(s->ev[3], s->stream), "event");
     SCUDA(s, cudaStreamSynchronize(s->stream), "price");
-    free_batch(b);
-    free_curve(cv);
-    // judge: |network - tree| on the sample; every tree-priced option returns the tree price
-    std::vector<double> errs;
-    errs.reserve(m);
-    int64_t routed = 0;
+    // judge: |network - tree| on the sample of the network's answers
+    std::vector<double> e;
+    e.reserve(cnt[KIND_JUDGED]);
     double worst = 0.0;
-    for (int j = 0; j < m; ++j) {
-        const int i = hl[j];
-        if (kh[i] == 2) {
-            const double e = fabs(out[i] - tree_px[j]);
-            errs.push_back(e);
-            worst = std::max(worst, e != e ? INFINITY : e);
-        } else {
-            ++routed;
+    for (int j = 0; j < m; ++j)
+        if (errs[j] >= 0.0 || errs[j] != errs[j]) {
+            const double v = errs[j] != errs[j] ? INFINITY : errs[j];
+            e.push_back(v);
+            worst = std::max(worst, v);
         }
-        out[i] = tree_px[j];
-    }
     int fell_back = 0;
     double fallback_ms = 0;
+    int64_t n_network = (int64_t)n - cnt[KIND_OUTSIDE] - cnt[KIND_FLAGGED];
     if (judge_tolerance > 0 && worst > judge_tolerance) {
-        // the network failed its judge on this batch: the tree prices all of it
-        hwt_config tc;
-        memset(&tc, 0, sizeof(tc));
-        tc.mode = tree_mode;
-        tc.use_graph = 1;
-        hwt_stats ts;
-        r = hwt_price_ex(s->ctx, o, y, &tc, out, &ts);
-        if (r) return sfail(s, r, hwt_last_error(s->ctx));
+        // the network failed its judge on this batch: the tree prices the rest of
+        // the network's answers too
+        SCUDA(s, cudaMemsetAsync(s->counts.p, 0, 4, s->stream), "counts");
+        network_list_kernel<<<(n + 255) / 256, 256, 0, s->stream>>>(s->kind.p, n, s->list.p, s->counts.p);
+        int32_t m2 = 0;
+        SCUDA(s, cudaMemcpyAsync(&m2, s->counts.p, 4, cudaMemcpyDeviceToHost, s->stream), "count D2H");
+        SCUDA(s, cudaStreamSynchronize(s->stream), "fallback list");
+        if (m2 > 0) {
+            gather_options_kernel<<<(m2 + 255) / 256, 256, 0, s->stream>>>(dev_view(s->opts, n), s->list.p, m2,
+                                                                         s->sub.strike, s->sub.bm, s->sub.om, s->sub.tu,
+                                                                         s->sub.ts, s->sub.a, s->sub.sg, s->sub.ty);
+            SCUDA(s, cudaStreamSynchronize(s->stream), "gather");
+            hwt_options so = abi_view(s->sub, m2);
+            hwt_stats ts;
+            r = hwt_price_device(s->ctx, &so, y, &tc, s->tree.p, &ts);
+            if (r && r != HWT_EINVAL) return sfail(s, r, hwt_last_error(s->ctx));
+            fallback_ms = ts.total_ms;
+            scatter_tree_kernel<<<(m2 + 255) / 256, 256, 0, s->stream>>>(s->list.p, m2, s->tree.p, s->kind.p, s->price.p,
+                                                                       s->errs.p);
+            SCUDA(s, cudaMemcpyAsync(out, s->price.p, 8ull * n, cudaMemcpyDeviceToHost, s->stream), "prices D2H");
+            SCUDA(s, cudaStreamSynchronize(s->stream), "fallback");
+        }
         fell_back = 1;
-        fallback_ms = ts.total_ms;
+        n_network = 0;
     }
     if (stats) {
         float t0 = 0, t1 = 0, t2 = 0;
-        cudaEventElapsedTime(&t0, ev[0], ev[1]);
-        cudaEventElapsedTime(&t1, ev[0], ev[3]);
-        cudaEventElapsedTime(&t2, ev[1], ev[2]);
-        stats->n_in_box = n - routed;
-        stats->n_routed = routed;
-        stats->n_judged = (int64_t)errs.size();
-        if (!errs.empty()) {
-            std::vector<double> e = errs;
+        cudaEventElapsedTime(&t0, s->ev[0], s->ev[1]);
+        cudaEventElapsedTime(&t1, s->ev[0], s->ev[3]);
+        cudaEventElapsedTime(&t2, s->ev[1], s->ev[2]);
+        stats->n_in_box = n - cnt[KIND_OUTSIDE];
+        stats->n_routed = cnt[KIND_OUTSIDE];
+        stats->n_judged = (int64_t)e.size();
+        stats->n_flagged = cnt[KIND_FLAGGED];
+        stats->n_network = n_network;
+        if (!e.empty()) {
             std::sort(e.begin(), e.end());
             double sm = 0;
             for (double v : e) sm += v;
@@ -1006,8 +1318,7 @@ int hwt_surrogate_price(hwt_surrogate *s, const hwt_options *o, const hwt_yield 
         stats->route_ms = t2;
         stats->total_ms = t1 + fallback_ms;
     }
-    for (auto &e : ev) cudaEventDestroy(e);
-    return gemm_status(s);
+    return HWT_OK;
 }
 
 int hwt_surrogate_save(const hwt_surrogate *s, const char *path)
@@ -1020,13 +1331,13 @@ int hwt_surrogate_save(const hwt_surrogate *s, const char *path)
         return HWT_ECUDA;
     FILE *f = fopen(path, "wb");
     if (!f) return HWT_EINVAL;
-    const uint32_t magic = 0x48575453u, version = 1;
+    const uint32_t magic = 0x48575453u, version = 2;
     const uint64_t np = s->n_params;
     const int64_t t = s->adam_t;
     bool ok = fwrite(&magic, 4, 1, f) == 1 && fwrite(&version, 4, 1, f) == 1 && fwrite(&s->box, sizeof(hwt_box), 1, f) == 1 &&
-              fwrite(&s->ymean, 8, 1, f) == 1 && fwrite(&s->ystd, 8, 1, f) == 1 && fwrite(&t, 8, 1, f) == 1 &&
-              fwrite(&np, 8, 1, f) == 1 && fwrite(w.data(), 4, np, f) == np && fwrite(m.data(), 4, np, f) == np &&
-              fwrite(v.data(), 4, np, f) == np;
+              fwrite(&s->ymean, 8, 1, f) == 1 && fwrite(&s->ystd, 8, 1, f) == 1 && fwrite(&s->route_tau, 8, 1, f) == 1 &&
+              fwrite(&t, 8, 1, f) == 1 && fwrite(&np, 8, 1, f) == 1 && fwrite(w.data(), 4, np, f) == np &&
+              fwrite(m.data(), 4, np, f) == np && fwrite(v.data(), 4, np, f) == np;
     fclose(f);
     return ok ? HWT_OK : HWT_EINVAL;
 }
@@ -1040,10 +1351,10 @@ int hwt_surrogate_load(hwt_surrogate *s, const char *path)
     uint64_t np = 0;
     int64_t t = 0;
     hwt_box box;
-    double ym = 0, ysd = 1;
-    bool ok = fread(&magic, 4, 1, f) == 1 && fread(&version, 4, 1, f) == 1 && magic == 0x48575453u && version == 1 &&
+    double ym = 0, ysd = 1, tau = INFINITY;
+    bool ok = fread(&magic, 4, 1, f) == 1 && fread(&version, 4, 1, f) == 1 && magic == 0x48575453u && version == 2 &&
               fread(&box, sizeof(hwt_box), 1, f) == 1 && fread(&ym, 8, 1, f) == 1 && fread(&ysd, 8, 1, f) == 1 &&
-              fread(&t, 8, 1, f) == 1 && fread(&np, 8, 1, f) == 1 && np == s->n_params;
+              fread(&tau, 8, 1, f) == 1 && fread(&t, 8, 1, f) == 1 && fread(&np, 8, 1, f) == 1 && np == s->n_params;
     std::vector<float> w(s->n_params), m(s->n_params), v(s->n_params);
     ok = ok && fread(w.data(), 4, np, f) == np && fread(m.data(), 4, np, f) == np && fread(v.data(), 4, np, f) == np;
     fclose(f);
@@ -1052,6 +1363,7 @@ int hwt_surrogate_load(hwt_surrogate *s, const char *path)
     box_norm(box, s->fn);
     s->ymean = ym;
     s->ystd = ysd;
+    s->route_tau = tau;
     s->adam_t = t;
     SCUDA(s, cudaMemcpy(s->d_w, w.data(), 4 * np, cudaMemcpyHostToDevice), "load");
     SCUDA(s, cudaMemcpy(s->d_m, m.data(), 4 * np, cudaMemcpyHostToDevice), "load");

@@ -24,7 +24,9 @@
 // dY * SiLU'(Z), split-K atomics) with 16-byte loads and stores.
 //
 // Every wait on an mbarrier is bounded: past the limit the CTA raises *err, stops
-// issuing work, waits (bounded) for what it issued, frees its TMEM and returns.
+// issuing work, waits (bounded) for the MMAs it already committed, frees its TMEM
+// and returns.  test_stall injects a wait that nothing completes: 1 before any MMA,
+// 2 after the first K block's MMAs were committed.
 #pragma once
 
 #include <cuda_bf16.h>
@@ -58,7 +60,8 @@ struct GemmArgs {
     int ldc, ldcb;
     int epi;
     int *err;            // set to 1 by a CTA whose mbarrier wait ran out
-    int test_stall;      // fault injection: first wait on a phase nothing completes
+    int test_stall;      // fault injection: 1 = before any MMA, 2 = after block 0's MMAs, a wait
+                         // on a phase nothing completes
 };
 
 // Dynamic shared memory of one CTA for tile width bn.
@@ -67,12 +70,29 @@ __host__ __device__ constexpr int smem_bytes(int bn) { return STAGES * (BM + bn)
 // TMEM columns to allocate for bn accumulator columns (a power of two >= 32).
 __host__ __device__ constexpr int tmem_cols(int bn) { return bn <= 32 ? 32 : (bn <= 64 ? 64 : (bn <= 128 ? 128 : 256)); }
 
-__device__ __forceinline__ float silu_f(float z) { return z / (1.0f + __expf(-z)); }
+// Hardware tanh approximation (one MUFU operation, PTX tanh.approx.f32).
+__device__ __forceinline__ float tanh_approx(float x)
+{
+    float y;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
 
+// SiLU z * sigmoid(z) with sigmoid(z) = (1 + tanh(z / 2)) / 2: with h = z / 2,
+// silu = h + h tanh(h), one MUFU operation per activation (the exp-and-reciprocal
+// form takes two, and the activations of the fused network are MUFU-bound).  Its
+// error (~5e-4 |z| at most) is below the bf16 rounding the activations then take.
+__device__ __forceinline__ float silu_f(float z)
+{
+    const float h = 0.5f * z;
+    return fmaf(h, tanh_approx(h), h);
+}
+
+// d silu / dz = s (1 + z (1 - s)) with the same sigmoid s.
 __device__ __forceinline__ float dsilu_f(float z)
 {
-    const float s = 1.0f / (1.0f + __expf(-z));
-    return s * (1.0f + z * (1.0f - s));
+    const float s = fmaf(0.5f, tanh_approx(0.5f * z), 0.5f);
+    return s * fmaf(z, 1.0f - s, 1.0f);
 }
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -251,8 +271,8 @@ __global__ void __launch_bounds__(THREADS) umma_gemm_kernel(GemmArgs p)
         sA[s] = reinterpret_cast<__nv_bfloat16 *>(smem) + s * (BM + BN) * BK;
         sB[s] = sA[s] + BM * BK;
     }
-    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + STAGES * (BM + BN) * BK * 2);
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + STAGES);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + STAGES * (BM + BN) * BK * 2);  // STAGES + "never"
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + STAGES + 1);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
     const int kbeg = blockIdx.z * p.k_chunk;
@@ -261,7 +281,7 @@ __global__ void __launch_bounds__(THREADS) umma_gemm_kernel(GemmArgs p)
     constexpr uint32_t IDESC = make_idesc(BN) | ((TA ? 1u : 0u) << 15) | ((TB ? 1u : 0u) << 16);  // MN-major bits
 
     if (threadIdx.x == 0) {
-        for (int s = 0; s < STAGES; ++s) mbar_init(smem_u32(&bars[s]), 1);
+        for (int s = 0; s <= STAGES; ++s) mbar_init(smem_u32(&bars[s]), 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) tmem_alloc(smem_u32(tmem_slot), NCOLS);
@@ -275,8 +295,9 @@ __global__ void __launch_bounds__(THREADS) umma_gemm_kernel(GemmArgs p)
     const bool vecA = (p.lda % 8 == 0) && ((reinterpret_cast<uintptr_t>(p.A) & 15) == 0) && (TA || kbeg % 8 == 0);
     const bool vecB = (p.ldb % 8 == 0) && ((reinterpret_cast<uintptr_t>(p.B) & 15) == 0) && (TB || kbeg % 8 == 0);
     int nkb = kend > kbeg ? (kend - kbeg + BK - 1) / BK : 0;
+    int issued = 0;  // K blocks whose MMAs were committed
     bool ok = true;
-    if (p.test_stall) {
+    if (p.test_stall == 1) {
         // a fresh mbarrier's phase 0 never completes without arrivals: the bounded
         // wait runs out, and the CTA skips its work and reports it
         ok = mbar_wait(smem_u32(&bars[0]), 0u);
@@ -306,6 +327,14 @@ __global__ void __launch_bounds__(THREADS) umma_gemm_kernel(GemmArgs p)
                 mma_bf16(tmem, step_desc<BM, TA>(a0, kk), step_desc<BN, TB>(b0, kk), IDESC, (kb > 0 || kk > 0) ? 1u : 0u);
             mma_commit(smem_u32(&bars[s]));
         }
+        issued = kb + 1;
+        if (p.test_stall == 2 && kb == 0) {
+            // injected: a phase nothing completes, with block 0's MMAs in flight
+            ok = mbar_wait(smem_u32(&bars[STAGES]), 0u);
+            __syncthreads_and(ok ? 1 : 0);
+            ok = false;
+            break;
+        }
         // refill the stage block kb - 1 used, once its MMAs are done
         const int nb = kb + STAGES - 1;
         if (nb < nkb) {
@@ -322,10 +351,13 @@ __global__ void __launch_bounds__(THREADS) umma_gemm_kernel(GemmArgs p)
         cp_async_commit();
     }
     cp_async_wait<0>();
-    // the last commit covers every MMA this CTA issued
+    // The last commit covers every MMA this CTA issued: wait for it (bounded) before
+    // the epilogue reads TMEM or, after a wait that ran out, before TMEM is freed.
+    // If this wait runs out too, the tensor core is not completing work; the CTA
+    // then frees TMEM and returns with *err raised all the same.
     bool done = true;
-    if (ok && nkb > 0) {
-        const int last = nkb - 1;
+    if (issued > 0) {
+        const int last = issued - 1;
         done = mbar_wait(smem_u32(&bars[last % STAGES]), (uint32_t)((last / STAGES) & 1));
     }
     if (!ok || !done) {
@@ -333,7 +365,7 @@ __global__ void __launch_bounds__(THREADS) umma_gemm_kernel(GemmArgs p)
     }
     fence_after_sync();
     // (a split-K slice with no K block has nothing to add)
-    const bool good = __syncthreads_and((ok && done && nkb > 0) ? 1 : 0) != 0;
+    const bool good = __syncthreads_and((ok && done && issued == nkb && nkb > 0) ? 1 : 0) != 0;
 
     if (good) {
         const int m = m0 + warp * 32 + lane;  // this thread's tile row = TMEM lane

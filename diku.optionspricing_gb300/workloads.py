@@ -240,3 +240,56 @@ def surrogate_query_batch(n=1_000_000, seed=4, outside_fraction=0.10):
     b["outside"] = np.zeros(n, dtype=bool)
     b["outside"][out] = True
     return b
+
+
+# ---------------------------------------------------------------------------
+# Surrogate on the single-tree box: samples drawn as the 1,000-option book draws
+# them (t = 5 y, T = 10 y, 12 steps/year, a = 0.10, sigma = 0.01; strike U[75, 95],
+# call/put 50/50), so only strike and type vary.  The tree's price is then a
+# piecewise-linear function of strike, with a kink at each maturity-row bond value.
+# ---------------------------------------------------------------------------
+def _book_forward():
+    return float(forward_bond_price(5.0, 10.0))
+
+
+def single_tree_box():
+    """Training box of the single-tree surrogate: the book's fixed tree parameters,
+    strike / forward bond price in [75, 95] / F(5 y, 10 y)."""
+    f = _book_forward()
+    return dict(t_min=5.0, t_max=5.0, span_min=5.0, span_max=5.0, moneyness_min=75.0 / f, moneyness_max=95.0 / f,
+                a_min=0.10, a_max=0.10, sigma_min=0.01, sigma_max=0.01, steps_min=12, steps_max=12, term_unit=365)
+
+
+def single_tree_training_batch(n=4_000_000, seed=3):
+    """Training samples drawn as the 1,000-option book (seed 3)."""
+    return uniform_book(n, seed)
+
+
+def single_tree_query_batch(n=1_000_000, seed=4, outside_fraction=0.10):
+    """Queries: the book's distribution, with 10% drawn outside the single-tree box
+    (strike 60-75 or 95-110, a in [0.05, 0.2], sigma in [0.005, 0.02], 6-48 steps per
+    year, or option maturity 1-4 y), in random order."""
+    rng = np.random.default_rng(seed)
+    b = uniform_book(n, seed)
+    out = rng.permutation(n)[: int(round(n * outside_fraction))]
+    kind = rng.integers(0, 5, len(out))
+    strike, a, sigma, steps, t = b["strike"], b["a"], b["sigma"], b["term_steps"], b["option_maturity"]
+    for k in range(5):
+        idx = out[kind == k]
+        if k == 0:
+            lo = rng.integers(0, 2, len(idx)) == 0
+            strike[idx] = np.where(lo, rng.uniform(60.0, 74.5, len(idx)), rng.uniform(95.5, 110.0, len(idx)))
+        elif k == 1:
+            a[idx] = np.where(rng.integers(0, 2, len(idx)) == 0, rng.uniform(0.05, 0.095, len(idx)),
+                              rng.uniform(0.105, 0.20, len(idx)))
+        elif k == 2:
+            sigma[idx] = np.where(rng.integers(0, 2, len(idx)) == 0, rng.uniform(0.005, 0.0095, len(idx)),
+                                  rng.uniform(0.0105, 0.02, len(idx)))
+        elif k == 3:
+            steps[idx] = np.where(rng.integers(0, 2, len(idx)) == 0, rng.integers(6, 12, len(idx)),
+                                  rng.integers(13, 49, len(idx)))
+        else:
+            t[idx] = rng.integers(1, 5, len(idx)).astype(np.float64)
+    b["outside"] = np.zeros(n, dtype=bool)
+    b["outside"][out] = True
+    return b

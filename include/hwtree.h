@@ -225,13 +225,18 @@ int hwt_get_config(const hwt_ctx *ctx, int mode, hwt_config *cfg);
 int hwt_measure_peaks(hwt_ctx *ctx, double *fp64_tflops, double *fp32_tflops);
 
 /* ---- Learned surrogate -------------------------------------------------------
- * A 7 -> 4 x 256 (SiLU) -> 1 MLP mapping standardised (option maturity, bond
- * maturity, strike / forward bond price, a, sigma, steps per year, call/put) to
- * price / forward bond price, bf16 weights with fp32 accumulation on the tensor
- * cores.  Trained on prices from the batched FP64 tree; options outside its
- * training box go to the tree, and a random sample of every batch is repriced by
- * the tree as its judge.  The reference has no learned part (row a10 of the
- * build's scope); these entry points have no reference counterpart. */
+ * An 8 -> 4 x 256 (SiLU) -> 2 MLP over standardised (option maturity, bond
+ * maturity, strike / forward bond price, a, sigma, steps per year, call/put) and a
+ * zero pad.  Output 0 is price / forward bond price (or, with box.residual, the
+ * tree price minus the Hull-White closed-form price over the forward bond price),
+ * standardised; output 1 estimates log |output-0 error| and routes the options it
+ * does not trust to the tree.  Layer 0 is fp32 (CUDA cores); layers 1-4 use bf16
+ * weights with fp32 accumulation on the tensor cores.  Trained on prices from the
+ * batched FP64 tree; inference runs the whole network in one fused tensor-core
+ * kernel.  Options outside the training box and options the error head flags go
+ * to the tree, and a random sample of the network's answers is repriced by the
+ * tree as its judge.  The reference has no learned part; these entry points have
+ * no reference counterpart. */
 typedef struct hwt_box {
     double t_min, t_max;             /* option maturity [years] */
     double span_min, span_max;       /* bond maturity - option maturity [years] */
@@ -248,24 +253,36 @@ typedef struct hwt_train_config {
     int32_t epochs;                  /* passes over the samples (default 1) */
     int32_t batch;                   /* samples per Adam step (default 8192) */
     double lr, lr_min;               /* cosine decay from lr to lr_min over all steps */
-    uint64_t seed;                   /* shuffling */
+    uint64_t seed;                   /* shuffling and the held-out split */
+    double err_weight;               /* weight of the error head's loss; 0: head untrained, no routing */
+    double route_tolerance;          /* price error (per 100 face) that the network's answers must keep
+                                        on the held-out samples; sets the routing threshold (default 1e-4) */
+    double holdout;                  /* fraction of in-box samples held out for that (default 0.05) */
 } hwt_train_config;
 
 typedef struct hwt_train_stats {
-    double final_loss;               /* mean 0.5 (y - f(x))^2 of the last epoch, standardised units */
+    double final_loss;               /* mean loss of the last epoch, standardised units */
     double train_ms, label_ms;       /* training time; time the tree took to price the labels */
-    int64_t steps, samples;          /* Adam steps; in-box samples used */
+    int64_t steps, samples;          /* Adam steps; in-box samples trained on */
     double samples_per_s;
     double y_mean, y_std;            /* target standardisation */
+    double route_threshold;          /* predicted price error above which an option goes to the tree
+                                        (+inf: routing off) */
+    double holdout_answered;         /* fraction of held-out samples the network answers */
+    double holdout_max_abs, holdout_p99_abs; /* |network - tree| over those it answers */
+    double holdout_all_max_abs;      /* |network - tree| over all held-out samples */
+    int64_t holdout;                 /* held-out samples */
 } hwt_train_stats;
 
 typedef struct hwt_surrogate_stats {
-    int64_t n_in_box, n_routed, n_judged;
+    int64_t n_in_box, n_routed, n_judged;  /* n_routed: outside the box; n_judged: the judge's sample */
     int32_t fell_back;               /* 1: the judge saw an error above the tolerance and the tree
-                                        priced the whole batch */
+                                        priced the network's answers too */
     int32_t pad;
     double judge_max_abs, judge_p99_abs, judge_mean_abs; /* |network - tree| on the judged sample */
     double network_ms, tree_ms, route_ms, total_ms;
+    int64_t n_flagged;               /* in-box options the error head sent to the tree */
+    int64_t n_network;               /* options answered by the network */
 } hwt_surrogate_stats;
 
 typedef struct hwt_surrogate hwt_surrogate;
@@ -273,36 +290,46 @@ typedef struct hwt_surrogate hwt_surrogate;
 hwt_surrogate *hwt_surrogate_create(hwt_ctx *ctx, const hwt_box *box, uint64_t seed);
 void hwt_surrogate_destroy(hwt_surrogate *s);
 const char *hwt_surrogate_last_error(const hwt_surrogate *s);
-/* Prices the (host) samples with the batched FP64 tree and trains on them. */
+/* Prices the (host) samples with the batched FP64 tree, trains on the in-box ones
+ * but a held-out slice, and sets the routing threshold on that slice. */
 int hwt_surrogate_train(hwt_surrogate *s, const hwt_options *samples, const hwt_yield *yield,
                         const hwt_train_config *cfg, hwt_train_stats *stats);
-/* Prices host options: network inside the box, tree (tree_mode: a batched mode)
- * outside it and for the judge's sample (fraction judge_fraction, drawn from
- * `seed`), whose options get the tree price.  If judge_tolerance > 0 and the
- * judge's largest |network - tree| exceeds it, the tree prices the whole batch
- * (stats->fell_back = 1), so the answer is never worse than the tolerance on
- * the judged sample. */
+/* Prices host options: network inside the box unless the error head flags the
+ * option, tree (tree_mode: a batched mode) outside the box, for flagged options
+ * and for the judge's sample (fraction judge_fraction of the in-box options the
+ * network answers, drawn from `seed`), whose options get the tree price.  If
+ * judge_tolerance > 0 and the judge's largest |network - tree| exceeds it, the
+ * tree prices the network's other answers as well (stats->fell_back = 1), so the
+ * answer is never worse than the tolerance on the judged sample. */
 int hwt_surrogate_price(hwt_surrogate *s, const hwt_options *opts, const hwt_yield *yield, double judge_fraction,
                         uint64_t seed, int tree_mode, double judge_tolerance, double *out_prices,
                         hwt_surrogate_stats *stats);
-/* Checkpoint: box, target scaling, weights and Adam state (resume training). */
+/* Checkpoint: box, target scaling, routing threshold, weights and Adam state. */
 int hwt_surrogate_save(const hwt_surrogate *s, const char *path);
 int hwt_surrogate_load(hwt_surrogate *s, const char *path);
-/* Parameters: layer l has W_l [fan_in][fan_out] then b_l [fan_out], fan_in 8
- * (7 features + a zero pad row) for the first layer; get (set = 0) or set them. */
+/* Parameters: layer l has W_l [fan_in][fan_out] then b_l [fan_out]; fan_in 8
+ * (7 features + a zero pad row) for the first layer, fan_out 2 for the last; get
+ * (set = 0) or set them. */
 int64_t hwt_surrogate_param_count(const hwt_surrogate *s);
 int hwt_surrogate_params(hwt_surrogate *s, float *params, int64_t count, int set);
-/* Forward pass and loss/gradients on host buffers of standardised features
- * x [n][7] and standardised targets y [n] (no update): the hooks the gradient
- * check against the CPU oracle uses. */
+/* Forward pass on host standardised features x [n][7] into out [n][2]: path 0 =
+ * the fused inference kernel, 1 = the layer-by-layer training kernels.
+ * hwt_surrogate_forward is path 0. */
 int hwt_surrogate_forward(hwt_surrogate *s, const float *x, int n, float *out);
-/* Fault injection for tests of the failure path: while on, every GEMM first waits
- * on an mbarrier phase that nothing completes; the bounded wait runs out (about a
- * second), the GEMM skips its work and the call returns HWT_ETIMEOUT with the
- * context still usable.  No GPU fault is involved. */
-int hwt_surrogate_inject_stall(hwt_surrogate *s, int on);
-int hwt_surrogate_loss_grads(hwt_surrogate *s, const float *x, const float *y, int n, double *loss,
-                             float *grads);
+int hwt_surrogate_forward_ex(hwt_surrogate *s, const float *x, int n, float *out, int path);
+/* Loss and gradients (no update) of the training path on x [n][7] and standardised
+ * targets y [n]: 0.5 mean (o0 - y)^2 + err_weight 0.5 mean (o1 - log(|o0 - y| +
+ * 1e-3))^2, the error-head target held constant; gradients in the params layout.
+ * The hook the gradient check against the CPU oracle uses. */
+int hwt_surrogate_loss_grads(hwt_surrogate *s, const float *x, const float *y, int n, double err_weight,
+                             double *loss, float *grads);
+/* Fault injection for tests of the failure path (no GPU fault involved): mode 1
+ * makes every tensor-core kernel wait, before its first MMA, on an mbarrier phase
+ * that nothing completes; mode 2 does so after its first K block's MMAs were
+ * committed; 0 turns it off.  The bounded wait runs out (about a second), the
+ * kernel waits for what it issued, frees its tensor memory and returns, and the
+ * call returns HWT_ETIMEOUT with the context still usable. */
+int hwt_surrogate_inject_stall(hwt_surrogate *s, int mode);
 
 /* ---- Input files ------------------------------------------------------------
  * Replace trinom::Options(const std::string&) and trinom::Yield(const

@@ -1,20 +1,27 @@
 """ORACLE - test infrastructure, not the product.
 
 FP64 numpy restatement of the surrogate MLP that the GPU trains and evaluates
-(7 inputs -> 4 x 256 SiLU -> 1).  The reference project has no learned part, so
-this restatement is the oracle for the GPU forward pass, the gradients and the Adam
+(8 inputs: 7 features and a zero pad -> 4 x 256 SiLU -> 2 outputs: the price
+target and the error head).  The reference project has no learned part, so this
+restatement is the oracle for the GPU forward pass, the gradients and the Adam
 step; it is itself checked by central finite differences (tests/test_mlp_oracle.py).
 
 Layout matches the GPU kernels: W_l is [fan_in, fan_out] row-major, y = x W + b.
-The GPU keeps bf16 copies of the weights and bf16 activations between layers with
-fp32 accumulation; `forward(..., bf16=True)` rounds the same tensors the same way so
-the comparison isolates accumulation-order differences.
+The GPU computes layer 0 in fp32 from fp32 features, and keeps bf16 copies of the
+weights of layers 1-4 and bf16 activations between layers with fp32 accumulation;
+`forward(..., bf16=True)` rounds the same tensors the same way (layer 0's inputs
+and weights are not rounded) so the comparison isolates accumulation-order and
+activation-approximation differences.
+
+Loss: 0.5 mean((o0 - y)^2) + err_weight * 0.5 mean((o1 - log(|o0 - y| + eps))^2),
+the error head's target held constant (no gradient flows through it).
 """
 from __future__ import annotations
 
 import numpy as np
 
-DIMS = (7, 256, 256, 256, 256, 1)
+DIMS = (8, 256, 256, 256, 256, 2)
+ERR_EPS = 1e-3
 
 
 def bf16_round(x: np.ndarray) -> np.ndarray:
@@ -48,14 +55,13 @@ def init_params(seed: int = 0, dims=DIMS):
 
 
 def forward(params, x, bf16: bool = False):
-    """Returns (output [n], cache of pre-activations and layer inputs)."""
+    """Returns (outputs [n, fan_out of the last layer], cache of pre-activations and
+    layer inputs)."""
     h = np.asarray(x, dtype=np.float64)
-    if bf16:
-        h = bf16_round(h)
     inputs, pre = [], []
     last = len(params) - 1
     for li, (W, b) in enumerate(params):
-        Wq = bf16_round(W) if bf16 else W
+        Wq = bf16_round(W) if (bf16 and li > 0) else W
         inputs.append(h)
         z = h @ Wq + b
         pre.append(z)
@@ -65,16 +71,22 @@ def forward(params, x, bf16: bool = False):
                 h = bf16_round(h)
         else:
             h = z
-    return h[:, 0], {"inputs": inputs, "pre": pre}
+    return h, {"inputs": inputs, "pre": pre}
 
 
-def loss_and_grads(params, x, y, bf16: bool = False):
-    """Mean squared error 0.5 * mean((f(x) - y)^2) and its gradients."""
+def loss_and_grads(params, x, y, bf16: bool = False, err_weight: float = 0.0, eps: float = ERR_EPS):
+    """Loss (module docstring) and its gradients; a one-output network has only the
+    squared-error term."""
     out, cache = forward(params, x, bf16)
     n = x.shape[0]
-    r = out - y
+    r = out[:, 0] - y
     loss = 0.5 * float(np.mean(r * r))
-    g = (r / n)[:, None]
+    g = np.zeros_like(out)
+    g[:, 0] = r / n
+    if out.shape[1] > 1:
+        r1 = out[:, 1] - np.log(np.abs(r) + eps)
+        loss += err_weight * 0.5 * float(np.mean(r1 * r1))
+        g[:, 1] = err_weight * r1 / n
     grads = [None] * len(params)
     last = len(params) - 1
     for li in range(last, -1, -1):

@@ -59,3 +59,37 @@ def test_adam_decreases_loss():
         mo.adam_step(params, g, state, mo.cosine_lr(step, 200, 3e-3))
     l1, _ = mo.loss_and_grads(params, x, y)
     assert l1 < 0.2 * l0
+
+
+def test_error_head_gradients_match_finite_differences():
+    """Two outputs: the error head's target log(|o0 - y| + eps) is held constant, so
+    the analytic gradients equal finite differences of the loss with that target
+    frozen at the unperturbed parameters."""
+    dims = (8, 12, 12, 2)
+    params = mo.init_params(5, dims)
+    rng = np.random.default_rng(4)
+    x = rng.standard_normal((24, 8))
+    y = rng.standard_normal(24) * 0.1
+    w = 0.3
+    out0, _ = mo.forward(params, x)
+    target = np.log(np.abs(out0[:, 0] - y) + mo.ERR_EPS)
+
+    def frozen_loss():
+        o, _ = mo.forward(params, x)
+        r = o[:, 0] - y
+        r1 = o[:, 1] - target
+        return 0.5 * np.mean(r * r) + w * 0.5 * np.mean(r1 * r1)
+
+    loss, grads = mo.loss_and_grads(params, x, y, err_weight=w)
+    assert abs(loss - frozen_loss()) <= 1e-12
+    eps = 1e-6
+    for li, (W, b) in enumerate(params):
+        for (i, j) in ((0, 0), (W.shape[0] - 1, W.shape[1] - 1)):
+            old = W[i, j]
+            W[i, j] = old + eps
+            lp = frozen_loss()
+            W[i, j] = old - eps
+            lm = frozen_loss()
+            W[i, j] = old
+            fd = (lp - lm) / (2 * eps)
+            assert abs(fd - grads[li][0][i, j]) <= 1e-6 * max(1.0, abs(fd)), (li, i, j, fd, grads[li][0][i, j])
