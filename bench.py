@@ -236,6 +236,180 @@ def cpu_reference(args, rank, world):
     return 0
 
 
+def errors(got, ref) -> dict:
+    err = np.abs(got - ref)
+    return {"max_abs_err": float(np.max(err)), "p99_abs_err": float(np.percentile(err, 99)),
+            "max_rel_err": float(np.max(err / np.maximum(np.abs(ref), 1e-300)))}
+
+
+def config_runs(pkg, orc, pricer, y, reps: int) -> dict:
+    """The other benchmark configurations, outside the timed region: device time per
+    batch (CUDA events on the pricer's stream, best of `reps`), options/s and errors
+    against the FP64 oracle priced here.
+      uniform_1k   the 1,000-option book (latency-bound: one tiny tree per option)
+      skewed_100k  1% heavy trees (up to 3,5xx nodes wide, 2,880 steps): per-block busy
+                   time (tail imbalance) under the engine's binned persistent schedule,
+                   under arrival order without binning ('i'), and with the one-block-per-
+                   option plain kernel, the scheduler of the plain method"""
+    wl = pkg.workloads
+    out = {}
+
+    def run(opts, mode, **cfg):
+        best, st = 1e300, None
+        for _ in range(reps):
+            got = pricer.price(opts, y, mode, **cfg)
+            s = pricer.last_stats
+            if s.sizing_ms + s.pricing_ms < best:
+                best, st = s.sizing_ms + s.pricing_ms, pkg.Stats.from_buffer_copy(s)
+        return got, best, st
+
+    # config 1
+    book = pkg.Options.from_batch(wl.uniform_book())
+    ref = orc.price(book, y, "f64")
+    entry = {"options": book.N}
+    for m in (pkg.BATCHED_MIXED, pkg.BATCHED_FP32, pkg.BATCHED_FP64, pkg.BATCHED_DF64, pkg.PLAIN_FP64):
+        got, ms, st = run(book, m)
+        entry[pkg.MODE_NAMES[m]] = {"device_ms": ms, "options_per_s": book.N / (ms * 1e-3),
+                                    "call_ms_with_copies": st.total_ms, **errors(got, ref)}
+    out["uniform_1k"] = entry
+    # config 3
+    sk = pkg.Options.from_batch(wl.skewed_batch())
+    ref = orc.price(sk, y, "f64")
+    entry = {"options": sk.N, "max_width": None, "max_height": None}
+    for m in (pkg.BATCHED_FP64, pkg.BATCHED_MIXED, pkg.BATCHED_FP32, pkg.BATCHED_DF64):
+        for sort in ("-", "i"):
+            if sort == "i" and m not in (pkg.BATCHED_FP64, pkg.BATCHED_MIXED):
+                continue
+            got, ms, st = run(sk, m, sort=sort, record_busy=True)
+            name = pkg.MODE_NAMES[m] + ("" if sort == "-" else "_arrival_order")
+            entry[name] = {"device_ms": ms, "options_per_s": sk.N / (ms * 1e-3), "busy_max_ms": st.busy_max_ms,
+                           "busy_mean_ms": st.busy_mean_ms, "tail": st.busy_max_ms / max(st.busy_mean_ms, 1e-12) - 1,
+                           **errors(got, ref)}
+            entry["max_width"], entry["max_height"] = st.max_width, st.max_height
+    got, ms, st = run(sk, pkg.PLAIN_FP64)
+    entry["plain_fp64_one_block_per_option"] = {"device_ms": ms, "options_per_s": sk.N / (ms * 1e-3),
+                                                **errors(got, ref)}
+    entry["note"] = ("tail = busiest pricing block / mean block busy time - 1; the reference's cuda-multi rejects "
+                     "trees wider than 1,024 nodes (cuda-multi/Kernel.cuh:395-400), so it cannot price this batch")
+    out["skewed_100k"] = entry
+    return out
+
+
+# FLOP per row of the surrogate network: 2 x (8 x 256 + 3 x 256 x 256 + 256 x 2)
+NETWORK_FLOP_PER_ROW = 2 * (8 * 256 + 3 * 256 * 256 + 256 * 2)
+NETWORK_TENSOR_FLOP_PER_ROW = 2 * 3 * 256 * 256  # the three tensor-core layers
+
+
+def network_kernel_time(pkg, pricer, rows: int, steps: int, warmup: int, dev) -> dict:
+    """The fused network kernel alone on device-resident standardised features
+    (random weights: its cost does not depend on them), CUDA-event time per launch,
+    L2 flushed between launches."""
+    import torch
+    sur = pkg.Surrogate(pricer, seed=1)
+    g = torch.Generator(device="cpu").manual_seed(0)
+    x = torch.randn(rows, 8, generator=g, dtype=torch.float32)
+    x[:, 7] = 0
+    x = x.to(dev)
+    out = torch.empty(rows, 2, dtype=torch.float32, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    for _ in range(warmup):
+        sur.forward_device(x.data_ptr(), rows, out.data_ptr())
+    ms = []
+    for _ in range(steps):
+        flush.zero_()
+        torch.cuda.synchronize(dev)
+        ms.append(sur.forward_device(x.data_ptr(), rows, out.data_ptr()))
+    sur.close()
+    t = sum(ms) / len(ms)
+    measured = load_json(os.path.join(ROOT, "MEASURED_PEAKS.json")) or {}
+    peak = measured.get("bf16_tflops")
+    tensor_tflops = rows * NETWORK_TENSOR_FLOP_PER_ROW / (t * 1e-3) / 1e12
+    return {"rows": rows, "kernel_ms": t, "rows_per_s": rows / (t * 1e-3),
+            "tflops": rows * NETWORK_FLOP_PER_ROW / (t * 1e-3) / 1e12, "tensor_tflops": tensor_tflops,
+            "tensor_frac_of_bf16_peak": tensor_tflops / peak if peak else None,
+            "peak": f"bf16 burst {peak} TFLOP/s of measured (MEASURED_PEAKS.json)" if peak else None,
+            "flop_per_row": NETWORK_FLOP_PER_ROW}
+
+
+def surrogate_run(pkg, pricer, y, box, train, queries, epochs: int, reps: int) -> dict:
+    """Trains the surrogate on `train` (labels from the FP64 tree), then prices the
+    1M `queries` through hwt_surrogate_price (host arrays in and out; network inside
+    the box unless routed, tree outside it, for routed options and for the judge's 1%
+    sample), against the batched trees on the same queries.  Errors against the
+    batched FP64 tree (itself within 1e-10 relative of the oracle)."""
+    sur = pkg.Surrogate(pricer, box=box, seed=1)
+    t0 = time.perf_counter()
+    tstats = sur.train(pkg.Options.from_batch(train), y, epochs=epochs, batch=8192, lr=2e-3, lr_min=2e-6,
+                       route_tolerance=1e-4, holdout=0.05)
+    train_s = time.perf_counter() - t0
+    qo = pkg.Options.from_batch(queries)
+    trees = {}
+    ref = None
+    for m in (pkg.BATCHED_FP64, pkg.BATCHED_MIXED, pkg.BATCHED_FP32, pkg.PLAIN_FP64):
+        best_dev, best_host = 1e300, 1e300
+        for _ in range(reps if m != pkg.PLAIN_FP64 else 1):
+            t0 = time.perf_counter()
+            got = pricer.price(qo, y, m)
+            best_host = min(best_host, time.perf_counter() - t0)
+            best_dev = min(best_dev, pricer.last_stats.total_ms)
+        if m == pkg.BATCHED_FP64:
+            ref = got
+        trees[pkg.MODE_NAMES[m]] = {"options_per_s": qo.N / best_host, "host_ms": 1e3 * best_host,
+                                    "device_ms_with_copies": best_dev, **errors(got, ref)}
+    wall, got = [], None
+    for k in range(reps + 1):
+        t0 = time.perf_counter()
+        got = sur.price(qo, y, judge_fraction=0.01, seed=7 + k, tree_mode=pkg.BATCHED_MIXED, judge_tolerance=1e-4)
+        wall.append(time.perf_counter() - t0)
+    st = sur.stats.as_dict()
+    sur.close()
+    best = min(wall[1:])
+    inb = ~queries["outside"]
+    err = np.abs(got - ref)
+    net = np.zeros(qo.N, dtype=bool)
+    mixed_rate = trees["batched_mixed"]["options_per_s"]
+    return {
+        "train": {**tstats, "wall_s": train_s, "epochs": epochs, "samples_offered": len(train["strike"])},
+        "queries": {"n": int(qo.N), "outside_box": int(queries["outside"].sum()),
+                    "options_per_s": qo.N / best, "host_ms": 1e3 * best,
+                    "x_batched_mixed": (qo.N / best) / mixed_rate,
+                    "x_plain_fp64": (qo.N / best) / trees["plain_fp64"]["options_per_s"],
+                    "stats": st, "in_box_max_abs_err": float(np.max(err[inb])),
+                    "in_box_p99_abs_err": float(np.percentile(err[inb], 99)),
+                    "in_box_median_abs_err": float(np.median(err[inb])),
+                    "in_box_frac_above_1e-4": float(np.mean(err[inb] > 1e-4)),
+                    "out_of_box_max_abs_err": float(np.max(err[~inb])),
+                    "timing": "host clock around hwt_surrogate_price (host arrays in and out), best of the calls "
+                              "after the first; trees: host clock around hwt_price_ex on the same queries"},
+        "trees": trees,
+    }
+
+
+def surrogate_batch(pkg, pricer, y, opts, ref_prices, args) -> dict:
+    """The uneven-box surrogate on the 30,000-option uneven batch itself, judge
+    tolerance 1e-4 enforced (answers above it send the network's answers to the tree)."""
+    wl = pkg.workloads
+    sur = pkg.Surrogate(pricer, seed=1)
+    sur.train(pkg.Options.from_batch(wl.surrogate_training_batch(args.sur_samples, 3)), y,
+              epochs=args.sur_epochs_uneven, batch=8192, lr=2e-3, lr_min=2e-6)
+    out = {}
+    for name, tol in (("unjudged", 0.0), ("judged_1e-4", 1e-4)):
+        wall = []
+        for k in range(4):
+            t0 = time.perf_counter()
+            got = sur.price(opts, y, judge_fraction=0.01, seed=100 + k, tree_mode=pkg.BATCHED_MIXED,
+                            judge_tolerance=tol)
+            wall.append(time.perf_counter() - t0)
+        st = sur.stats.as_dict()
+        e = {"options_per_s": opts.N / min(wall[1:]), "fell_back_to_tree": bool(st["fell_back"]),
+             "judge_max_abs": st["judge_max_abs"], "n_judged": st["n_judged"]}
+        if ref_prices is not None:
+            e.update(errors(got, ref_prices))
+        out[name] = e
+    sur.close()
+    return out
+
+
 def run_ours(args, rank, world, local):
     import torch
     import __graft_entry__ as g
@@ -256,6 +430,13 @@ def run_ours(args, rank, world, local):
     flop_per_batch = FLOP_PER_NODE * nodes
 
     pricer = pkg.Pricer(local)
+    if args.network_rows:
+        # the surrogate's fused network kernel alone (profiling runs)
+        res = network_kernel_time(pkg, pricer, args.network_rows, args.steps, args.warmup, dev)
+        if rank == 0:
+            print(json.dumps({"network_kernel": res}))
+        pricer.close()
+        return 0
     mode = {"mixed": pkg.BATCHED_MIXED, "fp64": pkg.BATCHED_FP64, "fp32": pkg.BATCHED_FP32, "df64": pkg.BATCHED_DF64,
             "plain": pkg.PLAIN_FP64}[args.mode]
     # the library's autotuner (hwt_autotune) picks group size, warp-task width
@@ -328,59 +509,25 @@ def run_ours(args, rank, world, local):
             entry.update({"max_abs_err": float(np.max(err)), "p99_abs_err": float(np.percentile(err, 99)),
                           "max_rel_err": float(np.max(err / np.maximum(np.abs(ref_prices), 1e-300)))})
         modes[name] = entry
+    # the other configurations (the 1,000-option book, the skewed batch), untimed
+    configs = None
+    if modes and not args.no_configs and rank == 0:
+        orc_c = g.oracle()
+        orc_c.build()
+        configs = config_runs(pkg, orc_c, pricer, y, reps=3)
     # learned surrogate: trained on tree prices, tree fallback outside its box and
-    # tree judge on 1% of every batch (config 5 plus the uneven batch itself)
+    # tree judge on 1% of every batch: the single-tree box (samples drawn as the
+    # 1,000-option book draws them) and the uneven batch's box
     surrogate = None
-    if modes and not args.no_surrogate:
-        sur = pkg.Surrogate(pricer, seed=1, residual=True)
-        train = pkg.Options.from_batch(wl.surrogate_training_batch(args.sur_samples, 3))
-        tstats = sur.train(train, y, epochs=args.sur_epochs, batch=8192, lr=1e-3)
-        del train
-        for name, tol in (("surrogate_unjudged", 0.0), ("surrogate", 1e-4)):
-            # "surrogate": the judge's 1e-4 bound is enforced (a batch whose judged
-            # error exceeds it is priced by the tree); "surrogate_unjudged": the
-            # network's answers as they are, judge measured but not acted on
-            wall = []
-            for k in range(max(3, min(args.steps, 10))):
-                t0 = time.perf_counter()
-                got = sur.price(opts, y, judge_fraction=0.01, seed=100 + k, tree_mode=pkg.BATCHED_MIXED,
-                                judge_tolerance=tol)
-                wall.append(time.perf_counter() - t0)
-            sst = sur.stats.as_dict()
-            entry = {"options_per_s": n / (sum(wall[1:]) / len(wall[1:])),
-                     "ms_per_step": 1e3 * sum(wall[1:]) / len(wall[1:]), "device_ms": sst["total_ms"],
-                     "judge_tolerance": tol, "fell_back_to_tree": bool(sst["fell_back"]),
-                     "judge_max_abs": sst["judge_max_abs"], "judge_p99_abs": sst["judge_p99_abs"],
-                     "n_judged": sst["n_judged"], "n_routed": sst["n_routed"],
-                     "timing": "host clock around hwt_surrogate_price (host arrays in and out, judge and routing "
-                               "included)"}
-            if ref_prices is not None:
-                err = np.abs(got - ref_prices)
-                entry.update({"max_abs_err": float(np.max(err)), "p99_abs_err": float(np.percentile(err, 99)),
-                              "max_rel_err": float(np.max(err / np.maximum(np.abs(ref_prices), 1e-300)))})
-            modes[name] = entry
-        q = wl.surrogate_query_batch(1_000_000, 4)
-        qo = pkg.Options.from_batch(q)
-        ref_q = pricer.price(qo, y, pkg.BATCHED_FP64)
-        tree_q = pricer.last_stats.total_ms
-        t0 = time.perf_counter()
-        got_q = sur.price(qo, y, judge_fraction=0.01, seed=7, tree_mode=pkg.BATCHED_MIXED)
-        wq = time.perf_counter() - t0
-        qst = sur.stats.as_dict()
-        eq = np.abs(got_q - ref_q)
-        inb = ~q["outside"]
-        surrogate = {"train": tstats, "control_variate": "Hull-White closed form (Jamshidian)",
-                     "queries": {"n": int(qo.N), "outside_box": int(q["outside"].sum()), "options_per_s": qo.N / wq,
-                                 "device_ms": qst["total_ms"], "network_ms": qst["network_ms"],
-                                 "tree_ms": qst["tree_ms"], "judge": {k: qst[k] for k in (
-                                     "n_judged", "judge_max_abs", "judge_p99_abs", "judge_mean_abs")},
-                                 "in_box_max_abs_err": float(np.max(eq[inb])),
-                                 "in_box_p99_abs_err": float(np.percentile(eq[inb], 99)),
-                                 "in_box_median_abs_err": float(np.median(eq[inb])),
-                                 "out_of_box_max_abs_err": float(np.max(eq[~inb])),
-                                 "fp64_tree_ms": tree_q, "x_fp64_tree": tree_q / (wq * 1e3),
-                                 "reference": "batched FP64 tree on the same 1M options"}}
-        sur.close()
+    if modes and not args.no_surrogate and rank == 0:
+        surrogate = {"network_kernel": network_kernel_time(pkg, pricer, 1 << 20, 10, 3, dev)}
+        surrogate["single_tree"] = surrogate_run(
+            pkg, pricer, y, box=wl.single_tree_box(), train=wl.single_tree_training_batch(args.sur_samples, 3),
+            queries=wl.single_tree_query_batch(1_000_000, 4), epochs=args.sur_epochs, reps=3)
+        surrogate["uneven_box"] = surrogate_run(
+            pkg, pricer, y, box=None, train=wl.surrogate_training_batch(args.sur_samples, 3),
+            queries=wl.surrogate_query_batch(1_000_000, 4), epochs=args.sur_epochs_uneven, reps=3)
+        surrogate["uneven_30k"] = surrogate_batch(pkg, pricer, y, opts, ref_prices, args)
     # the reference's seven benchmark distributions (65,536 options each, data/yield.in
     # curve), device time per batch, beside the thesis's best CUDA numbers
     datasets = None
@@ -534,6 +681,17 @@ def run_ours(args, rank, world, local):
             "peaks_measured": {"fp64_tflops": peaks[0], "fp32_tflops": peaks[1]},
             "modes": modes,
         }
+        if modes and cpu is not None:
+            # like-for-like multiples beside the headline (which sets mixed precision
+            # on the GPU against the FP64 CPU pricer)
+            line["like_for_like"] = {
+                "batched_fp64_over_cpu_fp64": modes["batched_fp64"]["options_per_s"] / cpu["value"],
+                "batched_df64_over_cpu_fp64": modes["batched_df64"]["options_per_s"] / cpu["value"],
+                "mixed_over_batched_fp64": modes["batched_mixed"]["options_per_s"] / modes["batched_fp64"]["options_per_s"],
+                "mixed_over_plain_fp64": modes["batched_mixed"]["options_per_s"] / modes["plain_fp64"]["options_per_s"],
+                "note": "all on the same batch; cpu = the FP64 oracle on every host core, the whole batch"}
+        if configs is not None:
+            line["configs"] = configs
         if surrogate is not None:
             line["surrogate"] = surrogate
         if datasets is not None:
@@ -566,8 +724,12 @@ def main():
     ap.add_argument("--skip-survey", action="store_true", help="time only the headline mode (profiling runs)")
     ap.add_argument("--no-surrogate", action="store_true")
     ap.add_argument("--no-datasets", action="store_true", help="skip the seven thesis benchmark distributions")
+    ap.add_argument("--no-configs", action="store_true", help="skip the 1,000-option book and the skewed batch")
+    ap.add_argument("--network-rows", type=int, default=0,
+                    help="time only the surrogate's fused network kernel on this many rows (profiling runs)")
     ap.add_argument("--sur-samples", type=int, default=4_000_000)
-    ap.add_argument("--sur-epochs", type=int, default=24)
+    ap.add_argument("--sur-epochs", type=int, default=400, help="surrogate epochs on the single-tree box")
+    ap.add_argument("--sur-epochs-uneven", type=int, default=48, help="surrogate epochs on the uneven batch's box")
     ap.add_argument("--shard", action="store_true",
                     help="N>1: split the batch across ranks by tree work (LPT) and gather the prices, instead of "
                          "one replica of the whole batch per GPU")

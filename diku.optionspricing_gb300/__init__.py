@@ -536,7 +536,7 @@ class TrainStats(ctypes.Structure):
                 ("y_mean", ctypes.c_double), ("y_std", ctypes.c_double), ("route_threshold", ctypes.c_double),
                 ("holdout_answered", ctypes.c_double), ("holdout_max_abs", ctypes.c_double),
                 ("holdout_p99_abs", ctypes.c_double), ("holdout_all_max_abs", ctypes.c_double),
-                ("holdout", ctypes.c_int64)]
+                ("holdout", ctypes.c_int64), ("n_kinks", ctypes.c_int64), ("kink_delta", ctypes.c_double)]
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_}
@@ -569,6 +569,8 @@ _SIGNATURES.update({
     "hwt_surrogate_forward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
     "hwt_surrogate_forward_ex": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
                                                 ctypes.c_int]),
+    "hwt_surrogate_forward_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                                    ctypes.POINTER(ctypes.c_double)]),
     "hwt_surrogate_inject_stall": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "hwt_surrogate_loss_grads": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                                                 ctypes.c_double, ctypes.POINTER(ctypes.c_double), ctypes.c_void_p]),
@@ -665,6 +667,13 @@ class Surrogate:
         out = np.empty((len(x), 2), dtype=np.float32)
         self._check(lib().hwt_surrogate_forward_ex(self._s, x.ctypes.data, len(x), out.ctypes.data, 0 if fused else 1))
         return out
+
+    def forward_device(self, x_ptr: int, n: int, out_ptr: int) -> float:
+        """Fused kernel on device buffers (x [n][8] float32 with a zero last column,
+        out [n][2] float32); returns the kernel's CUDA-event time in ms."""
+        ms = ctypes.c_double()
+        self._check(lib().hwt_surrogate_forward_device(self._s, x_ptr, n, out_ptr, ctypes.byref(ms)))
+        return ms.value
 
     def loss_grads(self, x: np.ndarray, y: np.ndarray, err_weight: float = 0.0):
         x = np.ascontiguousarray(x, dtype=np.float32)

@@ -8,12 +8,12 @@
 //                         (A operand, K-major core-matrix layout), bf16 weights
 //                         streamed from L2 (B operand), fp32 accumulator in 256
 //                         TMEM columns (M = 128, N = 256, K = 16 per instruction)
-//   layer 4 (256 -> 2):   fp32 dot products of the bf16-rounded activations with
-//                         bf16-rounded weights, in the last layer's epilogue
+//   layer 4 (256 -> 2):   fp32 dot products of layer 3's fp32 activations with fp32
+//                         weights, in the last layer's epilogue
 //
 // Each output row is computed exactly as the layer-by-layer training path computes
-// it (same roundings, same K order of the tensor-core sums; layer 4 sums in another
-// order), so a network trained there evaluates the same here.
+// it (same roundings, same K order of the tensor-core sums, layer 4 summed in the
+// same order), so a network trained there evaluates the same here.
 //
 // Weights of the three tensor-core layers are pre-packed (the surrogate's refresh
 // kernel) into 24 blocks of [256 output rows x 32 K] in the canonical no-swizzle
@@ -63,7 +63,7 @@ struct MlpArgs {
     const float *W0, *b0;      // fp32 [8][256], [256]
     const __nv_bfloat16 *Wp;   // packed blocks of layers 1-3 (see pack_offset)
     const float *b1, *b2, *b3; // [256] biases of layers 1-3
-    const float *W4r;          // [256][2] bf16-rounded weights of layer 4, as float
+    const float *W4;           // [256][2] fp32 weights of layer 4
     const float *b4;           // [2]
     float *out;                // [n][2]
     int *err;
@@ -267,12 +267,11 @@ __global__ void __launch_bounds__(kThreads, 2) mlp_forward_kernel(MlpArgs p)
                     *reinterpret_cast<uint4 *>(act + act_offset(tid, c)) = lo;
                     *reinterpret_cast<uint4 *>(act + act_offset(tid, c + 8)) = hi;
                 } else {
-                    const float4 *w4 = reinterpret_cast<const float4 *>(p.W4r + 2 * c);
+                    const float4 *w4 = reinterpret_cast<const float4 *>(p.W4 + 2 * c);
 #pragma unroll
                     for (int q = 0; q < 8; ++q) {
                         const float4 w = __ldg(w4 + q);  // rows c + 2q, c + 2q + 1, two outputs each
-                        const float h0 = __bfloat162float(__float2bfloat16_rn(umma::silu_f(v[2 * q])));
-                        const float h1 = __bfloat162float(__float2bfloat16_rn(umma::silu_f(v[2 * q + 1])));
+                        const float h0 = umma::silu_f(v[2 * q]), h1 = umma::silu_f(v[2 * q + 1]);
                         o0 = fmaf(h0, w.x, o0); o1 = fmaf(h0, w.y, o1);
                         o0 = fmaf(h1, w.z, o0); o1 = fmaf(h1, w.w, o1);
                     }

@@ -4,9 +4,9 @@
 //             standardised (or price / forward bond price with residual = 0), and
 //   output 1: an estimate of log |output-0 error| (the error head), which routes
 //             the options it does not trust to the tree.
-// Layer 0 runs in fp32 on the CUDA cores from fp32 features; layers 1-4 keep fp32
-// master weights with bf16 copies for the tcgen05 tensor cores, bf16 activations
-// and fp32 accumulation.
+// Layers 0 and 4 run in fp32 on the CUDA cores (layer 0 from fp32 features, layer
+// 4 from the fp32 activations of layer 3); layers 1-3 keep fp32 master weights with
+// bf16 copies for the tcgen05 tensor cores, bf16 activations and fp32 accumulation.
 // Training: Adam with cosine decay on labels priced by the batched FP64 tree, the
 // layer-by-layer tensor-core GEMMs of hwt_umma.cuh, one CUDA graph per step; a
 // held-out slice of the samples calibrates the error head's routing threshold.
@@ -135,6 +135,57 @@ __global__ void dw0_kernel(const float *X, const float *dZ, int n, float *dW0)
     }
     if (r1 > r0)
         for (int k = 0; k < kInPad; ++k) atomicAdd(dW0 + k * kHidden + c, acc[k]);
+}
+
+// Layer 4 of the training path in fp32: out[r][c] = b4[c] + sum_k silu(Z3[r][k]) W4[k][c]
+// (the fused kernel's last epilogue computes the same sum in the same order).
+__global__ void layer4_kernel(const float *Z3, const float *W4, const float *b4, int n, float *out)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    const float *z = Z3 + (size_t)r * kHidden;
+    float o0 = 0.f, o1 = 0.f;
+    for (int k = 0; k < kHidden; ++k) {
+        const float h = silu_f(z[k]);
+        o0 = fmaf(h, __ldg(W4 + 2 * k), o0);
+        o1 = fmaf(h, __ldg(W4 + 2 * k + 1), o1);
+    }
+    out[2 * r] = o0 + __ldg(b4);
+    out[2 * r + 1] = o1 + __ldg(b4 + 1);
+}
+
+// Backward through layer 4 (fp32): dZ3[r][k] = (dZ4[r] . W4[k]) silu'(Z3[r][k]), as
+// bf16 (operand of the next GEMMs) and fp32 (column sums); one warp per row.
+__global__ void layer4_back_kernel(const float *Z3, const float *dZ4, const float *W4, int n, __nv_bfloat16 *dZb,
+                                   float *dZf)
+{
+    const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+    const int r = gt >> 5, lane = gt & 31;
+    if (r >= n) return;
+    const float d0 = dZ4[2 * r], d1 = dZ4[2 * r + 1];
+    for (int k = lane; k < kHidden; k += 32) {
+        const float g = fmaf(d0, __ldg(W4 + 2 * k), d1 * __ldg(W4 + 2 * k + 1)) * dsilu_f(Z3[(size_t)r * kHidden + k]);
+        dZb[(size_t)r * kHidden + k] = __float2bfloat16(g);
+        dZf[(size_t)r * kHidden + k] = g;
+    }
+}
+
+// dW4[k][c] += sum over rows of silu(Z3[r][k]) dZ4[r][c] (fp32), a slice of rows per block.
+__global__ void dw4_kernel(const float *Z3, const float *dZ4, int n, float *dW4)
+{
+    const int k = threadIdx.x;  // kHidden threads
+    const int per = (n + gridDim.x - 1) / gridDim.x;
+    const int r0 = blockIdx.x * per, r1 = min(n, r0 + per);
+    float a0 = 0.f, a1 = 0.f;
+    for (int r = r0; r < r1; ++r) {
+        const float h = silu_f(Z3[(size_t)r * kHidden + k]);
+        a0 = fmaf(h, __ldg(dZ4 + 2 * r), a0);
+        a1 = fmaf(h, __ldg(dZ4 + 2 * r + 1), a1);
+    }
+    if (r1 > r0) {
+        atomicAdd(dW4 + 2 * k, a0);
+        atomicAdd(dW4 + 2 * k + 1, a1);
+    }
 }
 
 // Outputs [n][2] against targets y: r = o0 - y; error-head target g = log(|r| + eps)
@@ -295,9 +346,10 @@ enum Kind : uint8_t {
 // flagged options (the tree answers them), and the judge's draw among the network's
 // answers.  counts[k] = options of kind k (k = 1..3).
 __global__ void decode_route_kernel(const float *out, const double *F, const double *base, const uint8_t *inbox,
-                                    int n, double ymean, double ystd, float log_tau_over_ystd,
-                                    unsigned long long seed, unsigned long long thresh, double *price,
-                                    uint8_t *kind, int32_t *list, int32_t *counts)
+                                    const double *strike, int n, double ymean, double ystd, float log_tau_over_ystd,
+                                    const double *kinks, int n_kinks, double kink_delta, unsigned long long seed,
+                                    unsigned long long thresh, double *price, uint8_t *kind, int32_t *list,
+                                    int32_t *counts)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -308,7 +360,15 @@ __global__ void decode_route_kernel(const float *out, const double *F, const dou
         const float2 o = reinterpret_cast<const float2 *>(out)[i];
         price[i] = base[i] + F[i] * ((double)o.x * ystd + ymean);
         // predicted |price error| = exp(o1) ystd F > tau  <=>  o1 > log(tau / ystd) - log(F)
-        if (o.y > log_tau_over_ystd - logf((float)F[i])) k = KIND_FLAGGED;
+        bool flag = o.y > log_tau_over_ystd - logf((float)F[i]);
+        // a strike within kink_delta (moneyness) of a payoff kink of the box's tree
+        if (n_kinks > 0) {
+            const double x = strike[i] / F[i];
+            double d = INFINITY;
+            for (int j = 0; j < n_kinks; ++j) d = fmin(d, fabs(x - kinks[j]));
+            flag = flag || d <= kink_delta;
+        }
+        if (flag) k = KIND_FLAGGED;
         else if (mix64(seed ^ (unsigned long long)i) < thresh) k = KIND_JUDGED;
     }
     kind[i] = k;
@@ -453,6 +513,11 @@ struct hwt_surrogate {
     FeatureNorm fn;
     double ymean = 0.0, ystd = 1.0;
     double route_tau = INFINITY;  // price error the error head's routing keeps network answers under
+    // Single-tree boxes: the payoff kinks of the box's tree in moneyness (from the
+    // training labels) and the distance from them inside which options go to the tree
+    std::vector<double> kinks;
+    double kink_delta = -1.0;     // < 0: no kink routing
+    Buf<double> dkinks;
     int trained = 0;
     std::string err;
     // parameters (fp32 masters) and Adam state, one flat buffer each
@@ -461,7 +526,6 @@ struct hwt_surrogate {
     size_t w_off[kLayers], b_off[kLayers];
     __nv_bfloat16 *d_wt[kLayers] = {}, *d_wb[kLayers] = {};  // layers 1-4
     __nv_bfloat16 *d_wp = nullptr;                           // packed blocks of layers 1-3
-    float *d_w4r = nullptr;                                  // bf16-rounded layer-4 weights
     long adam_t = 0;
     // training activations for one batch
     int act_cap = 0;
@@ -470,6 +534,7 @@ struct hwt_surrogate {
     float *d_z[kLayers] = {};              // pre-activations (z[4] = outputs [rows][2])
     __nv_bfloat16 *d_dz = nullptr, *d_dz2 = nullptr;
     float *d_dzf = nullptr;
+    float *d_dz4 = nullptr;                // [rows][2] fp32 output gradients
     double *d_loss = nullptr;
     float *d_y = nullptr;
     int *d_gemm_err = nullptr;  // raised by a kernel whose mbarrier wait ran out
@@ -513,8 +578,8 @@ int ensure_act(hwt_surrogate *s, int rows)
         cudaFree(s->d_h[l]); s->d_h[l] = nullptr;
         cudaFree(s->d_z[l]); s->d_z[l] = nullptr;
     }
-    cudaFree(s->d_dz); cudaFree(s->d_dz2); cudaFree(s->d_dzf); cudaFree(s->d_y);
-    s->d_dz = s->d_dz2 = nullptr; s->d_dzf = nullptr; s->d_y = nullptr;
+    cudaFree(s->d_dz); cudaFree(s->d_dz2); cudaFree(s->d_dzf); cudaFree(s->d_y); cudaFree(s->d_dz4);
+    s->d_dz = s->d_dz2 = nullptr; s->d_dzf = nullptr; s->d_y = nullptr; s->d_dz4 = nullptr;
     s->act_cap = 0;
     SCUDA(s, cudaMalloc(&s->d_x, sizeof(float) * (size_t)rows * kInPad), "alloc X");
     for (int l = 1; l < kLayers; ++l) SCUDA(s, cudaMalloc(&s->d_h[l], sizeof(__nv_bfloat16) * (size_t)rows * kHidden), "alloc H");
@@ -523,6 +588,7 @@ int ensure_act(hwt_surrogate *s, int rows)
     SCUDA(s, cudaMalloc(&s->d_dz2, sizeof(__nv_bfloat16) * (size_t)rows * kHidden), "alloc dZ");
     SCUDA(s, cudaMalloc(&s->d_dzf, sizeof(float) * (size_t)rows * kHidden), "alloc dZf");
     SCUDA(s, cudaMalloc(&s->d_y, sizeof(float) * (size_t)rows), "alloc y");
+    SCUDA(s, cudaMalloc(&s->d_dz4, sizeof(float) * (size_t)rows * kOut), "alloc dZ4");
     s->act_cap = rows;
     return HWT_OK;
 }
@@ -594,17 +660,20 @@ int forward_layers(hwt_surrogate *s, int rows)
     layer0_kernel<<<(rows * 32 + 255) / 256, 256, 0, s->stream>>>(s->d_x, s->d_w + s->w_off[0], s->d_w + s->b_off[0],
                                                                   rows, s->d_z[0], s->d_h[1]);
     SCUDA(s, cudaGetLastError(), "layer 0");
-    for (int l = 1; l < kLayers; ++l) {
-        const bool last = l == kLayers - 1;
-        GemmArgs g = gargs(s, s->d_h[l], s->d_wt[l], rows, kFanOut[l], kFanIn[l], kFanIn[l], kFanIn[l],
-                           last ? EPI_BIAS : EPI_BIAS_SILU);
+    for (int l = 1; l < kLayers - 1; ++l) {
+        const bool to_last = l == kLayers - 2;  // layer 4 reads fp32 Z3, not bf16 activations
+        GemmArgs g = gargs(s, s->d_h[l], s->d_wt[l], rows, kFanOut[l], kFanIn[l], kFanIn[l], kFanIn[l], EPI_BIAS_SILU);
         g.bias = s->d_w + s->b_off[l];
         g.Cf = s->d_z[l];
         g.ldc = kFanOut[l];
-        g.Cb = last ? nullptr : s->d_h[l + 1];
+        g.Cb = to_last ? nullptr : s->d_h[l + 1];
         g.ldcb = kFanOut[l];
+        if (to_last) g.epi = EPI_BIAS;
         SCUDA(s, (gemm<false, false>(g, 1, s->stream)), "forward gemm");
     }
+    layer4_kernel<<<(rows + 127) / 128, 128, 0, s->stream>>>(s->d_z[kLayers - 2], s->d_w + s->w_off[kLayers - 1],
+                                                             s->d_w + s->b_off[kLayers - 1], rows, s->d_z[kLayers - 1]);
+    SCUDA(s, cudaGetLastError(), "layer 4");
     return HWT_OK;
 }
 
@@ -621,7 +690,7 @@ int forward_fused(hwt_surrogate *s, const float *X, int rows, float *out)
     a.b1 = s->d_w + s->b_off[1];
     a.b2 = s->d_w + s->b_off[2];
     a.b3 = s->d_w + s->b_off[3];
-    a.W4r = s->d_w4r;
+    a.W4 = s->d_w + s->w_off[kLayers - 1];
     a.b4 = s->d_w + s->b_off[4];
     a.out = out;
     a.err = s->d_gemm_err;
@@ -638,14 +707,28 @@ int backward(hwt_surrogate *s, int rows, float lam, bool zero_loss)
 {
     SCUDA(s, cudaMemsetAsync(s->d_g, 0, sizeof(float) * s->n_params, s->stream), "zero grads");
     if (zero_loss) SCUDA(s, cudaMemsetAsync(s->d_loss, 0, sizeof(double), s->stream), "zero loss");
-    loss_kernel<<<(rows + 255) / 256, 256, 0, s->stream>>>(s->d_z[kLayers - 1], s->d_y, rows, lam, s->d_dz, s->d_dzf,
+    loss_kernel<<<(rows + 255) / 256, 256, 0, s->stream>>>(s->d_z[kLayers - 1], s->d_y, rows, lam, s->d_dz, s->d_dz4,
                                                            s->d_loss);
     SCUDA(s, cudaGetLastError(), "loss kernel");
     __nv_bfloat16 *dz = s->d_dz, *dz_next = s->d_dz2;
     const int splits = std::max(1, std::min(64, rows / 512));
     int kc = (rows + splits - 1) / splits;
     kc = (kc + BK - 1) / BK * BK;
-    for (int l = kLayers - 1; l >= 1; --l) {
+    // layer 4 in fp32: dW4 = silu(Z3)^T dZ4, db4 = column sums of dZ4, dZ3 = (dZ4 W4^T) silu'(Z3)
+    {
+        const float *dz4 = s->d_dz4;
+        dw4_kernel<<<std::max(1, std::min(256, rows / 32)), kHidden, 0, s->stream>>>(s->d_z[kLayers - 2], dz4, rows,
+                                                                                     s->d_g + s->w_off[kLayers - 1]);
+        SCUDA(s, cudaGetLastError(), "dW4 kernel");
+        dim3 cg(1, std::max(1, std::min(256, rows / 32)));
+        colsum_kernel<<<cg, 256, 0, s->stream>>>(dz4, rows, kOut, kOut, s->d_g + s->b_off[kLayers - 1]);
+        SCUDA(s, cudaGetLastError(), "db4 kernel");
+        layer4_back_kernel<<<(rows * 32 + 255) / 256, 256, 0, s->stream>>>(s->d_z[kLayers - 2], dz4,
+                                                                           s->d_w + s->w_off[kLayers - 1], rows, dz,
+                                                                           s->d_dzf);
+        SCUDA(s, cudaGetLastError(), "layer 4 backward");
+    }
+    for (int l = kLayers - 2; l >= 1; --l) {
         const int in = kFanIn[l], out = kFanOut[l];
         // dW_l[in][out] = H_l^T dZ_l   (split-K over the batch)
         GemmArgs gw = gargs(s, s->d_h[l], dz, in, out, rows, in, out, EPI_ATOMIC);
@@ -679,11 +762,11 @@ int backward(hwt_surrogate *s, int rows, float lam, bool zero_loss)
 
 int refresh(hwt_surrogate *s)
 {
-    for (int l = 1; l < kLayers; ++l) {
+    for (int l = 1; l < kLayers - 1; ++l) {  // layer 4 stays fp32
         const int tot = kFanIn[l] * kFanOut[l];
-        __nv_bfloat16 *wp = l <= mlp::kTcLayers ? s->d_wp + (size_t)(l - 1) * mlp::kBlocksPerLayer * mlp::kWBlockElems : nullptr;
+        __nv_bfloat16 *wp = s->d_wp + (size_t)(l - 1) * mlp::kBlocksPerLayer * mlp::kWBlockElems;
         refresh_kernel<<<(tot + 255) / 256, 256, 0, s->stream>>>(s->d_w + s->w_off[l], kFanIn[l], kFanOut[l], s->d_wt[l],
-                                                               s->d_wb[l], wp, l == kLayers - 1 ? s->d_w4r : nullptr);
+                                                               s->d_wb[l], wp, nullptr);
         SCUDA(s, cudaGetLastError(), "refresh kernel");
     }
     return HWT_OK;
@@ -786,9 +869,8 @@ hwt_surrogate *hwt_surrogate_create(hwt_ctx *ctx, const hwt_box *box, uint64_t s
          cudaMalloc(&s->d_v, 4 * off) == cudaSuccess && cudaMalloc(&s->d_g, 4 * off) == cudaSuccess &&
          cudaMalloc(&s->d_loss, sizeof(double)) == cudaSuccess &&
          cudaMalloc(&s->d_gemm_err, sizeof(int)) == cudaSuccess && cudaMemset(s->d_gemm_err, 0, sizeof(int)) == cudaSuccess &&
-         cudaMalloc(&s->d_wp, 2ull * mlp::kBlocks * mlp::kWBlockElems) == cudaSuccess &&
-         cudaMalloc(&s->d_w4r, 4ull * kHidden * kOut) == cudaSuccess;
-    for (int l = 1; l < kLayers && ok; ++l) {
+         cudaMalloc(&s->d_wp, 2ull * mlp::kBlocks * mlp::kWBlockElems) == cudaSuccess;
+    for (int l = 1; l < kLayers - 1 && ok; ++l) {
         ok = cudaMalloc(&s->d_wt[l], 2 * (size_t)kFanIn[l] * kFanOut[l]) == cudaSuccess &&
              cudaMalloc(&s->d_wb[l], 2 * (size_t)kFanIn[l] * kFanOut[l]) == cudaSuccess;
     }
@@ -831,14 +913,14 @@ void hwt_surrogate_destroy(hwt_surrogate *s)
     if (!s) return;
     if (s->stream) cudaStreamSynchronize(s->stream);
     cudaFree(s->d_w); cudaFree(s->d_m); cudaFree(s->d_v); cudaFree(s->d_g); cudaFree(s->d_loss); cudaFree(s->d_gemm_err);
-    cudaFree(s->d_wp); cudaFree(s->d_w4r); cudaFree(s->d_x);
+    cudaFree(s->d_wp); cudaFree(s->d_x);
     for (int l = 0; l < kLayers; ++l) { cudaFree(s->d_wt[l]); cudaFree(s->d_wb[l]); cudaFree(s->d_z[l]); cudaFree(s->d_h[l]); }
-    cudaFree(s->d_dz); cudaFree(s->d_dz2); cudaFree(s->d_dzf); cudaFree(s->d_y);
+    cudaFree(s->d_dz); cudaFree(s->d_dz2); cudaFree(s->d_dzf); cudaFree(s->d_y); cudaFree(s->d_dz4);
     free_batch(s->opts);
     free_batch(s->sub);
     s->xf.release(); s->out2.release(); s->F.release(); s->base.release(); s->price.release(); s->tree.release();
     s->errs.release(); s->inbox.release(); s->kind.release(); s->list.release(); s->counts.release();
-    s->crate.release(); s->crate_f.release(); s->cday.release();
+    s->crate.release(); s->crate_f.release(); s->cday.release(); s->dkinks.release();
     for (auto &e : s->ev)
         if (e) cudaEventDestroy(e);
     if (s->stream) cudaStreamDestroy(s->stream);
@@ -906,6 +988,24 @@ int hwt_surrogate_forward_ex(hwt_surrogate *s, const float *x, int n, float *out
 int hwt_surrogate_forward(hwt_surrogate *s, const float *x, int n, float *out)
 {
     return hwt_surrogate_forward_ex(s, x, n, out, 0);
+}
+
+int hwt_surrogate_forward_device(hwt_surrogate *s, const float *dev_x, int n, float *dev_out, double *kernel_ms)
+{
+    if (!s || !dev_x || !dev_out || n <= 0) return HWT_EINVAL;
+    if ((reinterpret_cast<uintptr_t>(dev_x) & 15) != 0 || (reinterpret_cast<uintptr_t>(dev_out) & 7) != 0)
+        return sfail(s, HWT_EINVAL, "feature rows must start on 16-byte boundaries, outputs on 8");
+    SCUDA(s, cudaEventRecord(s->ev[0], s->stream), "event");
+    int r = forward_fused(s, dev_x, n, dev_out);
+    if (r) return r;
+    SCUDA(s, cudaEventRecord(s->ev[1], s->stream), "event");
+    SCUDA(s, cudaEventSynchronize(s->ev[1]), "forward");
+    if (kernel_ms) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, s->ev[0], s->ev[1]);
+        *kernel_ms = ms;
+    }
+    return gemm_status(s);
 }
 
 int hwt_surrogate_loss_grads(hwt_surrogate *s, const float *x, const float *y, int n, double err_weight, double *loss,
@@ -1006,6 +1106,61 @@ double calibrate_tau(const std::vector<double> &pred, const std::vector<double> 
     return tau;
 }
 
+constexpr int kMaxKinks = 256;
+
+// A box that pins every tree parameter (maturities, a, sigma, steps): all its
+// options share one tree, and only strike and type vary.
+bool single_tree_box(const hwt_box &b)
+{
+    return b.t_min == b.t_max && b.span_min == b.span_max && b.a_min == b.a_max && b.sigma_min == b.sigma_max &&
+           b.steps_min == b.steps_max;
+}
+
+// Payoff kinks of one tree as moneyness values x = strike / F, from labelled
+// samples (x, price) of one option type.  The tree's price is piecewise linear in
+// the strike: the root value is a fixed linear combination of the maturity row's
+// payoffs max(+-(bond value - strike), 0), so its slope changes exactly where the
+// strike crosses a maturity-node bond value.  A slope change above `thr` (price per
+// unit of moneyness) between consecutive samples at least 1e-8 apart marks one.
+void detect_kinks(std::vector<std::pair<double, double>> &pts, double thr, std::vector<double> &out)
+{
+    std::sort(pts.begin(), pts.end());
+    std::vector<std::pair<double, double>> q;
+    q.reserve(pts.size());
+    for (const auto &pt : pts)
+        if (q.empty() || pt.first - q.back().first > 1e-8) q.push_back(pt);
+    for (size_t i = 2; i < q.size(); ++i) {
+        const double s0 = (q[i - 1].second - q[i - 2].second) / (q[i - 1].first - q[i - 2].first);
+        const double s1 = (q[i].second - q[i - 1].second) / (q[i].first - q[i - 1].first);
+        if (fabs(s1 - s0) > thr) out.push_back(q[i - 1].first);
+    }
+}
+
+// Sorted kinks, detections closer than 1e-4 in moneyness merged to their midpoint
+// (one kink is detected on both sides of the sample gap it falls in, and once per
+// option type; neighbouring kinks of a tree are about B(T - t) dr apart in log
+// moneyness, 2e-2 for the book's tree).
+std::vector<double> merge_kinks(std::vector<double> k)
+{
+    std::sort(k.begin(), k.end());
+    std::vector<double> m;
+    size_t i = 0;
+    while (i < k.size()) {
+        size_t j = i;
+        while (j + 1 < k.size() && k[j + 1] - k[i] <= 1e-4) ++j;
+        m.push_back(0.5 * (k[i] + k[j]));
+        i = j + 1;
+    }
+    return m;
+}
+
+double kink_distance(const std::vector<double> &kinks, double x)
+{
+    double d = INFINITY;
+    for (double k : kinks) d = std::min(d, fabs(x - k));
+    return d;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1058,6 +1213,22 @@ int hwt_surrogate_train(hwt_surrogate *s, const hwt_options *samples, const hwt_
     const int64_t nin = (int64_t)idx.size();
     const int64_t nhold = (int64_t)(holdout * nin);
     const int64_t ntrain = nin - nhold;
+    // single-tree box: the tree's payoff kinks from the training part's labels
+    s->kinks.clear();
+    s->kink_delta = -1.0;
+    if (single_tree_box(s->box)) {
+        std::vector<double> k;
+        for (int type = 0; type <= 1; ++type) {
+            std::vector<std::pair<double, double>> pts;
+            for (int64_t j = 0; j < ntrain; ++j) {
+                const int i = idx[j];
+                if (samples->type[i] == type) pts.emplace_back(samples->strike[i] / Fh[i], price[i]);
+            }
+            detect_kinks(pts, 1e-3, k);
+        }
+        s->kinks = merge_kinks(k);
+        if (s->kinks.size() > (size_t)kMaxKinks) s->kinks.clear();  // not one tree after all
+    }
     if (ntrain < batch) return sfail(s, HWT_EINVAL, "fewer in-box training samples than one batch");
     double sum = 0, sum2 = 0;
     for (int64_t j = 0; j < ntrain; ++j) {
@@ -1170,6 +1341,26 @@ int hwt_surrogate_train(hwt_surrogate *s, const hwt_options *samples, const hwt_
         }
         if (lam > 0) {
             s->route_tau = calibrate_tau(pred, err, route_tol, &answered, &max_ans, &p99_ans);
+        } else if (!s->kinks.empty()) {
+            // the smallest distance from the kinks beyond which every held-out answer
+            // is within the tolerance
+            std::vector<double> d(nhold);
+            double delta = 0.0;
+            for (int64_t j = 0; j < nhold; ++j) {
+                const int i = hold[j];
+                d[j] = kink_distance(s->kinks, samples->strike[i] / Fh[i]);
+                if (!(err[j] <= route_tol)) delta = std::max(delta, d[j]);
+            }
+            s->kink_delta = delta;
+            std::vector<double> e;
+            for (int64_t j = 0; j < nhold; ++j)
+                if (d[j] > delta) e.push_back(err[j]);
+            answered = (double)e.size() / nhold;
+            if (!e.empty()) {
+                std::sort(e.begin(), e.end());
+                max_ans = e.back();
+                p99_ans = e[std::min(e.size() - 1, (size_t)floor(0.99 * (e.size() - 1)))];
+            }
         } else {
             std::vector<double> e = err;
             std::sort(e.begin(), e.end());
@@ -1193,6 +1384,8 @@ int hwt_surrogate_train(hwt_surrogate *s, const hwt_options *samples, const hwt_
         stats->holdout_p99_abs = p99_ans;
         stats->holdout_all_max_abs = max_all;
         stats->holdout = nhold;
+        stats->n_kinks = (int64_t)s->kinks.size();
+        stats->kink_delta = s->kink_delta;
     }
     return HWT_OK;
 }
@@ -1220,9 +1413,15 @@ int hwt_surrogate_price(hwt_surrogate *s, const hwt_options *o, const hwt_yield 
     // flag when exp(o1) ystd F > tau; tau = +inf: the router is off, tau <= 0: nothing is answered
     const float log_tau = std::isinf(s->route_tau) ? INFINITY
                           : (s->route_tau > 0 ? (float)log(s->route_tau / s->ystd) : -INFINITY);
-    decode_route_kernel<<<(n + 255) / 256, 256, 0, s->stream>>>(s->out2.p, s->F.p, s->base.p, s->inbox.p, n, s->ymean,
-                                                               s->ystd, log_tau, seed, thresh, s->price.p, s->kind.p,
-                                                               s->list.p, s->counts.p);
+    const int nk = s->kink_delta >= 0 ? (int)s->kinks.size() : 0;
+    if (nk > 0) {
+        if (!s->dkinks.grow(kMaxKinks)) return sfail(s, HWT_ENOMEM, "kink buffer");
+        SCUDA(s, cudaMemcpyAsync(s->dkinks.p, s->kinks.data(), 8ull * nk, cudaMemcpyHostToDevice, s->stream), "kinks H2D");
+    }
+    decode_route_kernel<<<(n + 255) / 256, 256, 0, s->stream>>>(s->out2.p, s->F.p, s->base.p, s->inbox.p,
+                                                               s->opts.strike, n, s->ymean, s->ystd, log_tau,
+                                                               s->dkinks.p, nk, s->kink_delta, seed, thresh,
+                                                               s->price.p, s->kind.p, s->list.p, s->counts.p);
     SCUDA(s, cudaGetLastError(), "decode kernel");
     SCUDA(s, cudaEventRecord(s->ev[1], s->stream), "event");
     int32_t cnt[4] = {0, 0, 0, 0};
@@ -1331,11 +1530,13 @@ int hwt_surrogate_save(const hwt_surrogate *s, const char *path)
         return HWT_ECUDA;
     FILE *f = fopen(path, "wb");
     if (!f) return HWT_EINVAL;
-    const uint32_t magic = 0x48575453u, version = 2;
-    const uint64_t np = s->n_params;
+    const uint32_t magic = 0x48575453u, version = 3;
+    const uint64_t np = s->n_params, nk = s->kinks.size();
     const int64_t t = s->adam_t;
     bool ok = fwrite(&magic, 4, 1, f) == 1 && fwrite(&version, 4, 1, f) == 1 && fwrite(&s->box, sizeof(hwt_box), 1, f) == 1 &&
               fwrite(&s->ymean, 8, 1, f) == 1 && fwrite(&s->ystd, 8, 1, f) == 1 && fwrite(&s->route_tau, 8, 1, f) == 1 &&
+              fwrite(&s->kink_delta, 8, 1, f) == 1 && fwrite(&nk, 8, 1, f) == 1 &&
+              (nk == 0 || fwrite(s->kinks.data(), 8, nk, f) == nk) &&
               fwrite(&t, 8, 1, f) == 1 && fwrite(&np, 8, 1, f) == 1 && fwrite(w.data(), 4, np, f) == np &&
               fwrite(m.data(), 4, np, f) == np && fwrite(v.data(), 4, np, f) == np;
     fclose(f);
@@ -1351,10 +1552,17 @@ int hwt_surrogate_load(hwt_surrogate *s, const char *path)
     uint64_t np = 0;
     int64_t t = 0;
     hwt_box box;
-    double ym = 0, ysd = 1, tau = INFINITY;
-    bool ok = fread(&magic, 4, 1, f) == 1 && fread(&version, 4, 1, f) == 1 && magic == 0x48575453u && version == 2 &&
+    double ym = 0, ysd = 1, tau = INFINITY, kd = -1.0;
+    uint64_t nk = 0;
+    std::vector<double> kinks;
+    bool ok = fread(&magic, 4, 1, f) == 1 && fread(&version, 4, 1, f) == 1 && magic == 0x48575453u && version == 3 &&
               fread(&box, sizeof(hwt_box), 1, f) == 1 && fread(&ym, 8, 1, f) == 1 && fread(&ysd, 8, 1, f) == 1 &&
-              fread(&tau, 8, 1, f) == 1 && fread(&t, 8, 1, f) == 1 && fread(&np, 8, 1, f) == 1 && np == s->n_params;
+              fread(&tau, 8, 1, f) == 1 && fread(&kd, 8, 1, f) == 1 && fread(&nk, 8, 1, f) == 1 && nk <= (uint64_t)kMaxKinks;
+    if (ok && nk) {
+        kinks.resize(nk);
+        ok = fread(kinks.data(), 8, nk, f) == nk;
+    }
+    ok = ok && fread(&t, 8, 1, f) == 1 && fread(&np, 8, 1, f) == 1 && np == s->n_params;
     std::vector<float> w(s->n_params), m(s->n_params), v(s->n_params);
     ok = ok && fread(w.data(), 4, np, f) == np && fread(m.data(), 4, np, f) == np && fread(v.data(), 4, np, f) == np;
     fclose(f);
@@ -1364,6 +1572,8 @@ int hwt_surrogate_load(hwt_surrogate *s, const char *path)
     s->ymean = ym;
     s->ystd = ysd;
     s->route_tau = tau;
+    s->kink_delta = kd;
+    s->kinks = kinks;
     s->adam_t = t;
     SCUDA(s, cudaMemcpy(s->d_w, w.data(), 4 * np, cudaMemcpyHostToDevice), "load");
     SCUDA(s, cudaMemcpy(s->d_m, m.data(), 4 * np, cudaMemcpyHostToDevice), "load");

@@ -256,7 +256,8 @@ typedef struct hwt_train_config {
     uint64_t seed;                   /* shuffling and the held-out split */
     double err_weight;               /* weight of the error head's loss; 0: head untrained, no routing */
     double route_tolerance;          /* price error (per 100 face) that the network's answers must keep
-                                        on the held-out samples; sets the routing threshold (default 1e-4) */
+                                        on the held-out samples; sets the routing threshold of the error
+                                        head or, on a single-tree box, the kink distance (default 1e-4) */
     double holdout;                  /* fraction of in-box samples held out for that (default 0.05) */
 } hwt_train_config;
 
@@ -272,6 +273,9 @@ typedef struct hwt_train_stats {
     double holdout_max_abs, holdout_p99_abs; /* |network - tree| over those it answers */
     double holdout_all_max_abs;      /* |network - tree| over all held-out samples */
     int64_t holdout;                 /* held-out samples */
+    int64_t n_kinks;                 /* single-tree box: payoff kinks found in the labels */
+    double kink_delta;               /* options closer than this (moneyness) to a kink go to the tree
+                                        (< 0: no kink routing) */
 } hwt_train_stats;
 
 typedef struct hwt_surrogate_stats {
@@ -294,8 +298,11 @@ const char *hwt_surrogate_last_error(const hwt_surrogate *s);
  * but a held-out slice, and sets the routing threshold on that slice. */
 int hwt_surrogate_train(hwt_surrogate *s, const hwt_options *samples, const hwt_yield *yield,
                         const hwt_train_config *cfg, hwt_train_stats *stats);
-/* Prices host options: network inside the box unless the error head flags the
- * option, tree (tree_mode: a batched mode) outside the box, for flagged options
+/* Prices host options: network inside the box unless the option is flagged - by
+ * the error head, or, on a single-tree box (every tree parameter pinned, so the
+ * price is piecewise linear in the strike), by a strike within the calibrated
+ * distance of one of the tree's payoff kinks, which training finds in its labels -
+ * tree (tree_mode: a batched mode) outside the box, for flagged options
  * and for the judge's sample (fraction judge_fraction of the in-box options the
  * network answers, drawn from `seed`), whose options get the tree price.  If
  * judge_tolerance > 0 and the judge's largest |network - tree| exceeds it, the
@@ -317,6 +324,11 @@ int hwt_surrogate_params(hwt_surrogate *s, float *params, int64_t count, int set
  * hwt_surrogate_forward is path 0. */
 int hwt_surrogate_forward(hwt_surrogate *s, const float *x, int n, float *out);
 int hwt_surrogate_forward_ex(hwt_surrogate *s, const float *x, int n, float *out, int path);
+/* The fused inference kernel on DEVICE buffers of the surrogate's device: dev_x
+ * [n][8] standardised features with a zero eighth column (16-byte aligned rows),
+ * dev_out [n][2]; waits for the kernel and returns its CUDA-event time in
+ * *kernel_ms (may be NULL). */
+int hwt_surrogate_forward_device(hwt_surrogate *s, const float *dev_x, int n, float *dev_out, double *kernel_ms);
 /* Loss and gradients (no update) of the training path on x [n][7] and standardised
  * targets y [n]: 0.5 mean (o0 - y)^2 + err_weight 0.5 mean (o1 - log(|o0 - y| +
  * 1e-3))^2, the error-head target held constant; gradients in the params layout.

@@ -7,11 +7,11 @@ restatement is the oracle for the GPU forward pass, the gradients and the Adam
 step; it is itself checked by central finite differences (tests/test_mlp_oracle.py).
 
 Layout matches the GPU kernels: W_l is [fan_in, fan_out] row-major, y = x W + b.
-The GPU computes layer 0 in fp32 from fp32 features, and keeps bf16 copies of the
-weights of layers 1-4 and bf16 activations between layers with fp32 accumulation;
-`forward(..., bf16=True)` rounds the same tensors the same way (layer 0's inputs
-and weights are not rounded) so the comparison isolates accumulation-order and
-activation-approximation differences.
+The GPU computes layers 0 and 4 in fp32 (layer 0 from fp32 features, layer 4 from
+layer 3's fp32 activations) and keeps bf16 copies of the weights of layers 1-3 and
+bf16 activations between them with fp32 accumulation; `forward(..., bf16=True)`
+rounds the same tensors the same way so the comparison isolates accumulation-order
+and activation-approximation differences.
 
 Loss: 0.5 mean((o0 - y)^2) + err_weight * 0.5 mean((o1 - log(|o0 - y| + eps))^2),
 the error head's target held constant (no gradient flows through it).
@@ -61,13 +61,13 @@ def forward(params, x, bf16: bool = False):
     inputs, pre = [], []
     last = len(params) - 1
     for li, (W, b) in enumerate(params):
-        Wq = bf16_round(W) if (bf16 and li > 0) else W
+        Wq = bf16_round(W) if (bf16 and 0 < li < last) else W
         inputs.append(h)
         z = h @ Wq + b
         pre.append(z)
         if li < last:
             h = silu(z)
-            if bf16:
+            if bf16 and li < last - 1:  # the last layer reads fp32 activations
                 h = bf16_round(h)
         else:
             h = z
@@ -91,7 +91,7 @@ def loss_and_grads(params, x, y, bf16: bool = False, err_weight: float = 0.0, ep
     last = len(params) - 1
     for li in range(last, -1, -1):
         W, _ = params[li]
-        Wq = bf16_round(W) if bf16 else W
+        Wq = bf16_round(W) if (bf16 and 0 < li < last) else W
         if li < last:
             g = g * dsilu(cache["pre"][li])
         a = cache["inputs"][li]

@@ -174,3 +174,37 @@ def test_bounded_wait_reports_timeout_and_context_survives(pkg, sur, mode):
     assert np.array_equal(sur.forward(x, fused=False), ok_layers)
     # (the loss is summed with double atomics: equal up to summation order)
     assert abs(sur.loss_grads(x, y)[0] - ok_loss) <= 1e-12 * abs(ok_loss)
+
+
+def test_kink_routing_on_the_single_tree_box(pkg, pricer, orc):
+    """On a box that pins every tree parameter the tree's price is piecewise linear
+    in the strike; training finds the kinks in its labels (the maturity row's bond
+    values), and options within the calibrated distance of one go to the tree."""
+    wl = pkg.workloads
+    rates, days = wl.yield_curve()
+    y = pkg.Yield(rates, days)
+    s = pkg.Surrogate(pricer, box=wl.single_tree_box(), seed=4)
+    train = pkg.Options.from_batch(wl.single_tree_training_batch(200_000, seed=31))
+    st = s.train(train, y, epochs=4, batch=8192, lr=1e-3, route_tolerance=2e-3, holdout=0.1)
+    # the book's tree (t = 5 y, T = 10 y, 12 steps/year) has 12 kinks between strikes 75 and 95
+    assert st["n_kinks"] == 12, st["n_kinks"]
+    assert st["kink_delta"] >= 0.0 and st["holdout_max_abs"] <= 2e-3
+    # kinks are where the oracle's price changes slope
+    q = wl.single_tree_query_batch(20_000, seed=33)
+    opts = pkg.Options.from_batch(q)
+    got = s.price(opts, y, judge_fraction=0.02, seed=3, tree_mode=pkg.BATCHED_FP64)
+    stats = s.stats.as_dict()
+    ref = orc.price(opts, y, "f64")
+    assert stats["n_network"] + stats["n_flagged"] + stats["n_routed"] == opts.N
+    tree_priced = np.abs(got - ref) <= 1e-10 * np.abs(ref) + 1e-12
+    assert tree_priced.sum() >= stats["n_routed"] + stats["n_flagged"]
+    # a checkpoint keeps the kinks and the routing distance
+    s2 = pkg.Surrogate(pricer, seed=9)
+    import tempfile
+    with tempfile.TemporaryDirectory() as d:
+        s.save(os.path.join(d, "k.bin"))
+        s2.load(os.path.join(d, "k.bin"))
+    got2 = s2.price(opts, y, judge_fraction=0.02, seed=3, tree_mode=pkg.BATCHED_FP64)
+    assert np.array_equal(got, got2) and s2.stats.as_dict()["n_flagged"] == stats["n_flagged"]
+    s.close()
+    s2.close()
