@@ -536,10 +536,14 @@ class TrainStats(ctypes.Structure):
                 ("y_mean", ctypes.c_double), ("y_std", ctypes.c_double), ("route_threshold", ctypes.c_double),
                 ("holdout_answered", ctypes.c_double), ("holdout_max_abs", ctypes.c_double),
                 ("holdout_p99_abs", ctypes.c_double), ("holdout_all_max_abs", ctypes.c_double),
-                ("holdout", ctypes.c_int64), ("n_kinks", ctypes.c_int64), ("kink_delta", ctypes.c_double)]
+                ("holdout", ctypes.c_int64), ("n_kinks", ctypes.c_int64), ("kink_delta", ctypes.c_double),
+                ("ladder_tolerance", ctypes.c_double * 7), ("ladder_answered", ctypes.c_double * 7)]
 
     def as_dict(self) -> dict:
-        return {name: getattr(self, name) for name, _ in self._fields_}
+        d = {name: getattr(self, name) for name, _ in self._fields_}
+        d["ladder_tolerance"] = list(d["ladder_tolerance"])
+        d["ladder_answered"] = list(d["ladder_answered"])
+        return d
 
 
 class SurrogateStats(ctypes.Structure):
@@ -547,7 +551,7 @@ class SurrogateStats(ctypes.Structure):
                 ("fell_back", ctypes.c_int32), ("pad", ctypes.c_int32), ("judge_max_abs", ctypes.c_double), ("judge_p99_abs", ctypes.c_double),
                 ("judge_mean_abs", ctypes.c_double), ("network_ms", ctypes.c_double), ("tree_ms", ctypes.c_double),
                 ("route_ms", ctypes.c_double), ("total_ms", ctypes.c_double), ("n_flagged", ctypes.c_int64),
-                ("n_network", ctypes.c_int64)]
+                ("n_network", ctypes.c_int64), ("route_tolerance", ctypes.c_double)]
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_}

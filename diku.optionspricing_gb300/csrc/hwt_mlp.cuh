@@ -9,21 +9,25 @@
 //                         streamed from L2 (B operand), fp32 accumulator in 256
 //                         TMEM columns (M = 128, N = 256, K = 16 per instruction)
 //   layer 4 (256 -> 2):   fp32 dot products of layer 3's fp32 activations with fp32
-//                         weights, in the last layer's epilogue
+//                         weights, in the last layer's epilogue: a partial sum per
+//                         128 columns (k in order from 0), the two partials added
 //
 // Each output row is computed exactly as the layer-by-layer training path computes
 // it (same roundings, same K order of the tensor-core sums, layer 4 summed in the
 // same order), so a network trained there evaluates the same here.
 //
+// The fp32 constants (layer 0's weights and bias, the biases of layers 1-3, layer 4's
+// weights and bias; 14 KB) are copied to shared memory once per CTA.
 // Weights of the three tensor-core layers are pre-packed (the surrogate's refresh
 // kernel) into 24 blocks of [256 output rows x 32 K] in the canonical no-swizzle
 // K-major layout, 16 KB each, so one thread streams a block with a single untiled
 // bulk copy (cp.async.bulk, completion counted on an mbarrier) through a ring of
 // kStages shared-memory stages; the tensor core frees a stage by committing the
 // MMAs that read it to the stage's "empty" mbarrier.  One thread (thread 0) issues
-// copies and MMAs; all 128 threads run the epilogues (thread t owns TMEM lane t =
-// tile row t).  Two CTAs share an SM (112 KB of shared memory and 256 TMEM
-// columns each), so one CTA's epilogue overlaps the other's MMAs.
+// copies and MMAs; all 256 threads run layer 0 and the epilogues, two per tile row
+// (row r = TMEM lane r; warps w and w + 4 read lane quarter w % 4 and take the first
+// and the second 128 columns).  Two CTAs share an SM (112 KB of shared memory and
+// 256 TMEM columns each), so one CTA's epilogue overlaps the other's MMAs.
 //
 // Every mbarrier wait is bounded.  A CTA whose wait runs out raises *err, stops
 // issuing, waits (bounded) for the copies and MMAs it already issued, frees its
@@ -49,12 +53,19 @@ constexpr int kKB = 32;         // K per streamed weight block
 constexpr int kBlocksPerLayer = kHidden / kKB;  // 8
 constexpr int kTcLayers = 3;
 constexpr int kBlocks = kTcLayers * kBlocksPerLayer;  // 24 per tile
-constexpr int kStages = 3;
-constexpr int kThreads = 128;
+constexpr int kStages = 2;      // weight stages in shared memory
+constexpr int kCtasPerSm = 2;   // 112 KB of shared memory per CTA fits twice per SM
+constexpr int kThreads = 256;   // two threads per row: each takes half of the 256 columns
+constexpr int kHalf = kHidden / 2;
 constexpr int kActBytes = kRows * kHidden * 2;       // 64 KB
 constexpr int kWBlockElems = kHidden * kKB;           // 8192
 constexpr int kWBlockBytes = kWBlockElems * 2;        // 16 KB
-constexpr int kSmemBytes = kActBytes + kStages * kWBlockBytes + 128;
+// fp32 constants kept in shared memory: W0 [8][256], b0..b3 [4][256], W4 [256][2], b4 [2] (+2 pad)
+constexpr int kConstFloats = kIn * kHidden + 4 * kHidden + kHidden * kOut + 4;
+constexpr int kConstBytes = kConstFloats * 4;
+constexpr int kBarBytes = ((2 * kStages + 2) * 8 + 8 + 127) / 128 * 128;  // mbarriers, TMEM slot, abort word
+constexpr int kSmemBytes = kActBytes + kStages * kWBlockBytes + kConstBytes + kBarBytes;
+static_assert(kSmemBytes * kCtasPerSm + kCtasPerSm * 1024 <= 228 * 1024, "shared memory of the CTAs of one SM");
 constexpr int kTmemCols = 256;
 
 struct MlpArgs {
@@ -83,18 +94,19 @@ __host__ __device__ __forceinline__ int pack_offset(int nrow, int k)
 __device__ __forceinline__ int act_offset(int r, int k) { return (k >> 6) * (kRows * 64) + umma::core_offset(r, k & 63); }
 
 // Layer 0 of one row for output columns [n0, n0 + 8): z = b0 + x W0 (fp32, k in
-// order), shared by the fused kernel and the training path.
+// order), shared by the fused kernel (weights in shared memory) and the training
+// path (weights in global memory).
 __device__ __forceinline__ void layer0_chunk(const float (&x)[kIn], const float *__restrict__ W0,
                                              const float *__restrict__ b0, int n0, float (&z)[8])
 {
     const float4 *b4 = reinterpret_cast<const float4 *>(b0 + n0);
-    const float4 ba = __ldg(b4), bb = __ldg(b4 + 1);
+    const float4 ba = b4[0], bb = b4[1];
     z[0] = ba.x; z[1] = ba.y; z[2] = ba.z; z[3] = ba.w;
     z[4] = bb.x; z[5] = bb.y; z[6] = bb.z; z[7] = bb.w;
 #pragma unroll
     for (int k = 0; k < kIn; ++k) {
         const float4 *w4 = reinterpret_cast<const float4 *>(W0 + k * kHidden + n0);
-        const float4 wa = __ldg(w4), wb = __ldg(w4 + 1);
+        const float4 wa = w4[0], wb = w4[1];
         z[0] = fmaf(x[k], wa.x, z[0]); z[1] = fmaf(x[k], wa.y, z[1]);
         z[2] = fmaf(x[k], wa.z, z[2]); z[3] = fmaf(x[k], wa.w, z[3]);
         z[4] = fmaf(x[k], wb.x, z[4]); z[5] = fmaf(x[k], wb.y, z[5]);
@@ -116,16 +128,21 @@ __device__ __forceinline__ void bulk_copy_g2s(uint32_t dst, const void *src, uin
                  : "memory");
 }
 
-__global__ void __launch_bounds__(kThreads, 2) mlp_forward_kernel(MlpArgs p)
+__global__ void __launch_bounds__(kThreads, kCtasPerSm) mlp_forward_kernel(MlpArgs p)
 {
     extern __shared__ __align__(1024) unsigned char smem[];
     __nv_bfloat16 *act = reinterpret_cast<__nv_bfloat16 *>(smem);
     unsigned char *wst = smem + kActBytes;
-    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + kActBytes + kStages * kWBlockBytes);
+    float *cst = reinterpret_cast<float *>(smem + kActBytes + kStages * kWBlockBytes);
+    float *sW0 = cst, *sB = cst + kIn * kHidden, *sW4 = sB + 4 * kHidden, *sB4 = sW4 + kHidden * kOut;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + kActBytes + kStages * kWBlockBytes + kConstBytes);
     // bars: full[3], empty[3], acc, never; then the TMEM address and the abort word
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * kStages + 2);
     volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
     const int tid = threadIdx.x, warp = tid >> 5;
+    // row r of the tile is TMEM lane r: warps w and w + 4 share lane quarter w % 4 and
+    // split the columns (warps 0-3 the first half, 4-7 the second)
+    const int r = tid & (kRows - 1), half = tid >> 7, cbase = half * kHalf;
     const uint32_t full0 = umma::smem_u32(&bars[0]), empty0 = umma::smem_u32(&bars[kStages]);
     const uint32_t acc_bar = umma::smem_u32(&bars[2 * kStages]), never_bar = umma::smem_u32(&bars[2 * kStages + 1]);
     constexpr uint32_t IDESC = umma::make_idesc(kHidden);
@@ -136,16 +153,29 @@ __global__ void __launch_bounds__(kThreads, 2) mlp_forward_kernel(MlpArgs p)
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) umma::tmem_alloc(umma::smem_u32(tmem_slot), kTmemCols);
+    // the fp32 constants into shared memory (read by every thread of every tile)
+    for (int i = tid; i < kIn * kHidden; i += kThreads) sW0[i] = p.W0[i];
+    for (int i = tid; i < kHidden; i += kThreads) {
+        sB[i] = p.b0[i];
+        sB[kHidden + i] = p.b1[i];
+        sB[2 * kHidden + i] = p.b2[i];
+        sB[3 * kHidden + i] = p.b3[i];
+    }
+    for (int i = tid; i < kHidden * kOut; i += kThreads) sW4[i] = p.W4[i];
+    if (tid < kOut) sB4[tid] = p.b4[tid];
     umma::fence_before_sync();
     __syncthreads();
     umma::fence_after_sync();
     const uint32_t tmem = *tmem_slot;
-    const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);  // this warp's TMEM lane quarter
+    const uint32_t trow = tmem + ((uint32_t)((warp & 3) * 32) << 16);  // this warp's TMEM lane quarter
 
     uint32_t ld = 0, mm = 0, acc_uses = 0;  // blocks copied, blocks consumed, accumulator completions (thread 0)
     bool ok = true;                          // thread 0: no wait ran out
     int stall = p.test_stall;
     const int ntiles = (p.n + kRows - 1) / kRows;
+    // weight blocks this CTA consumes in all (copies never run past them)
+    const uint32_t total_blocks =
+        (blockIdx.x < ntiles ? (uint32_t)((ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1) : 0u) * kBlocks;
 
     // Thread 0: copy weight block `ld` (global block ld % kBlocks) into its stage,
     // once the MMAs that last read that stage have completed.
@@ -159,8 +189,8 @@ __global__ void __launch_bounds__(kThreads, 2) mlp_forward_kernel(MlpArgs p)
     };
 
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const int row = tile * kRows + tid;
-        // ---- layer 0 on the CUDA cores: this thread's row -> activation tile
+        const int row = tile * kRows + r;
+        // ---- layer 0 on the CUDA cores: this thread's row and half -> activation tile
         {
             float x[kIn];
             if (row < p.n) {
@@ -173,15 +203,15 @@ __global__ void __launch_bounds__(kThreads, 2) mlp_forward_kernel(MlpArgs p)
                 for (int k = 0; k < kIn; ++k) x[k] = 0.f;
             }
 #pragma unroll 1
-            for (int n0 = 0; n0 < kHidden; n0 += 8) {
+            for (int n0 = cbase; n0 < cbase + kHalf; n0 += 8) {
                 float z[8];
-                layer0_chunk(x, p.W0, p.b0, n0, z);
+                layer0_chunk(x, sW0, sB, n0, z);
                 uint4 v;
                 v.x = pack_bf16x2(umma::silu_f(z[0]), umma::silu_f(z[1]));
                 v.y = pack_bf16x2(umma::silu_f(z[2]), umma::silu_f(z[3]));
                 v.z = pack_bf16x2(umma::silu_f(z[4]), umma::silu_f(z[5]));
                 v.w = pack_bf16x2(umma::silu_f(z[6]), umma::silu_f(z[7]));
-                *reinterpret_cast<uint4 *>(act + act_offset(tid, n0)) = v;
+                *reinterpret_cast<uint4 *>(act + act_offset(r, n0)) = v;
             }
         }
         float o0 = 0.f, o1 = 0.f;
@@ -239,19 +269,30 @@ __global__ void __launch_bounds__(kThreads, 2) mlp_forward_kernel(MlpArgs p)
             if (__syncthreads_or(*abort_flag)) break;
             // the stages are free: prefetch the next layer's (or the next tile's) first blocks
             if (tid == 0) {
-                const bool more = l + 1 < kTcLayers || tile + (int)gridDim.x < ntiles;
-                while (ok && more && ld < mm + kStages) ok = load_next();  // a failure is seen at the next barrier
+                while (ok && ld < total_blocks && ld < mm + kStages) ok = load_next();  // a failure is seen at the next barrier
             }
             // ---- epilogue: accumulator + bias -> SiLU -> bf16 (next layer's A) or layer 4
-            const float *bias = l == 0 ? p.b1 : (l == 1 ? p.b2 : p.b3);
+            const float *bias = sB + (l + 1) * kHidden;
 #pragma unroll 1
-            for (int c = 0; c < kHidden; c += 16) {
+            for (int c2 = cbase; c2 < cbase + kHalf; c2 += 32) {
+                // two 16-column TMEM loads in flight, the biases fetched meanwhile
+                uint32_t ra[16], rb[16];
+                umma::tmem_ld16_async(trow + (uint32_t)c2, ra);
+                umma::tmem_ld16_async(trow + (uint32_t)(c2 + 16), rb);
+                float4 bv[8];
+                const float4 *b4 = reinterpret_cast<const float4 *>(bias + c2);
+#pragma unroll
+                for (int q = 0; q < 8; ++q) bv[q] = b4[q];
+                umma::tmem_wait_ld();
+#pragma unroll
+              for (int half = 0; half < 2; ++half) {
+                const int c = c2 + 16 * half;
                 float v[16];
-                umma::tmem_ld16(trow + (uint32_t)c, v);
-                const float4 *b4 = reinterpret_cast<const float4 *>(bias + c);
+#pragma unroll
+                for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(half ? rb[i] : ra[i]);
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
-                    const float4 b = __ldg(b4 + q);
+                    const float4 b = bv[4 * half + q];
                     v[4 * q] += b.x; v[4 * q + 1] += b.y; v[4 * q + 2] += b.z; v[4 * q + 3] += b.w;
                 }
                 if (l + 1 < kTcLayers) {
@@ -264,30 +305,36 @@ __global__ void __launch_bounds__(kThreads, 2) mlp_forward_kernel(MlpArgs p)
                     hi.y = pack_bf16x2(umma::silu_f(v[10]), umma::silu_f(v[11]));
                     hi.z = pack_bf16x2(umma::silu_f(v[12]), umma::silu_f(v[13]));
                     hi.w = pack_bf16x2(umma::silu_f(v[14]), umma::silu_f(v[15]));
-                    *reinterpret_cast<uint4 *>(act + act_offset(tid, c)) = lo;
-                    *reinterpret_cast<uint4 *>(act + act_offset(tid, c + 8)) = hi;
+                    *reinterpret_cast<uint4 *>(act + act_offset(r, c)) = lo;
+                    *reinterpret_cast<uint4 *>(act + act_offset(r, c + 8)) = hi;
                 } else {
-                    const float4 *w4 = reinterpret_cast<const float4 *>(p.W4 + 2 * c);
+                    const float4 *w4 = reinterpret_cast<const float4 *>(sW4 + 2 * c);
 #pragma unroll
                     for (int q = 0; q < 8; ++q) {
-                        const float4 w = __ldg(w4 + q);  // rows c + 2q, c + 2q + 1, two outputs each
+                        const float4 w = w4[q];  // rows c + 2q, c + 2q + 1, two outputs each
                         const float h0 = umma::silu_f(v[2 * q]), h1 = umma::silu_f(v[2 * q + 1]);
                         o0 = fmaf(h0, w.x, o0); o1 = fmaf(h0, w.y, o1);
                         o0 = fmaf(h1, w.z, o0); o1 = fmaf(h1, w.w, o1);
                     }
                 }
+              }
             }
         }
+        // layer 4: the second half's partial sums through the (now free) activation tile
+        float2 *part = reinterpret_cast<float2 *>(act);
+        if (half == 1) part[r] = make_float2(o0, o1);
         if (__syncthreads_or((tid == 0 && !ok) || *abort_flag)) {
             if (tid == 0) *abort_flag = 1;
             break;
         }
-        if (row < p.n) {
-            float2 r;
-            r.x = o0 + __ldg(p.b4);
-            r.y = o1 + __ldg(p.b4 + 1);
-            *reinterpret_cast<float2 *>(p.out + (size_t)row * kOut) = r;
+        if (half == 0 && row < p.n) {
+            const float2 q = part[r];
+            float2 res;
+            res.x = (o0 + q.x) + sB4[0];
+            res.y = (o1 + q.y) + sB4[1];
+            *reinterpret_cast<float2 *>(p.out + (size_t)row * kOut) = res;
         }
+        __syncthreads();  // the partial sums are read before the next tile's layer 0 overwrites them
     }
 
     __syncthreads();

@@ -137,21 +137,23 @@ __global__ void dw0_kernel(const float *X, const float *dZ, int n, float *dW0)
         for (int k = 0; k < kInPad; ++k) atomicAdd(dW0 + k * kHidden + c, acc[k]);
 }
 
-// Layer 4 of the training path in fp32: out[r][c] = b4[c] + sum_k silu(Z3[r][k]) W4[k][c]
-// (the fused kernel's last epilogue computes the same sum in the same order).
+// Layer 4 of the training path in fp32: out[r][c] = b4[c] + sum_k silu(Z3[r][k]) W4[k][c],
+// summed as the fused kernel's last epilogue does: one partial per 128 columns (k in
+// order), the second added to the first, then the bias.
 __global__ void layer4_kernel(const float *Z3, const float *W4, const float *b4, int n, float *out)
 {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= n) return;
     const float *z = Z3 + (size_t)r * kHidden;
-    float o0 = 0.f, o1 = 0.f;
-    for (int k = 0; k < kHidden; ++k) {
-        const float h = silu_f(z[k]);
-        o0 = fmaf(h, __ldg(W4 + 2 * k), o0);
-        o1 = fmaf(h, __ldg(W4 + 2 * k + 1), o1);
-    }
-    out[2 * r] = o0 + __ldg(b4);
-    out[2 * r + 1] = o1 + __ldg(b4 + 1);
+    float p0[2] = {0.f, 0.f}, p1[2] = {0.f, 0.f};
+    for (int h = 0; h < 2; ++h)
+        for (int k = h * mlp::kHalf; k < (h + 1) * mlp::kHalf; ++k) {
+            const float a = silu_f(z[k]);
+            p0[h] = fmaf(a, __ldg(W4 + 2 * k), p0[h]);
+            p1[h] = fmaf(a, __ldg(W4 + 2 * k + 1), p1[h]);
+        }
+    out[2 * r] = (p0[0] + p0[1]) + __ldg(b4);
+    out[2 * r + 1] = (p1[0] + p1[1]) + __ldg(b4 + 1);
 }
 
 // Backward through layer 4 (fp32): dZ3[r][k] = (dZ4[r] . W4[k]) silu'(Z3[r][k]), as
@@ -517,6 +519,10 @@ struct hwt_surrogate {
     // training labels) and the distance from them inside which options go to the tree
     std::vector<double> kinks;
     double kink_delta = -1.0;     // < 0: no kink routing
+    // The same routing calibrated at a ladder of tolerances (kCalTol): a call with a
+    // judge tolerance routes with the largest of them at most half that tolerance
+    double cal_tau[7], cal_delta[7], cal_answered[7];
+    int cal_valid = 0;
     Buf<double> dkinks;
     int trained = 0;
     std::string err;
@@ -696,7 +702,7 @@ int forward_fused(hwt_surrogate *s, const float *X, int rows, float *out)
     a.err = s->d_gemm_err;
     a.test_stall = s->stall;
     const int tiles = (rows + mlp::kRows - 1) / mlp::kRows;
-    const int grid = std::min(tiles, 2 * s->sms);
+    const int grid = std::min(tiles, mlp::kCtasPerSm * s->sms);
     mlp::mlp_forward_kernel<<<grid, mlp::kThreads, mlp::kSmemBytes, s->stream>>>(a);
     SCUDA(s, cudaGetLastError(), "fused network kernel");
     return HWT_OK;
@@ -1107,6 +1113,8 @@ double calibrate_tau(const std::vector<double> &pred, const std::vector<double> 
 }
 
 constexpr int kMaxKinks = 256;
+constexpr int kCalTols = 7;
+const double kCalTol[kCalTols] = {2.5e-5, 5e-5, 1e-4, 2e-4, 5e-4, 1e-3, 2e-3};
 
 // A box that pins every tree parameter (maturities, a, sigma, steps): all its
 // options share one tree, and only strike and type vary.
@@ -1319,6 +1327,7 @@ int hwt_surrogate_train(hwt_surrogate *s, const hwt_options *samples, const hwt_
     // 4. router calibration on the held-out samples with the fused network
     double answered = 1.0, max_ans = 0.0, p99_ans = 0.0, max_all = 0.0;
     s->route_tau = INFINITY;
+    s->cal_valid = 0;
     if (nhold > 0) {
         std::vector<int32_t> hold(idx.begin() + ntrain, idx.end());
         if (!s->out2.grow((size_t)nhold * kOut)) return sfail(s, HWT_ENOMEM, "held-out outputs");
@@ -1339,34 +1348,47 @@ int hwt_surrogate_train(hwt_surrogate *s, const hwt_options *samples, const hwt_
             pred[j] = exp((double)o[2 * j + 1]) * s->ystd * Fh[i];
             max_all = std::max(max_all, err[j]);
         }
-        if (lam > 0) {
-            s->route_tau = calibrate_tau(pred, err, route_tol, &answered, &max_ans, &p99_ans);
-        } else if (!s->kinks.empty()) {
-            // the smallest distance from the kinks beyond which every held-out answer
-            // is within the tolerance
-            std::vector<double> d(nhold);
-            double delta = 0.0;
-            for (int64_t j = 0; j < nhold; ++j) {
-                const int i = hold[j];
-                d[j] = kink_distance(s->kinks, samples->strike[i] / Fh[i]);
-                if (!(err[j] <= route_tol)) delta = std::max(delta, d[j]);
+        std::vector<double> d;
+        if (!s->kinks.empty()) {
+            d.resize(nhold);
+            for (int64_t j = 0; j < nhold; ++j) d[j] = kink_distance(s->kinks, samples->strike[hold[j]] / Fh[hold[j]]);
+        }
+        // routing that keeps every held-out answer within tol: (tau, delta), the
+        // answered fraction and the largest and p99 errors of the answered samples
+        auto calibrate = [&](double tol, double *tau, double *delta, double *ans, double *mx, double *p99) {
+            *tau = INFINITY;
+            *delta = -1.0;
+            if (lam > 0) {
+                *tau = calibrate_tau(pred, err, tol, ans, mx, p99);
+                return;
             }
-            s->kink_delta = delta;
             std::vector<double> e;
-            for (int64_t j = 0; j < nhold; ++j)
-                if (d[j] > delta) e.push_back(err[j]);
-            answered = (double)e.size() / nhold;
+            if (!d.empty()) {
+                // the smallest distance from the kinks beyond which every held-out
+                // answer is within the tolerance
+                double dl = 0.0;
+                for (int64_t j = 0; j < nhold; ++j)
+                    if (!(err[j] <= tol)) dl = std::max(dl, d[j]);
+                *delta = dl;
+                for (int64_t j = 0; j < nhold; ++j)
+                    if (d[j] > dl) e.push_back(err[j]);
+            } else {
+                e = err;
+            }
+            *ans = (double)e.size() / nhold;
+            *mx = *p99 = 0.0;
             if (!e.empty()) {
                 std::sort(e.begin(), e.end());
-                max_ans = e.back();
-                p99_ans = e[std::min(e.size() - 1, (size_t)floor(0.99 * (e.size() - 1)))];
+                *mx = e.back();
+                *p99 = e[std::min(e.size() - 1, (size_t)floor(0.99 * (e.size() - 1)))];
             }
-        } else {
-            std::vector<double> e = err;
-            std::sort(e.begin(), e.end());
-            max_ans = e.back();
-            p99_ans = e[std::min(e.size() - 1, (size_t)floor(0.99 * (e.size() - 1)))];
+        };
+        calibrate(route_tol, &s->route_tau, &s->kink_delta, &answered, &max_ans, &p99_ans);
+        for (int k = 0; k < kCalTols; ++k) {
+            double mx, p99;
+            calibrate(kCalTol[k], &s->cal_tau[k], &s->cal_delta[k], &s->cal_answered[k], &mx, &p99);
         }
+        s->cal_valid = 1;
     }
     s->trained = 1;
     if (stats) {
@@ -1386,6 +1408,10 @@ int hwt_surrogate_train(hwt_surrogate *s, const hwt_options *samples, const hwt_
         stats->holdout = nhold;
         stats->n_kinks = (int64_t)s->kinks.size();
         stats->kink_delta = s->kink_delta;
+        for (int k = 0; k < kCalTols; ++k) {
+            stats->ladder_tolerance[k] = kCalTol[k];
+            stats->ladder_answered[k] = s->cal_valid ? s->cal_answered[k] : 0.0;
+        }
     }
     return HWT_OK;
 }
@@ -1410,17 +1436,27 @@ int hwt_surrogate_price(hwt_surrogate *s, const hwt_options *o, const hwt_yield 
     SCUDA(s, cudaMemsetAsync(s->counts.p, 0, 16, s->stream), "counts");
     const double jf = std::min(std::max(judge_fraction, 0.0), 1.0);
     const unsigned long long thresh = jf >= 1.0 ? ~0ull : (unsigned long long)(jf * 18446744073709551616.0);
+    // routing: the training tolerance's calibration, or, with a judge tolerance, the
+    // ladder's largest tolerance not above it (the strictest if none is)
+    double tau = s->route_tau, delta = s->kink_delta, route_tol = NAN;
+    if (judge_tolerance > 0 && s->cal_valid) {
+        int k = 0;
+        for (int q = 0; q < kCalTols; ++q)
+            if (kCalTol[q] <= judge_tolerance * (1.0 + 1e-12)) k = q;
+        tau = s->cal_tau[k];
+        delta = s->cal_delta[k];
+        route_tol = kCalTol[k];
+    }
     // flag when exp(o1) ystd F > tau; tau = +inf: the router is off, tau <= 0: nothing is answered
-    const float log_tau = std::isinf(s->route_tau) ? INFINITY
-                          : (s->route_tau > 0 ? (float)log(s->route_tau / s->ystd) : -INFINITY);
-    const int nk = s->kink_delta >= 0 ? (int)s->kinks.size() : 0;
+    const float log_tau = std::isinf(tau) ? INFINITY : (tau > 0 ? (float)log(tau / s->ystd) : -INFINITY);
+    const int nk = delta >= 0 ? (int)s->kinks.size() : 0;
     if (nk > 0) {
         if (!s->dkinks.grow(kMaxKinks)) return sfail(s, HWT_ENOMEM, "kink buffer");
         SCUDA(s, cudaMemcpyAsync(s->dkinks.p, s->kinks.data(), 8ull * nk, cudaMemcpyHostToDevice, s->stream), "kinks H2D");
     }
     decode_route_kernel<<<(n + 255) / 256, 256, 0, s->stream>>>(s->out2.p, s->F.p, s->base.p, s->inbox.p,
                                                                s->opts.strike, n, s->ymean, s->ystd, log_tau,
-                                                               s->dkinks.p, nk, s->kink_delta, seed, thresh,
+                                                               s->dkinks.p, nk, delta, seed, thresh,
                                                                s->price.p, s->kind.p, s->list.p, s->counts.p);
     SCUDA(s, cudaGetLastError(), "decode kernel");
     SCUDA(s, cudaEventRecord(s->ev[1], s->stream), "event");
@@ -1512,6 +1548,7 @@ int hwt_surrogate_price(hwt_surrogate *s, const hwt_options *o, const hwt_yield 
             stats->judge_mean_abs = sm / e.size();
         }
         stats->fell_back = fell_back;
+        stats->route_tolerance = route_tol;
         stats->network_ms = t0;
         stats->tree_ms = tree_ms + fallback_ms;
         stats->route_ms = t2;
@@ -1530,13 +1567,15 @@ int hwt_surrogate_save(const hwt_surrogate *s, const char *path)
         return HWT_ECUDA;
     FILE *f = fopen(path, "wb");
     if (!f) return HWT_EINVAL;
-    const uint32_t magic = 0x48575453u, version = 3;
+    const uint32_t magic = 0x48575453u, version = 4;
     const uint64_t np = s->n_params, nk = s->kinks.size();
     const int64_t t = s->adam_t;
     bool ok = fwrite(&magic, 4, 1, f) == 1 && fwrite(&version, 4, 1, f) == 1 && fwrite(&s->box, sizeof(hwt_box), 1, f) == 1 &&
               fwrite(&s->ymean, 8, 1, f) == 1 && fwrite(&s->ystd, 8, 1, f) == 1 && fwrite(&s->route_tau, 8, 1, f) == 1 &&
               fwrite(&s->kink_delta, 8, 1, f) == 1 && fwrite(&nk, 8, 1, f) == 1 &&
-              (nk == 0 || fwrite(s->kinks.data(), 8, nk, f) == nk) &&
+              (nk == 0 || fwrite(s->kinks.data(), 8, nk, f) == nk) && fwrite(&s->cal_valid, 4, 1, f) == 1 &&
+              fwrite(s->cal_tau, 8, kCalTols, f) == kCalTols && fwrite(s->cal_delta, 8, kCalTols, f) == kCalTols &&
+              fwrite(s->cal_answered, 8, kCalTols, f) == kCalTols &&
               fwrite(&t, 8, 1, f) == 1 && fwrite(&np, 8, 1, f) == 1 && fwrite(w.data(), 4, np, f) == np &&
               fwrite(m.data(), 4, np, f) == np && fwrite(v.data(), 4, np, f) == np;
     fclose(f);
@@ -1555,13 +1594,17 @@ int hwt_surrogate_load(hwt_surrogate *s, const char *path)
     double ym = 0, ysd = 1, tau = INFINITY, kd = -1.0;
     uint64_t nk = 0;
     std::vector<double> kinks;
-    bool ok = fread(&magic, 4, 1, f) == 1 && fread(&version, 4, 1, f) == 1 && magic == 0x48575453u && version == 3 &&
+    int cal_valid = 0;
+    double cal_tau[kCalTols], cal_delta[kCalTols], cal_answered[kCalTols];
+    bool ok = fread(&magic, 4, 1, f) == 1 && fread(&version, 4, 1, f) == 1 && magic == 0x48575453u && version == 4 &&
               fread(&box, sizeof(hwt_box), 1, f) == 1 && fread(&ym, 8, 1, f) == 1 && fread(&ysd, 8, 1, f) == 1 &&
               fread(&tau, 8, 1, f) == 1 && fread(&kd, 8, 1, f) == 1 && fread(&nk, 8, 1, f) == 1 && nk <= (uint64_t)kMaxKinks;
     if (ok && nk) {
         kinks.resize(nk);
         ok = fread(kinks.data(), 8, nk, f) == nk;
     }
+    ok = ok && fread(&cal_valid, 4, 1, f) == 1 && fread(cal_tau, 8, kCalTols, f) == kCalTols &&
+         fread(cal_delta, 8, kCalTols, f) == kCalTols && fread(cal_answered, 8, kCalTols, f) == kCalTols;
     ok = ok && fread(&t, 8, 1, f) == 1 && fread(&np, 8, 1, f) == 1 && np == s->n_params;
     std::vector<float> w(s->n_params), m(s->n_params), v(s->n_params);
     ok = ok && fread(w.data(), 4, np, f) == np && fread(m.data(), 4, np, f) == np && fread(v.data(), 4, np, f) == np;
@@ -1574,6 +1617,10 @@ int hwt_surrogate_load(hwt_surrogate *s, const char *path)
     s->route_tau = tau;
     s->kink_delta = kd;
     s->kinks = kinks;
+    s->cal_valid = cal_valid;
+    memcpy(s->cal_tau, cal_tau, sizeof(cal_tau));
+    memcpy(s->cal_delta, cal_delta, sizeof(cal_delta));
+    memcpy(s->cal_answered, cal_answered, sizeof(cal_answered));
     s->adam_t = t;
     SCUDA(s, cudaMemcpy(s->d_w, w.data(), 4 * np, cudaMemcpyHostToDevice), "load");
     SCUDA(s, cudaMemcpy(s->d_m, m.data(), 4 * np, cudaMemcpyHostToDevice), "load");

@@ -39,7 +39,7 @@ constexpr int BM = 128;           // rows per tile (the MMA's M)
 constexpr int BK = 64;            // K per stage (four 16-wide MMAs)
 constexpr int THREADS = 128;
 constexpr int STAGES = 3;
-constexpr unsigned kWaitLimit = 1u << 22;  // mbarrier polls before giving up (~0.1-1 s)
+constexpr uint64_t kWaitNs = 250000000ull;  // an mbarrier wait gives up after 0.25 s
 
 enum Epilogue : int {
     EPI_BIAS_SILU = 0,   // Z = acc + bias -> store Z (fp32) and silu(Z) (bf16)
@@ -120,22 +120,33 @@ __device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count)
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
 }
 
-// Polls the mbarrier phase with the given parity; false if the limit ran out.
+__device__ __forceinline__ uint64_t global_ns()
+{
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Waits for the mbarrier phase with the given parity; false once kWaitNs have
+// passed (global timer) without it.  mbarrier.try_wait suspends the thread in
+// hardware until the phase completes or a 20 us hint elapses, so a completed phase
+// wakes the waiter at once (a polling loop with sleeps overshoots).
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity)
 {
-    for (unsigned i = 0; i < kWaitLimit; ++i) {
+    uint64_t t0 = 0;
+    for (unsigned i = 0;; ++i) {
         uint32_t done;
         asm volatile(
             "{\n\t.reg .pred p;\n\t"
-            "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
             "selp.u32 %0, 1, 0, p;\n\t}"
             : "=r"(done)
-            : "r"(bar), "r"(parity)
+            : "r"(bar), "r"(parity), "r"(20000u)
             : "memory");
         if (done) return true;
-        if (i > 64) __nanosleep(64);
+        if (i == 0) t0 = global_ns();
+        else if (global_ns() - t0 > kWaitNs) return false;
     }
-    return false;
 }
 
 __device__ __forceinline__ void tmem_alloc(uint32_t dst_smem, uint32_t ncols)
@@ -171,6 +182,20 @@ __device__ __forceinline__ void mma_commit(uint32_t bar)
 {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
 }
+
+// 16 consecutive fp32 accumulator columns of this thread's TMEM lane, without
+// waiting: the registers are valid after tmem_wait_ld().
+__device__ __forceinline__ void tmem_ld16_async(uint32_t taddr, uint32_t (&r)[16])
+{
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr)
+        : "memory");
+}
+
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 // 16 consecutive fp32 accumulator columns of this thread's TMEM lane.
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])

@@ -276,6 +276,8 @@ typedef struct hwt_train_stats {
     int64_t n_kinks;                 /* single-tree box: payoff kinks found in the labels */
     double kink_delta;               /* options closer than this (moneyness) to a kink go to the tree
                                         (< 0: no kink routing) */
+    double ladder_tolerance[7];      /* the routing also calibrated at these tolerances ... */
+    double ladder_answered[7];       /* ... answering these fractions of the held-out samples */
 } hwt_train_stats;
 
 typedef struct hwt_surrogate_stats {
@@ -285,8 +287,9 @@ typedef struct hwt_surrogate_stats {
     int32_t pad;
     double judge_max_abs, judge_p99_abs, judge_mean_abs; /* |network - tree| on the judged sample */
     double network_ms, tree_ms, route_ms, total_ms;
-    int64_t n_flagged;               /* in-box options the error head sent to the tree */
+    int64_t n_flagged;               /* in-box options the routing sent to the tree */
     int64_t n_network;               /* options answered by the network */
+    double route_tolerance;          /* the ladder tolerance the call routed with (NaN: the training one) */
 } hwt_surrogate_stats;
 
 typedef struct hwt_surrogate hwt_surrogate;
@@ -298,7 +301,10 @@ const char *hwt_surrogate_last_error(const hwt_surrogate *s);
  * but a held-out slice, and sets the routing threshold on that slice. */
 int hwt_surrogate_train(hwt_surrogate *s, const hwt_options *samples, const hwt_yield *yield,
                         const hwt_train_config *cfg, hwt_train_stats *stats);
-/* Prices host options: network inside the box unless the option is flagged - by
+/* Routing tolerance: with judge_tolerance > 0 the call routes with the calibration
+ * (of the training ladder) for the largest tolerance not above judge_tolerance;
+ * otherwise with the training's route_tolerance.
+ * Prices host options: network inside the box unless the option is flagged - by
  * the error head, or, on a single-tree box (every tree parameter pinned, so the
  * price is piecewise linear in the strike), by a strike within the calibrated
  * distance of one of the tree's payoff kinks, which training finds in its labels -
