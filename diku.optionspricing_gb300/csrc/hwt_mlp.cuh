@@ -101,17 +101,30 @@ __device__ __forceinline__ void layer0_chunk(const float (&x)[kIn], const float 
 {
     const float4 *b4 = reinterpret_cast<const float4 *>(b0 + n0);
     const float4 ba = b4[0], bb = b4[1];
-    z[0] = ba.x; z[1] = ba.y; z[2] = ba.z; z[3] = ba.w;
-    z[4] = bb.x; z[5] = bb.y; z[6] = bb.z; z[7] = bb.w;
+    float2 z2[4] = {make_float2(ba.x, ba.y), make_float2(ba.z, ba.w), make_float2(bb.x, bb.y), make_float2(bb.z, bb.w)};
 #pragma unroll
     for (int k = 0; k < kIn; ++k) {
+        // fma(x_k, W0[k][n], z[n]) for eight columns, two per paired instruction
         const float4 *w4 = reinterpret_cast<const float4 *>(W0 + k * kHidden + n0);
         const float4 wa = w4[0], wb = w4[1];
-        z[0] = fmaf(x[k], wa.x, z[0]); z[1] = fmaf(x[k], wa.y, z[1]);
-        z[2] = fmaf(x[k], wa.z, z[2]); z[3] = fmaf(x[k], wa.w, z[3]);
-        z[4] = fmaf(x[k], wb.x, z[4]); z[5] = fmaf(x[k], wb.y, z[5]);
-        z[6] = fmaf(x[k], wb.z, z[6]); z[7] = fmaf(x[k], wb.w, z[7]);
+        const float2 xk = make_float2(x[k], x[k]);
+        z2[0] = __ffma2_rn(xk, make_float2(wa.x, wa.y), z2[0]);
+        z2[1] = __ffma2_rn(xk, make_float2(wa.z, wa.w), z2[1]);
+        z2[2] = __ffma2_rn(xk, make_float2(wb.x, wb.y), z2[2]);
+        z2[3] = __ffma2_rn(xk, make_float2(wb.z, wb.w), z2[3]);
     }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        z[2 * j] = z2[j].x;
+        z[2 * j + 1] = z2[j].y;
+    }
+}
+
+__device__ __forceinline__ uint32_t pack_silu2(float a, float b)
+{
+    const float2 h = umma::silu2_f(make_float2(a, b));
+    const __nv_bfloat162 q = __floats2bfloat162_rn(h.x, h.y);
+    return *reinterpret_cast<const uint32_t *>(&q);
 }
 
 __device__ __forceinline__ uint32_t pack_bf16x2(float a, float b)
@@ -207,10 +220,10 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) mlp_forward_kernel(MlpAr
                 float z[8];
                 layer0_chunk(x, sW0, sB, n0, z);
                 uint4 v;
-                v.x = pack_bf16x2(umma::silu_f(z[0]), umma::silu_f(z[1]));
-                v.y = pack_bf16x2(umma::silu_f(z[2]), umma::silu_f(z[3]));
-                v.z = pack_bf16x2(umma::silu_f(z[4]), umma::silu_f(z[5]));
-                v.w = pack_bf16x2(umma::silu_f(z[6]), umma::silu_f(z[7]));
+                v.x = pack_silu2(z[0], z[1]);
+                v.y = pack_silu2(z[2], z[3]);
+                v.z = pack_silu2(z[4], z[5]);
+                v.w = pack_silu2(z[6], z[7]);
                 *reinterpret_cast<uint4 *>(act + act_offset(r, n0)) = v;
             }
         }
@@ -291,20 +304,22 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) mlp_forward_kernel(MlpAr
 #pragma unroll
                 for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(half ? rb[i] : ra[i]);
 #pragma unroll
-                for (int q = 0; q < 4; ++q) {
+                for (int q = 0; q < 4; ++q) {  // + bias, two lanes per paired add
                     const float4 b = bv[4 * half + q];
-                    v[4 * q] += b.x; v[4 * q + 1] += b.y; v[4 * q + 2] += b.z; v[4 * q + 3] += b.w;
+                    const float2 s0 = __fadd2_rn(make_float2(v[4 * q], v[4 * q + 1]), make_float2(b.x, b.y));
+                    const float2 s1 = __fadd2_rn(make_float2(v[4 * q + 2], v[4 * q + 3]), make_float2(b.z, b.w));
+                    v[4 * q] = s0.x; v[4 * q + 1] = s0.y; v[4 * q + 2] = s1.x; v[4 * q + 3] = s1.y;
                 }
                 if (l + 1 < kTcLayers) {
                     uint4 lo, hi;
-                    lo.x = pack_bf16x2(umma::silu_f(v[0]), umma::silu_f(v[1]));
-                    lo.y = pack_bf16x2(umma::silu_f(v[2]), umma::silu_f(v[3]));
-                    lo.z = pack_bf16x2(umma::silu_f(v[4]), umma::silu_f(v[5]));
-                    lo.w = pack_bf16x2(umma::silu_f(v[6]), umma::silu_f(v[7]));
-                    hi.x = pack_bf16x2(umma::silu_f(v[8]), umma::silu_f(v[9]));
-                    hi.y = pack_bf16x2(umma::silu_f(v[10]), umma::silu_f(v[11]));
-                    hi.z = pack_bf16x2(umma::silu_f(v[12]), umma::silu_f(v[13]));
-                    hi.w = pack_bf16x2(umma::silu_f(v[14]), umma::silu_f(v[15]));
+                    lo.x = pack_silu2(v[0], v[1]);
+                    lo.y = pack_silu2(v[2], v[3]);
+                    lo.z = pack_silu2(v[4], v[5]);
+                    lo.w = pack_silu2(v[6], v[7]);
+                    hi.x = pack_silu2(v[8], v[9]);
+                    hi.y = pack_silu2(v[10], v[11]);
+                    hi.z = pack_silu2(v[12], v[13]);
+                    hi.w = pack_silu2(v[14], v[15]);
                     *reinterpret_cast<uint4 *>(act + act_offset(r, c)) = lo;
                     *reinterpret_cast<uint4 *>(act + act_offset(r, c + 8)) = hi;
                 } else {
@@ -312,9 +327,12 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) mlp_forward_kernel(MlpAr
 #pragma unroll
                     for (int q = 0; q < 8; ++q) {
                         const float4 w = w4[q];  // rows c + 2q, c + 2q + 1, two outputs each
-                        const float h0 = umma::silu_f(v[2 * q]), h1 = umma::silu_f(v[2 * q + 1]);
-                        o0 = fmaf(h0, w.x, o0); o1 = fmaf(h0, w.y, o1);
-                        o0 = fmaf(h1, w.z, o0); o1 = fmaf(h1, w.w, o1);
+                        const float2 h = umma::silu2_f(make_float2(v[2 * q], v[2 * q + 1]));
+                        // (o0, o1) += h_k (W4[k][0], W4[k][1]), the two outputs in one paired FMA
+                        float2 o = __ffma2_rn(make_float2(h.x, h.x), make_float2(w.x, w.y), make_float2(o0, o1));
+                        o = __ffma2_rn(make_float2(h.y, h.y), make_float2(w.z, w.w), o);
+                        o0 = o.x;
+                        o1 = o.y;
                     }
                 }
               }

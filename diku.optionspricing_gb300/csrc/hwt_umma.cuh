@@ -88,6 +88,14 @@ __device__ __forceinline__ float silu_f(float z)
     return fmaf(h, tanh_approx(h), h);
 }
 
+// silu_f on a pair with the paired FP32 instructions (each lane rounds as the scalar
+// code: the same bits, half the FP32 instruction issues).
+__device__ __forceinline__ float2 silu2_f(float2 z)
+{
+    const float2 h = __fmul2_rn(make_float2(0.5f, 0.5f), z);
+    return __ffma2_rn(h, make_float2(tanh_approx(h.x), tanh_approx(h.y)), h);
+}
+
 // d silu / dz = s (1 + z (1 - s)) with the same sigmoid s.
 __device__ __forceinline__ float dsilu_f(float z)
 {
