@@ -237,9 +237,11 @@ def cpu_reference(args, rank, world):
 
 
 def errors(got, ref) -> dict:
+    """Max / p99 absolute error and max relative error, the latter against
+    max(|ref|, 1e-6) so that prices that are zero up to rounding do not divide by 0."""
     err = np.abs(got - ref)
     return {"max_abs_err": float(np.max(err)), "p99_abs_err": float(np.percentile(err, 99)),
-            "max_rel_err": float(np.max(err / np.maximum(np.abs(ref), 1e-300)))}
+            "max_rel_err": float(np.max(err / np.maximum(np.abs(ref), 1e-6)))}
 
 
 def config_runs(pkg, orc, pricer, y, reps: int) -> dict:
