@@ -333,7 +333,8 @@ def network_kernel_time(pkg, pricer, rows: int, steps: int, warmup: int, dev) ->
             "flop_per_row": NETWORK_FLOP_PER_ROW}
 
 
-def surrogate_run(pkg, pricer, y, box, train, queries, epochs: int, reps: int, batch=None) -> dict:
+def surrogate_run(pkg, pricer, y, box, train, queries, epochs: int, reps: int, batch=None,
+                  kink_oversample: int = 1) -> dict:
     """Trains the surrogate on `train` (labels from the FP64 tree), then prices the
     1M `queries` through hwt_surrogate_price (host arrays in and out; network inside
     the box unless routed, tree outside it, for routed options and for the judge's 1%
@@ -342,7 +343,7 @@ def surrogate_run(pkg, pricer, y, box, train, queries, epochs: int, reps: int, b
     sur = pkg.Surrogate(pricer, box=box, seed=1)
     t0 = time.perf_counter()
     tstats = sur.train(pkg.Options.from_batch(train), y, epochs=epochs, batch=8192, lr=2e-3, lr_min=2e-6,
-                       route_tolerance=1e-4, holdout=0.05)
+                       route_tolerance=1e-4, holdout=0.05, kink_oversample=kink_oversample)
     train_s = time.perf_counter() - t0
     qo = pkg.Options.from_batch(queries)
     trees = {}
@@ -402,7 +403,8 @@ def surrogate_run(pkg, pricer, y, box, train, queries, epochs: int, reps: int, b
     sur.close()
     return {
         "on_uneven_30k": on_batch,
-        "train": {**tstats, "wall_s": train_s, "epochs": epochs, "samples_offered": len(train["strike"])},
+        "train": {**tstats, "wall_s": train_s, "epochs": epochs, "samples_offered": len(train["strike"]),
+                  "kink_oversample": kink_oversample},
         "queries": {"n": int(qo.N), "outside_box": int(queries["outside"].sum()), "at_judge_tolerance": at,
                     "timing": "host clock around hwt_surrogate_price (host arrays in and out), best of the calls "
                               "after the first; trees: host clock around hwt_price_ex on the same queries; errors "
@@ -524,7 +526,7 @@ def run_ours(args, rank, world, local):
         surrogate = {"network_kernel": network_kernel_time(pkg, pricer, 1 << 20, 10, 3, dev)}
         surrogate["single_tree"] = surrogate_run(
             pkg, pricer, y, box=wl.single_tree_box(), train=wl.single_tree_training_batch(args.sur_samples, 3),
-            queries=wl.single_tree_query_batch(1_000_000, 4), epochs=args.sur_epochs, reps=3)
+            queries=wl.single_tree_query_batch(1_000_000, 4), epochs=args.sur_epochs, reps=3, kink_oversample=3)
         surrogate["uneven_box"] = surrogate_run(
             pkg, pricer, y, box=None, train=wl.surrogate_training_batch(args.sur_samples, 3),
             queries=wl.surrogate_query_batch(1_000_000, 4), epochs=args.sur_epochs_uneven, reps=3,

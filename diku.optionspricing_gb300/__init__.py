@@ -527,7 +527,8 @@ class Box(ctypes.Structure):
 class TrainConfig(ctypes.Structure):
     _fields_ = [("epochs", ctypes.c_int32), ("batch", ctypes.c_int32), ("lr", ctypes.c_double),
                 ("lr_min", ctypes.c_double), ("seed", ctypes.c_uint64), ("err_weight", ctypes.c_double),
-                ("route_tolerance", ctypes.c_double), ("holdout", ctypes.c_double)]
+                ("route_tolerance", ctypes.c_double), ("holdout", ctypes.c_double),
+                ("kink_oversample", ctypes.c_int32), ("pad", ctypes.c_int32)]
 
 
 class TrainStats(ctypes.Structure):
@@ -617,10 +618,11 @@ class Surrogate:
 
     def train(self, samples: Options, yield_: Yield, epochs: int = 1, batch: int = 8192, lr: float = 1e-3,
               lr_min: float = 0.0, seed: int = 7, err_weight: float = 0.0, route_tolerance: float = 1e-4,
-              holdout: float = 0.05) -> dict:
+              holdout: float = 0.05, kink_oversample: int = 1) -> dict:
         """Labels the samples with the FP64 tree and trains; with err_weight > 0 the
-        error head is trained too and routes (held-out calibration at route_tolerance)."""
-        cfg = TrainConfig(epochs, batch, lr, lr_min, seed, err_weight, route_tolerance, holdout)
+        error head is trained too and routes (held-out calibration at route_tolerance);
+        on a single-tree box samples near a payoff kink can be repeated per epoch."""
+        cfg = TrainConfig(epochs, batch, lr, lr_min, seed, err_weight, route_tolerance, holdout, kink_oversample, 0)
         o, y = samples._c(), yield_._c()
         self._check(lib().hwt_surrogate_train(self._s, ctypes.byref(o), ctypes.byref(y), ctypes.byref(cfg),
                                               ctypes.byref(self.train_stats)))

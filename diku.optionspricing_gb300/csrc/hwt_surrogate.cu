@@ -1113,6 +1113,7 @@ double calibrate_tau(const std::vector<double> &pred, const std::vector<double> 
 }
 
 constexpr int kMaxKinks = 256;
+constexpr double kKinkBand = 0.005;  // moneyness: ~0.44 strike units around a kink of the book's tree
 constexpr int kCalTols = 7;
 const double kCalTol[kCalTols] = {2.5e-5, 5e-5, 1e-4, 2e-4, 5e-4, 1e-3, 2e-3};
 
@@ -1247,14 +1248,28 @@ int hwt_surrogate_train(hwt_surrogate *s, const hwt_options *samples, const hwt_
     s->ymean = sum / ntrain;
     s->ystd = std::max(sqrt(std::max(sum2 / ntrain - s->ymean * s->ymean, 0.0)), 1e-12);
 
+    // the epoch's sample list: on a single-tree box, samples within kKinkBand (moneyness)
+    // of a kink appear kink_oversample times (the network's largest errors sit there)
+    std::vector<int32_t> tr(idx.begin(), idx.begin() + ntrain);
+    const int reps = std::max(1, std::min(cfg->kink_oversample, 16));
+    if (reps > 1 && !s->kinks.empty()) {
+        for (int64_t j = 0; j < ntrain; ++j) {
+            const int i = idx[j];
+            if (kink_distance(s->kinks, samples->strike[i] / Fh[i]) < kKinkBand)
+                for (int q = 1; q < reps; ++q) tr.push_back(i);
+        }
+    }
+    const int64_t nlist = (int64_t)tr.size();
+    const int64_t nbuf = std::max(nlist, nin);
+
     Scoped guard;
     float *yv = nullptr, *Xs = nullptr, *ys = nullptr;
     double *dprice = nullptr;
     int32_t *perm = nullptr;
     StepState *dstate = nullptr;
-    bool ok = cudaMalloc(&yv, 4ull * n) == cudaSuccess && cudaMalloc(&Xs, 4ull * kInPad * nin) == cudaSuccess &&
-              cudaMalloc(&ys, 4ull * nin) == cudaSuccess && cudaMalloc(&dprice, 8ull * n) == cudaSuccess &&
-              cudaMalloc(&perm, 4ull * nin) == cudaSuccess && cudaMalloc(&dstate, sizeof(StepState)) == cudaSuccess;
+    bool ok = cudaMalloc(&yv, 4ull * n) == cudaSuccess && cudaMalloc(&Xs, 4ull * kInPad * nbuf) == cudaSuccess &&
+              cudaMalloc(&ys, 4ull * nbuf) == cudaSuccess && cudaMalloc(&dprice, 8ull * n) == cudaSuccess &&
+              cudaMalloc(&perm, 4ull * nbuf) == cudaSuccess && cudaMalloc(&dstate, sizeof(StepState)) == cudaSuccess;
     guard.ptrs = {yv, Xs, ys, dprice, perm, dstate};
     if (!ok) {
         cudaGetLastError();
@@ -1266,7 +1281,7 @@ int hwt_surrogate_train(hwt_surrogate *s, const hwt_options *samples, const hwt_
     if ((r = ensure_act(s, batch))) return r;
 
     // 3. Adam with cosine decay over the training part, reshuffled every epoch
-    const int steps_per_epoch = (int)(ntrain / batch);
+    const int steps_per_epoch = (int)(nlist / batch);
     const long total = (long)steps_per_epoch * epochs;
     const double lr0 = cfg->lr > 0 ? cfg->lr : 1e-3, lr_min = cfg->lr_min;
     long step = 0;
@@ -1297,12 +1312,11 @@ int hwt_surrogate_train(hwt_surrogate *s, const hwt_options *samples, const hwt_
         SCUDA(s, ce2, "end capture");
     }
     SCUDA(s, cudaGraphInstantiate(&gexec, graph, 0), "instantiate training graph");
-    std::vector<int32_t> tr(idx.begin(), idx.begin() + ntrain);
     SCUDA(s, cudaEventRecord(s->ev[0], s->stream), "event");
     for (int ep = 0; ep < epochs; ++ep) {
-        for (int64_t i = ntrain - 1; i > 0; --i) std::swap(tr[i], tr[rnd() % (unsigned long long)(i + 1)]);
-        SCUDA(s, cudaMemcpyAsync(perm, tr.data(), 4ull * ntrain, cudaMemcpyHostToDevice, s->stream), "perm H2D");
-        gather_rows_kernel<<<(int)((ntrain + 255) / 256), 256, 0, s->stream>>>(s->xf.p, yv, perm, (int)ntrain, Xs, ys);
+        for (int64_t i = nlist - 1; i > 0; --i) std::swap(tr[i], tr[rnd() % (unsigned long long)(i + 1)]);
+        SCUDA(s, cudaMemcpyAsync(perm, tr.data(), 4ull * nlist, cudaMemcpyHostToDevice, s->stream), "perm H2D");
+        gather_rows_kernel<<<(int)((nlist + 255) / 256), 256, 0, s->stream>>>(s->xf.p, yv, perm, (int)nlist, Xs, ys);
         SCUDA(s, cudaStreamSynchronize(s->stream), "shuffle");  // tr is reshuffled next epoch
         SCUDA(s, cudaMemsetAsync(s->d_loss, 0, sizeof(double), s->stream), "zero loss");
         SCUDA(s, cudaMemsetAsync(&dstate->k, 0, sizeof(int), s->stream), "epoch start");

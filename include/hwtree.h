@@ -259,6 +259,9 @@ typedef struct hwt_train_config {
                                         on the held-out samples; sets the routing threshold of the error
                                         head or, on a single-tree box, the kink distance (default 1e-4) */
     double holdout;                  /* fraction of in-box samples held out for that (default 0.05) */
+    int32_t kink_oversample;         /* single-tree box: samples within 0.005 in moneyness of a payoff
+                                        kink appear this many times per epoch (1 or 0: once) */
+    int32_t pad;
 } hwt_train_config;
 
 typedef struct hwt_train_stats {
