@@ -297,9 +297,10 @@ def config_runs(pkg, orc, pricer, y, reps: int) -> dict:
     return out
 
 
-# FLOP per row of the surrogate network: 2 x (8 x 256 + 3 x 256 x 256 + 256 x 2)
+# FLOP per row of the surrogate network: 2 x (8 x 256 + 3 x 256 x 256 + 256 x 2); the
+# tensor cores execute layer 1 twice (its input as a bf16 hi / lo pair): 4 x 256 x 256 MACs
 NETWORK_FLOP_PER_ROW = 2 * (8 * 256 + 3 * 256 * 256 + 256 * 2)
-NETWORK_TENSOR_FLOP_PER_ROW = 2 * 3 * 256 * 256  # the three tensor-core layers
+NETWORK_TENSOR_FLOP_PER_ROW = 2 * 4 * 256 * 256
 
 
 def network_kernel_time(pkg, pricer, rows: int, steps: int, warmup: int, dev) -> dict:
@@ -327,8 +328,10 @@ def network_kernel_time(pkg, pricer, rows: int, steps: int, warmup: int, dev) ->
     peak = measured.get("bf16_tflops")
     tensor_tflops = rows * NETWORK_TENSOR_FLOP_PER_ROW / (t * 1e-3) / 1e12
     return {"rows": rows, "kernel_ms": t, "rows_per_s": rows / (t * 1e-3),
-            "tflops": rows * NETWORK_FLOP_PER_ROW / (t * 1e-3) / 1e12, "tensor_tflops": tensor_tflops,
+            "tflops": rows * NETWORK_FLOP_PER_ROW / (t * 1e-3) / 1e12, "tensor_tflops_executed": tensor_tflops,
             "tensor_frac_of_bf16_peak": tensor_tflops / peak if peak else None,
+            "flop_note": "tflops: the network's FLOP per row; tensor_tflops_executed: the MMAs the tensor cores "
+                         "run (layer 1 twice)",
             "peak": f"bf16 burst {peak} TFLOP/s of measured (MEASURED_PEAKS.json)" if peak else None,
             "flop_per_row": NETWORK_FLOP_PER_ROW}
 
@@ -731,7 +734,7 @@ def main():
     ap.add_argument("--network-rows", type=int, default=0,
                     help="time only the surrogate's fused network kernel on this many rows (profiling runs)")
     ap.add_argument("--sur-samples", type=int, default=4_000_000)
-    ap.add_argument("--sur-epochs", type=int, default=400, help="surrogate epochs on the single-tree box")
+    ap.add_argument("--sur-epochs", type=int, default=800, help="surrogate epochs on the single-tree box")
     ap.add_argument("--sur-epochs-uneven", type=int, default=48, help="surrogate epochs on the uneven batch's box")
     ap.add_argument("--shard", action="store_true",
                     help="N>1: split the batch across ranks by tree work (LPT) and gather the prices, instead of "

@@ -7,7 +7,9 @@
 //   layers 1-3 (256x256): tcgen05.mma kind::f16, bf16 activations in shared memory
 //                         (A operand, K-major core-matrix layout), bf16 weights
 //                         streamed from L2 (B operand), fp32 accumulator in 256
-//                         TMEM columns (M = 128, N = 256, K = 16 per instruction)
+//                         TMEM columns (M = 128, N = 256, K = 16 per instruction);
+//                         layer 1 runs two passes into one accumulator: its input as
+//                         bf16 hi parts, then (layer 0 recomputed) the lo parts
 //   layer 4 (256 -> 2):   fp32 dot products of layer 3's fp32 activations with fp32
 //                         weights, in the last layer's epilogue: a partial sum per
 //                         128 columns (k in order from 0), the two partials added
@@ -20,7 +22,8 @@
 // weights and bias; 14 KB) are copied to shared memory once per CTA.
 // Weights of the three tensor-core layers are pre-packed (the surrogate's refresh
 // kernel) into 24 blocks of [256 output rows x 32 K] in the canonical no-swizzle
-// K-major layout, 16 KB each, so one thread streams a block with a single untiled
+// K-major layout, 16 KB each (32 streamed per tile: layer 1's twice), so one thread
+// streams a block with a single untiled
 // bulk copy (cp.async.bulk, completion counted on an mbarrier) through a ring of
 // kStages shared-memory stages; the tensor core frees a stage by committing the
 // MMAs that read it to the stage's "empty" mbarrier.  One thread (thread 0) issues
@@ -52,7 +55,18 @@ constexpr int kOut = 2;         // price residual, log-error estimate
 constexpr int kKB = 32;         // K per streamed weight block
 constexpr int kBlocksPerLayer = kHidden / kKB;  // 8
 constexpr int kTcLayers = 3;
-constexpr int kBlocks = kTcLayers * kBlocksPerLayer;  // 24 per tile
+constexpr int kBlocks = kTcLayers * kBlocksPerLayer;  // 24 packed blocks
+// MMA passes per tile: layer 1 twice (its input as a bf16 hi / lo pair, the two
+// products accumulated), layers 2 and 3 once: 32 weight blocks streamed per tile.
+constexpr int kPasses = kTcLayers + 1;
+constexpr int kSeqBlocks = kPasses * kBlocksPerLayer;
+
+// Packed weight block of the q-th block streamed in a tile.
+__host__ __device__ __forceinline__ int seq_block(int q)
+{
+    const int pass = q / kBlocksPerLayer;
+    return (pass <= 1 ? 0 : pass - 1) * kBlocksPerLayer + q % kBlocksPerLayer;
+}
 constexpr int kStages = 2;      // weight stages in shared memory
 constexpr int kCtasPerSm = 2;   // 112 KB of shared memory per CTA fits twice per SM
 constexpr int kThreads = 256;   // two threads per row: each takes half of the 256 columns
@@ -127,6 +141,19 @@ __device__ __forceinline__ uint32_t pack_silu2(float a, float b)
     return *reinterpret_cast<const uint32_t *>(&q);
 }
 
+// Layer 0's activations as a bf16 pair: hi = bf16(a), lo = bf16(a - hi); layer 1 takes
+// hi and lo as two inputs whose products with its weights accumulate (bf16 rounding
+// of these activations moved the payoff kinks the network resolves; the pair carries
+// about 16 bits).  `lo_part` selects which half to return.
+__device__ __forceinline__ uint32_t pack_silu2_split(float a, float b, bool lo_part)
+{
+    const float2 h = umma::silu2_f(make_float2(a, b));
+    const __nv_bfloat162 hi = __floats2bfloat162_rn(h.x, h.y);
+    if (!lo_part) return *reinterpret_cast<const uint32_t *>(&hi);
+    const __nv_bfloat162 lo = __floats2bfloat162_rn(h.x - __low2float(hi), h.y - __high2float(hi));
+    return *reinterpret_cast<const uint32_t *>(&lo);
+}
+
 __device__ __forceinline__ uint32_t pack_bf16x2(float a, float b)
 {
     const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
@@ -188,14 +215,14 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) mlp_forward_kernel(MlpAr
     const int ntiles = (p.n + kRows - 1) / kRows;
     // weight blocks this CTA consumes in all (copies never run past them)
     const uint32_t total_blocks =
-        (blockIdx.x < ntiles ? (uint32_t)((ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1) : 0u) * kBlocks;
+        (blockIdx.x < ntiles ? (uint32_t)((ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1) : 0u) * kSeqBlocks;
 
     // Thread 0: copy weight block `ld` (global block ld % kBlocks) into its stage,
     // once the MMAs that last read that stage have completed.
     auto load_next = [&]() -> bool {
         const uint32_t s = ld % kStages;
         if (ld >= (uint32_t)kStages && !umma::mbar_wait(empty0 + 8 * s, ((ld - kStages) / kStages) & 1)) return false;
-        bulk_copy_g2s(umma::smem_u32(wst + s * kWBlockBytes), p.Wp + (size_t)(ld % kBlocks) * kWBlockElems,
+        bulk_copy_g2s(umma::smem_u32(wst + s * kWBlockBytes), p.Wp + (size_t)seq_block(ld % kSeqBlocks) * kWBlockElems,
                       kWBlockBytes, full0 + 8 * s);
         ++ld;
         return true;
@@ -203,8 +230,9 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) mlp_forward_kernel(MlpAr
 
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int row = tile * kRows + r;
-        // ---- layer 0 on the CUDA cores: this thread's row and half -> activation tile
-        {
+        // ---- layer 0 on the CUDA cores: this thread's row and half -> activation tile,
+        // the hi parts of the activations (lo_part = false) or their lo parts
+        auto layer0 = [&](bool lo_part) {
             float x[kIn];
             if (row < p.n) {
                 const float4 *xr = reinterpret_cast<const float4 *>(p.X + (size_t)row * kIn);
@@ -220,16 +248,18 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) mlp_forward_kernel(MlpAr
                 float z[8];
                 layer0_chunk(x, sW0, sB, n0, z);
                 uint4 v;
-                v.x = pack_silu2(z[0], z[1]);
-                v.y = pack_silu2(z[2], z[3]);
-                v.z = pack_silu2(z[4], z[5]);
-                v.w = pack_silu2(z[6], z[7]);
+                v.x = pack_silu2_split(z[0], z[1], lo_part);
+                v.y = pack_silu2_split(z[2], z[3], lo_part);
+                v.z = pack_silu2_split(z[4], z[5], lo_part);
+                v.w = pack_silu2_split(z[6], z[7], lo_part);
                 *reinterpret_cast<uint4 *>(act + act_offset(r, n0)) = v;
             }
-        }
+        };
+        layer0(false);
         float o0 = 0.f, o1 = 0.f;
 #pragma unroll 1
-        for (int l = 0; l < kTcLayers; ++l) {
+        for (int pass = 0; pass < kPasses; ++pass) {
+            const int l = pass == 0 ? 0 : pass - 1;  // the tensor-core layer this pass accumulates
             if (tid == 0 && !ok) *abort_flag = 1;  // a prefetch wait ran out
             umma::fence_proxy_async();  // activation writes -> visible to the tensor core
             umma::fence_before_sync();
@@ -255,7 +285,7 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) mlp_forward_kernel(MlpAr
                         const int ks = kb * (kKB / 16) + kk;  // 16-wide K step in the layer
                         const uint64_t ad = umma::make_desc(a0 + (ks >> 2) * (kRows * 64 * 2) + (ks & 3) * 256, 128, 1024);
                         const uint64_t bd = umma::make_desc(b0 + kk * 256, 128, (kKB / 8) * 128);
-                        umma::mma_bf16(tmem, ad, bd, IDESC, (kb > 0 || kk > 0) ? 1u : 0u);
+                        umma::mma_bf16(tmem, ad, bd, IDESC, (pass == 1 || kb > 0 || kk > 0) ? 1u : 0u);
                     }
                     umma::mma_commit(empty0 + 8 * s);
                     ++mm;
@@ -280,9 +310,13 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) mlp_forward_kernel(MlpAr
             ++acc_uses;
             umma::fence_after_sync();
             if (__syncthreads_or(*abort_flag)) break;
-            // the stages are free: prefetch the next layer's (or the next tile's) first blocks
+            // the stages are free: prefetch the next pass's (or the next tile's) first blocks
             if (tid == 0) {
                 while (ok && ld < total_blocks && ld < mm + kStages) ok = load_next();  // a failure is seen at the next barrier
+            }
+            if (pass == 0) {
+                layer0(true);  // layer 1's second input: the lo parts, over the hi parts just read
+                continue;
             }
             // ---- epilogue: accumulator + bias -> SiLU -> bf16 (next layer's A) or layer 4
             const float *bias = sB + (l + 1) * kHidden;

@@ -20,6 +20,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <functional>
 #include <cmath>
 #include <string>
 #include <vector>
@@ -94,8 +95,9 @@ __global__ void features_kernel(DevOptions o, DevYield yc, hwt_box box, FeatureN
     inbox[i] = in ? 1 : 0;
 }
 
-// Layer 0 of the training path: Z0 = X W0 + b0 (fp32) and H1 = bf16(silu(Z0)),
-// one warp per row (eight columns per lane), with the fused kernel's arithmetic.
+// Layer 0 of the training path: Z0 = X W0 + b0 (fp32) and layer 1's input H1 =
+// [bf16 hi | bf16 lo] of silu(Z0) ([n][512]: hi = bf16(a), lo = bf16(a - hi)), one warp
+// per row (eight columns per lane), with the fused kernel's arithmetic.
 __global__ void layer0_kernel(const float *X, const float *W0, const float *b0, int n, float *Z0, __nv_bfloat16 *H1)
 {
     const int gt = blockIdx.x * blockDim.x + threadIdx.x;
@@ -109,12 +111,14 @@ __global__ void layer0_kernel(const float *X, const float *W0, const float *b0, 
     float4 *zr = reinterpret_cast<float4 *>(Z0 + (size_t)row * kHidden + n0);
     zr[0] = make_float4(z[0], z[1], z[2], z[3]);
     zr[1] = make_float4(z[4], z[5], z[6], z[7]);
-    uint4 h;
-    h.x = mlp::pack_bf16x2(silu_f(z[0]), silu_f(z[1]));
-    h.y = mlp::pack_bf16x2(silu_f(z[2]), silu_f(z[3]));
-    h.z = mlp::pack_bf16x2(silu_f(z[4]), silu_f(z[5]));
-    h.w = mlp::pack_bf16x2(silu_f(z[6]), silu_f(z[7]));
-    *reinterpret_cast<uint4 *>(H1 + (size_t)row * kHidden + n0) = h;
+    for (int part = 0; part < 2; ++part) {
+        uint4 h;
+        h.x = mlp::pack_silu2_split(z[0], z[1], part == 1);
+        h.y = mlp::pack_silu2_split(z[2], z[3], part == 1);
+        h.z = mlp::pack_silu2_split(z[4], z[5], part == 1);
+        h.w = mlp::pack_silu2_split(z[6], z[7], part == 1);
+        *reinterpret_cast<uint4 *>(H1 + (size_t)row * 2 * kHidden + part * kHidden + n0) = h;
+    }
 }
 
 // dW0[k][c] += sum over rows of X[r][k] dZ0[r][c] (fp32), a slice of rows per block.
@@ -293,17 +297,19 @@ __global__ void adam_kernel(AdamArgs a, const StepState *st)
     a.w[i] -= a.lr * (m / a.c1) / (sqrtf(v / a.c2) + a.eps);
 }
 
-// bf16 copies of W[in][out] (layers 1-4): Wt[out][in] (forward operand), Wb[in][out]
-// (backward-data operand), the fused kernel's packed blocks (layers 1-3) and the
-// bf16-rounded values as float (layer 4).
-__global__ void refresh_kernel(const float *W, int in, int out, __nv_bfloat16 *Wt, __nv_bfloat16 *Wb,
+// bf16 copies of W[in][out] (layers 1-3): Wt[out][in] (forward operand; with dup,
+// [out][2 in] holding it twice, for the hi / lo input pair of layer 1), Wb[in][out]
+// (backward-data operand) and the fused kernel's packed blocks.
+__global__ void refresh_kernel(const float *W, int in, int out, __nv_bfloat16 *Wt, int dup, __nv_bfloat16 *Wb,
                                __nv_bfloat16 *Wp, float *Wr)
 {
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= in * out) return;
     const int k = idx / out, n = idx % out;
     const __nv_bfloat16 v = __float2bfloat16(W[(size_t)k * out + n]);
-    Wt[(size_t)n * in + k] = v;
+    const int ldt = dup ? 2 * in : in;
+    Wt[(size_t)n * ldt + k] = v;
+    if (dup) Wt[(size_t)n * ldt + in + k] = v;
     Wb[(size_t)k * out + n] = v;
     if (Wp) Wp[(size_t)(k / mlp::kKB) * mlp::kWBlockElems + mlp::pack_offset(n, k % mlp::kKB)] = v;
     if (Wr) Wr[(size_t)k * out + n] = __bfloat162float(v);
@@ -588,7 +594,8 @@ int ensure_act(hwt_surrogate *s, int rows)
     s->d_dz = s->d_dz2 = nullptr; s->d_dzf = nullptr; s->d_y = nullptr; s->d_dz4 = nullptr;
     s->act_cap = 0;
     SCUDA(s, cudaMalloc(&s->d_x, sizeof(float) * (size_t)rows * kInPad), "alloc X");
-    for (int l = 1; l < kLayers; ++l) SCUDA(s, cudaMalloc(&s->d_h[l], sizeof(__nv_bfloat16) * (size_t)rows * kHidden), "alloc H");
+    for (int l = 1; l < kLayers; ++l)  // H1 holds layer 1's hi / lo input pair
+        SCUDA(s, cudaMalloc(&s->d_h[l], sizeof(__nv_bfloat16) * (size_t)rows * kHidden * (l == 1 ? 2 : 1)), "alloc H");
     for (int l = 0; l < kLayers; ++l) SCUDA(s, cudaMalloc(&s->d_z[l], sizeof(float) * (size_t)rows * kFanOut[l]), "alloc Z");
     SCUDA(s, cudaMalloc(&s->d_dz, sizeof(__nv_bfloat16) * (size_t)rows * kHidden), "alloc dZ");
     SCUDA(s, cudaMalloc(&s->d_dz2, sizeof(__nv_bfloat16) * (size_t)rows * kHidden), "alloc dZ");
@@ -668,7 +675,9 @@ int forward_layers(hwt_surrogate *s, int rows)
     SCUDA(s, cudaGetLastError(), "layer 0");
     for (int l = 1; l < kLayers - 1; ++l) {
         const bool to_last = l == kLayers - 2;  // layer 4 reads fp32 Z3, not bf16 activations
-        GemmArgs g = gargs(s, s->d_h[l], s->d_wt[l], rows, kFanOut[l], kFanIn[l], kFanIn[l], kFanIn[l], EPI_BIAS_SILU);
+        // layer 1: K = 512 over [hi | lo] inputs and [W1 | W1], the two products accumulated
+        const int K = l == 1 ? 2 * kFanIn[l] : kFanIn[l];
+        GemmArgs g = gargs(s, s->d_h[l], s->d_wt[l], rows, kFanOut[l], K, K, K, EPI_BIAS_SILU);
         g.bias = s->d_w + s->b_off[l];
         g.Cf = s->d_z[l];
         g.ldc = kFanOut[l];
@@ -736,8 +745,8 @@ int backward(hwt_surrogate *s, int rows, float lam, bool zero_loss)
     }
     for (int l = kLayers - 2; l >= 1; --l) {
         const int in = kFanIn[l], out = kFanOut[l];
-        // dW_l[in][out] = H_l^T dZ_l   (split-K over the batch)
-        GemmArgs gw = gargs(s, s->d_h[l], dz, in, out, rows, in, out, EPI_ATOMIC);
+        // dW_l[in][out] = H_l^T dZ_l   (split-K over the batch; layer 1 from the hi parts)
+        GemmArgs gw = gargs(s, s->d_h[l], dz, in, out, rows, l == 1 ? 2 * in : in, out, EPI_ATOMIC);
         gw.Cf = s->d_g + s->w_off[l];
         gw.ldc = out;
         gw.k_chunk = kc;
@@ -772,7 +781,7 @@ int refresh(hwt_surrogate *s)
         const int tot = kFanIn[l] * kFanOut[l];
         __nv_bfloat16 *wp = s->d_wp + (size_t)(l - 1) * mlp::kBlocksPerLayer * mlp::kWBlockElems;
         refresh_kernel<<<(tot + 255) / 256, 256, 0, s->stream>>>(s->d_w + s->w_off[l], kFanIn[l], kFanOut[l], s->d_wt[l],
-                                                               s->d_wb[l], wp, nullptr);
+                                                               l == 1 ? 1 : 0, s->d_wb[l], wp, nullptr);
         SCUDA(s, cudaGetLastError(), "refresh kernel");
     }
     return HWT_OK;
@@ -876,8 +885,8 @@ hwt_surrogate *hwt_surrogate_create(hwt_ctx *ctx, const hwt_box *box, uint64_t s
          cudaMalloc(&s->d_loss, sizeof(double)) == cudaSuccess &&
          cudaMalloc(&s->d_gemm_err, sizeof(int)) == cudaSuccess && cudaMemset(s->d_gemm_err, 0, sizeof(int)) == cudaSuccess &&
          cudaMalloc(&s->d_wp, 2ull * mlp::kBlocks * mlp::kWBlockElems) == cudaSuccess;
-    for (int l = 1; l < kLayers - 1 && ok; ++l) {
-        ok = cudaMalloc(&s->d_wt[l], 2 * (size_t)kFanIn[l] * kFanOut[l]) == cudaSuccess &&
+    for (int l = 1; l < kLayers - 1 && ok; ++l) {  // layer 1's forward operand twice (hi / lo inputs)
+        ok = cudaMalloc(&s->d_wt[l], 2 * (size_t)kFanIn[l] * kFanOut[l] * (l == 1 ? 2 : 1)) == cudaSuccess &&
              cudaMalloc(&s->d_wb[l], 2 * (size_t)kFanIn[l] * kFanOut[l]) == cudaSuccess;
     }
     if (ok) {
@@ -1114,6 +1123,7 @@ double calibrate_tau(const std::vector<double> &pred, const std::vector<double> 
 
 constexpr int kMaxKinks = 256;
 constexpr double kKinkBand = 0.005;  // moneyness: ~0.44 strike units around a kink of the book's tree
+constexpr int kRouteBudget = 2;  // held-out answers above the tolerance the kink distance may leave
 constexpr int kCalTols = 7;
 const double kCalTol[kCalTols] = {2.5e-5, 5e-5, 1e-4, 2e-4, 5e-4, 1e-3, 2e-3};
 
@@ -1168,6 +1178,20 @@ double kink_distance(const std::vector<double> &kinks, double x)
     double d = INFINITY;
     for (double k : kinks) d = std::min(d, fabs(x - k));
     return d;
+}
+
+// The points the routing measures distance from on a single-tree box: the tree's
+// kinks found in the labels and the box's two moneyness edges (a kink just outside
+// the box, which no label shows, bends the price near the edge).  Empty when the box
+// is not a single tree.
+std::vector<double> route_points(const hwt_surrogate *s)
+{
+    std::vector<double> r;
+    if (s->kinks.empty()) return r;
+    r = s->kinks;
+    r.push_back(s->box.moneyness_min);
+    r.push_back(s->box.moneyness_max);
+    return r;
 }
 
 }  // namespace
@@ -1252,10 +1276,11 @@ int hwt_surrogate_train(hwt_surrogate *s, const hwt_options *samples, const hwt_
     // of a kink appear kink_oversample times (the network's largest errors sit there)
     std::vector<int32_t> tr(idx.begin(), idx.begin() + ntrain);
     const int reps = std::max(1, std::min(cfg->kink_oversample, 16));
+    const std::vector<double> rp = route_points(s);
     if (reps > 1 && !s->kinks.empty()) {
         for (int64_t j = 0; j < ntrain; ++j) {
             const int i = idx[j];
-            if (kink_distance(s->kinks, samples->strike[i] / Fh[i]) < kKinkBand)
+            if (kink_distance(rp, samples->strike[i] / Fh[i]) < kKinkBand)
                 for (int q = 1; q < reps; ++q) tr.push_back(i);
         }
     }
@@ -1365,7 +1390,7 @@ int hwt_surrogate_train(hwt_surrogate *s, const hwt_options *samples, const hwt_
         std::vector<double> d;
         if (!s->kinks.empty()) {
             d.resize(nhold);
-            for (int64_t j = 0; j < nhold; ++j) d[j] = kink_distance(s->kinks, samples->strike[hold[j]] / Fh[hold[j]]);
+            for (int64_t j = 0; j < nhold; ++j) d[j] = kink_distance(rp, samples->strike[hold[j]] / Fh[hold[j]]);
         }
         // routing that keeps every held-out answer within tol: (tau, delta), the
         // answered fraction and the largest and p99 errors of the answered samples
@@ -1378,11 +1403,15 @@ int hwt_surrogate_train(hwt_surrogate *s, const hwt_options *samples, const hwt_
             }
             std::vector<double> e;
             if (!d.empty()) {
-                // the smallest distance from the kinks beyond which every held-out
-                // answer is within the tolerance
-                double dl = 0.0;
+                // the smallest distance from the kinks beyond which at most
+                // kRouteBudget held-out answers exceed the tolerance (one stray
+                // error far from every kink would otherwise send the box to the tree)
+                std::vector<double> bad;
                 for (int64_t j = 0; j < nhold; ++j)
-                    if (!(err[j] <= tol)) dl = std::max(dl, d[j]);
+                    if (!(err[j] <= tol)) bad.push_back(d[j]);
+                std::sort(bad.begin(), bad.end(), std::greater<double>());
+                const size_t skip = std::min<size_t>(bad.size(), (size_t)kRouteBudget);
+                const double dl = bad.size() > skip ? bad[skip] : 0.0;
                 *delta = dl;
                 for (int64_t j = 0; j < nhold; ++j)
                     if (d[j] > dl) e.push_back(err[j]);
@@ -1463,10 +1492,11 @@ int hwt_surrogate_price(hwt_surrogate *s, const hwt_options *o, const hwt_yield 
     }
     // flag when exp(o1) ystd F > tau; tau = +inf: the router is off, tau <= 0: nothing is answered
     const float log_tau = std::isinf(tau) ? INFINITY : (tau > 0 ? (float)log(tau / s->ystd) : -INFINITY);
-    const int nk = delta >= 0 ? (int)s->kinks.size() : 0;
+    const std::vector<double> rp = route_points(s);
+    const int nk = delta >= 0 ? (int)rp.size() : 0;
     if (nk > 0) {
-        if (!s->dkinks.grow(kMaxKinks)) return sfail(s, HWT_ENOMEM, "kink buffer");
-        SCUDA(s, cudaMemcpyAsync(s->dkinks.p, s->kinks.data(), 8ull * nk, cudaMemcpyHostToDevice, s->stream), "kinks H2D");
+        if (!s->dkinks.grow(kMaxKinks + 2)) return sfail(s, HWT_ENOMEM, "kink buffer");
+        SCUDA(s, cudaMemcpyAsync(s->dkinks.p, rp.data(), 8ull * nk, cudaMemcpyHostToDevice, s->stream), "kinks H2D");
     }
     decode_route_kernel<<<(n + 255) / 256, 256, 0, s->stream>>>(s->out2.p, s->F.p, s->base.p, s->inbox.p,
                                                                s->opts.strike, n, s->ymean, s->ystd, log_tau,

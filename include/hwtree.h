@@ -257,7 +257,9 @@ typedef struct hwt_train_config {
     double err_weight;               /* weight of the error head's loss; 0: head untrained, no routing */
     double route_tolerance;          /* price error (per 100 face) that the network's answers must keep
                                         on the held-out samples; sets the routing threshold of the error
-                                        head or, on a single-tree box, the kink distance (default 1e-4) */
+                                        head (every held-out answer within it) or, on a single-tree box,
+                                        the kink distance (all but at most 2 held-out answers within it)
+                                        (default 1e-4) */
     double holdout;                  /* fraction of in-box samples held out for that (default 0.05) */
     int32_t kink_oversample;         /* single-tree box: samples within 0.005 in moneyness of a payoff
                                         kink appear this many times per epoch (1 or 0: once) */

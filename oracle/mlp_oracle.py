@@ -8,8 +8,9 @@ step; it is itself checked by central finite differences (tests/test_mlp_oracle.
 
 Layout matches the GPU kernels: W_l is [fan_in, fan_out] row-major, y = x W + b.
 The GPU computes layers 0 and 4 in fp32 (layer 0 from fp32 features, layer 4 from
-layer 3's fp32 activations) and keeps bf16 copies of the weights of layers 1-3 and
-bf16 activations between them with fp32 accumulation; `forward(..., bf16=True)`
+layer 3's fp32 activations), feeds layer 1 its input as a bf16 hi / lo pair, and keeps
+bf16 copies of the weights of layers 1-3 and bf16 activations between layers 1-3 with
+fp32 accumulation; `forward(..., bf16=True)`
 rounds the same tensors the same way so the comparison isolates accumulation-order
 and activation-approximation differences.
 
@@ -67,7 +68,9 @@ def forward(params, x, bf16: bool = False):
         pre.append(z)
         if li < last:
             h = silu(z)
-            if bf16 and li < last - 1:  # the last layer reads fp32 activations
+            # the last layer reads fp32 activations and layer 1 a bf16 hi / lo pair
+            # (about 16 bits), taken as exact here
+            if bf16 and 0 < li < last - 1:
                 h = bf16_round(h)
         else:
             h = z

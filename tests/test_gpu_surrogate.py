@@ -212,20 +212,21 @@ def test_kink_routing_on_the_single_tree_box(pkg, pricer, orc):
 
 def test_single_tree_surrogate_prices_faster_than_the_mixed_tree(pkg, pricer):
     """The learned part on the single-tree box (samples drawn as the 1,000-option book
-    draws them, so only strike and type vary): trained on 4M tree-priced samples, the
-    surrogate prices 1M fresh queries (10% outside the box) through the public
-    host-array call faster than the batched mixed tree prices the same queries, with
-    the judge enforcing 5e-4 per 100 face and not falling back, and every answer
-    within 5e-4 of the batched FP64 tree.  (At 1e-4 the network does not hold: its
-    held-out maximum is about 1.5e-4 after 800 epochs, so the routing sends the box
-    to the tree.)"""
+    draws them, so only strike and type vary), trained on 4M tree-priced samples with
+    the samples near the tree's payoff kinks repeated 3x: through the public
+    host-array call it prices 1M fresh queries (10% outside the box) faster than the
+    batched mixed tree prices the same queries, with the judge enforcing 1e-4 per 100
+    face on its 1% sample and not falling back.  Most in-box queries are answered by
+    the network (routing calibrated on held-out samples; 400 epochs here, the bench
+    trains 800), and its answers stay within 1e-4 of the batched FP64 tree but for a
+    few per 100,000 within 2e-4."""
     import time
     wl = pkg.workloads
     rates, days = wl.yield_curve()
     y = pkg.Yield(rates, days)
     s = pkg.Surrogate(pricer, box=wl.single_tree_box(), seed=1)
-    st = s.train(pkg.Options.from_batch(wl.single_tree_training_batch(4_000_000, 3)), y, epochs=200, batch=8192,
-                 lr=2e-3, lr_min=2e-6)
+    st = s.train(pkg.Options.from_batch(wl.single_tree_training_batch(4_000_000, 3)), y, epochs=400, batch=8192,
+                 lr=2e-3, lr_min=2e-6, kink_oversample=3)
     assert st["n_kinks"] == 12
     q = wl.single_tree_query_batch(1_000_000, 4)
     qo = pkg.Options.from_batch(q)
@@ -241,10 +242,11 @@ def test_single_tree_surrogate_prices_faster_than_the_mixed_tree(pkg, pricer):
 
     t_tree, _ = best(lambda: pricer.price(qo, y, pkg.BATCHED_MIXED))
     t_sur, got = best(lambda: s.price(qo, y, judge_fraction=0.01, seed=7, tree_mode=pkg.BATCHED_MIXED,
-                                      judge_tolerance=5e-4))
+                                      judge_tolerance=1e-4))
     stats = s.stats.as_dict()
     s.close()
-    assert stats["fell_back"] == 0 and stats["judge_max_abs"] <= 5e-4 and stats["n_judged"] > 5000
+    assert stats["fell_back"] == 0 and stats["judge_max_abs"] <= 1e-4 and stats["n_judged"] > 2500, stats
     assert stats["n_network"] >= 0.5 * stats["n_in_box"], stats
-    assert np.max(np.abs(got - ref)) <= 5e-4
+    err = np.abs(got - ref)
+    assert np.mean(err <= 1e-4) >= 0.9999 and np.max(err) <= 2e-4, (np.sum(err > 1e-4), np.max(err))
     assert t_sur < t_tree, (t_sur, t_tree)
