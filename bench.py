@@ -366,24 +366,39 @@ def surrogate_run(pkg, pricer, y, box, train, queries, epochs: int, reps: int, b
     mixed_rate = trees["batched_mixed"]["options_per_s"]
     # options/s at each judge tolerance: the routing calibrated on the held-out samples
     # for it, the judge enforcing it (answers above it send the network's answers to the tree)
+    # Every call draws its own judge sample (seed), so a call can fall back where another
+    # does not: options/s is the mean over the calls after the first (total options over
+    # total wall time, fallbacks included), with the best call and the fallback count beside.
     at = {}
+    calls = max(reps, 16)
     for tol in (1e-4, 2e-4, 5e-4, 1e-3):
-        wall, got = [], None
-        for k in range(reps + 1):
+        wall, sts, worst, worst_inb_p99 = [], [], 0.0, 0.0
+        for k in range(calls + 1):
             t0 = time.perf_counter()
             got = sur.price(qo, y, judge_fraction=0.01, seed=7 + k, tree_mode=pkg.BATCHED_MIXED, judge_tolerance=tol)
             wall.append(time.perf_counter() - t0)
-        st = sur.stats.as_dict()
+            sts.append(sur.stats.as_dict())
+            err = np.abs(got - ref)
+            worst = max(worst, float(np.max(err)))
+            worst_inb_p99 = max(worst_inb_p99, float(np.percentile(err[inb], 99)))
+        mean = sum(wall[1:]) / calls
         best = min(wall[1:])
-        err = np.abs(got - ref)
+        timed = sts[1:]
+        st = timed[-1]
         at[f"{tol:g}"] = {
-            "options_per_s": qo.N / best, "host_ms": 1e3 * best, "x_batched_mixed": (qo.N / best) / mixed_rate,
-            "x_plain_fp64": (qo.N / best) / trees["plain_fp64"]["options_per_s"],
-            "network_answered": st["n_network"], "routed_in_box": st["n_flagged"], "outside_box": st["n_routed"],
-            "fell_back": bool(st["fell_back"]), "route_tolerance": st["route_tolerance"],
-            "judge": {k: st[k] for k in ("n_judged", "judge_max_abs", "judge_p99_abs", "judge_mean_abs")},
-            "max_abs_err": float(np.max(err)), "in_box_p99_abs_err": float(np.percentile(err[inb], 99)),
-            "device_ms": {k: st[k] for k in ("network_ms", "tree_ms", "total_ms")}}
+            "options_per_s": qo.N / mean, "host_ms": 1e3 * mean, "x_batched_mixed": (qo.N / mean) / mixed_rate,
+            "x_plain_fp64": (qo.N / mean) / trees["plain_fp64"]["options_per_s"],
+            "best_call_options_per_s": qo.N / best, "calls": calls,
+            "calls_fell_back": sum(int(t["fell_back"]) for t in timed),
+            "network_answered_min": min(t["n_network"] for t in timed),
+            "network_answered_max": max(t["n_network"] for t in timed),
+            "routed_in_box": st["n_flagged"], "outside_box": st["n_routed"],
+            "route_tolerance": st["route_tolerance"],
+            "judge_max_abs_over_calls": max(t["judge_max_abs"] for t in timed),
+            "n_judged": st["n_judged"],
+            "max_abs_err_over_calls": worst, "in_box_p99_abs_err_over_calls": worst_inb_p99,
+            "device_ms_mean": {k: sum(t[k] for t in timed) / calls
+                               for k in ("copy_ms", "network_ms", "tree_ms", "total_ms")}}
     on_batch = None
     if batch is not None:
         # the same network on a batch of its own box (the 30,000-option uneven batch)
@@ -409,9 +424,9 @@ def surrogate_run(pkg, pricer, y, box, train, queries, epochs: int, reps: int, b
         "train": {**tstats, "wall_s": train_s, "epochs": epochs, "samples_offered": len(train["strike"]),
                   "kink_oversample": kink_oversample},
         "queries": {"n": int(qo.N), "outside_box": int(queries["outside"].sum()), "at_judge_tolerance": at,
-                    "timing": "host clock around hwt_surrogate_price (host arrays in and out), best of the calls "
-                              "after the first; trees: host clock around hwt_price_ex on the same queries; errors "
-                              "against the batched FP64 tree"},
+                    "timing": "host clock around hwt_surrogate_price (host arrays in and out), mean of the calls "
+                              "after the first, each with its own judge sample; trees: host clock around "
+                              "hwt_price_ex on the same queries, best call; errors against the batched FP64 tree"},
         "trees": trees,
     }
 
@@ -534,6 +549,15 @@ def run_ours(args, rank, world, local):
             pkg, pricer, y, box=None, train=wl.surrogate_training_batch(args.sur_samples, 3),
             queries=wl.surrogate_query_batch(1_000_000, 4), epochs=args.sur_epochs_uneven, reps=3,
             batch=(opts, ref_prices))
+        # the judged surrogate at 1e-4 beside the trees (its own workload: 1M queries on
+        # the single-tree box, 10% outside it)
+        a = surrogate["single_tree"]["queries"]["at_judge_tolerance"]["0.0001"]
+        modes["surrogate"] = {
+            "workload": "single_tree_1m (4M training samples, 1M queries, 10% outside the box)",
+            "judge_tolerance": 1e-4, "options_per_s": a["options_per_s"],
+            "x_batched_mixed_same_queries": a["x_batched_mixed"], "calls": a["calls"],
+            "calls_fell_back": a["calls_fell_back"], "max_abs_err_over_calls": a["max_abs_err_over_calls"],
+            "judge_max_abs_over_calls": a["judge_max_abs_over_calls"]}
     # the reference's seven benchmark distributions (65,536 options each, data/yield.in
     # curve), device time per batch, beside the thesis's best CUDA numbers
     datasets = None
@@ -559,6 +583,8 @@ def run_ours(args, rank, world, local):
         fp64_rate = modes["batched_fp64"]["options_per_s"]
         plain_rate = modes["plain_fp64"]["options_per_s"]
         for e in modes.values():
+            if "workload" in e:
+                continue  # measured on its own workload, against the trees on the same queries
             e["x_batched_fp64"] = e["options_per_s"] / fp64_rate
             e["x_plain_fp64"] = e["options_per_s"] / plain_rate
 

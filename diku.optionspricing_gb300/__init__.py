@@ -538,7 +538,8 @@ class TrainStats(ctypes.Structure):
                 ("holdout_answered", ctypes.c_double), ("holdout_max_abs", ctypes.c_double),
                 ("holdout_p99_abs", ctypes.c_double), ("holdout_all_max_abs", ctypes.c_double),
                 ("holdout", ctypes.c_int64), ("n_kinks", ctypes.c_int64), ("kink_delta", ctypes.c_double),
-                ("ladder_tolerance", ctypes.c_double * 7), ("ladder_answered", ctypes.c_double * 7)]
+                ("ladder_tolerance", ctypes.c_double * 7), ("ladder_answered", ctypes.c_double * 7),
+                ("holdout_over", ctypes.c_int64)]
 
     def as_dict(self) -> dict:
         d = {name: getattr(self, name) for name, _ in self._fields_}
@@ -552,7 +553,7 @@ class SurrogateStats(ctypes.Structure):
                 ("fell_back", ctypes.c_int32), ("pad", ctypes.c_int32), ("judge_max_abs", ctypes.c_double), ("judge_p99_abs", ctypes.c_double),
                 ("judge_mean_abs", ctypes.c_double), ("network_ms", ctypes.c_double), ("tree_ms", ctypes.c_double),
                 ("route_ms", ctypes.c_double), ("total_ms", ctypes.c_double), ("n_flagged", ctypes.c_int64),
-                ("n_network", ctypes.c_int64), ("route_tolerance", ctypes.c_double)]
+                ("n_network", ctypes.c_int64), ("route_tolerance", ctypes.c_double), ("copy_ms", ctypes.c_double)]
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_}

@@ -516,7 +516,7 @@ struct hwt_surrogate {
     hwt_ctx *ctx = nullptr;
     int device = 0, sms = 0;
     cudaStream_t stream = nullptr;
-    cudaEvent_t ev[4] = {};
+    cudaEvent_t ev[5] = {};
     hwt_box box;
     FeatureNorm fn;
     double ymean = 0.0, ystd = 1.0;
@@ -1066,7 +1066,7 @@ struct Scoped {
 
 // Features, forward prices and closed-form bases of the host options into the
 // surrogate's pricing buffers (options copied to s->opts).
-int features_for(hwt_surrogate *s, const hwt_options *o, const hwt_yield *y)
+int features_for(hwt_surrogate *s, const hwt_options *o, const hwt_yield *y, cudaEvent_t after_copy = nullptr)
 {
     const int n = o->n;
     DevYield yc;
@@ -1076,6 +1076,7 @@ int features_for(hwt_surrogate *s, const hwt_options *o, const hwt_yield *y)
         !s->inbox.grow(n))
         return sfail(s, HWT_ENOMEM, "pricing buffers");
     SCUDA(s, upload_batch(s->opts, o, s->stream), "options H2D");
+    if (after_copy) SCUDA(s, cudaEventRecord(after_copy, s->stream), "event");
     features_kernel<<<(n + 255) / 256, 256, 0, s->stream>>>(dev_view(s->opts, n), yc, s->box, s->fn, s->xf.p, s->F.p,
                                                            s->base.p, s->inbox.p);
     SCUDA(s, cudaGetLastError(), "features kernel");
@@ -1365,6 +1366,7 @@ int hwt_surrogate_train(hwt_surrogate *s, const hwt_options *samples, const hwt_
 
     // 4. router calibration on the held-out samples with the fused network
     double answered = 1.0, max_ans = 0.0, p99_ans = 0.0, max_all = 0.0;
+    int64_t holdout_over = 0;
     s->route_tau = INFINITY;
     s->cal_valid = 0;
     if (nhold > 0) {
@@ -1392,8 +1394,10 @@ int hwt_surrogate_train(hwt_surrogate *s, const hwt_options *samples, const hwt_
             d.resize(nhold);
             for (int64_t j = 0; j < nhold; ++j) d[j] = kink_distance(rp, samples->strike[hold[j]] / Fh[hold[j]]);
         }
-        // routing that keeps every held-out answer within tol: (tau, delta), the
+        // routing that keeps the held-out answers within tol (all of them for the
+        // error head, all but kRouteBudget for the kink distance): (tau, delta), the
         // answered fraction and the largest and p99 errors of the answered samples
+        int64_t over = 0;  // answered held-out samples above the training tolerance
         auto calibrate = [&](double tol, double *tau, double *delta, double *ans, double *mx, double *p99) {
             *tau = INFINITY;
             *delta = -1.0;
@@ -1427,6 +1431,12 @@ int hwt_surrogate_train(hwt_surrogate *s, const hwt_options *samples, const hwt_
             }
         };
         calibrate(route_tol, &s->route_tau, &s->kink_delta, &answered, &max_ans, &p99_ans);
+        for (int64_t j = 0; j < nhold; ++j) {
+            const bool kept = s->route_tau == INFINITY ? (d.empty() || s->kink_delta < 0 || d[j] > s->kink_delta)
+                                                       : pred[j] <= s->route_tau;
+            if (kept && !(err[j] <= route_tol)) ++over;
+        }
+        holdout_over = over;
         for (int k = 0; k < kCalTols; ++k) {
             double mx, p99;
             calibrate(kCalTol[k], &s->cal_tau[k], &s->cal_delta[k], &s->cal_answered[k], &mx, &p99);
@@ -1449,6 +1459,7 @@ int hwt_surrogate_train(hwt_surrogate *s, const hwt_options *samples, const hwt_
         stats->holdout_p99_abs = p99_ans;
         stats->holdout_all_max_abs = max_all;
         stats->holdout = nhold;
+        stats->holdout_over = holdout_over;
         stats->n_kinks = (int64_t)s->kinks.size();
         stats->kink_delta = s->kink_delta;
         for (int k = 0; k < kCalTols; ++k) {
@@ -1470,7 +1481,7 @@ int hwt_surrogate_price(hwt_surrogate *s, const hwt_options *o, const hwt_yield 
     if (n == 0) return HWT_OK;
     int r;
     SCUDA(s, cudaEventRecord(s->ev[0], s->stream), "event");
-    if ((r = features_for(s, o, y))) return r;
+    if ((r = features_for(s, o, y, s->ev[4]))) return r;
     if (!s->out2.grow((size_t)n * kOut) || !s->price.grow(n) || !s->kind.grow(n) || !s->list.grow(n) ||
         !s->counts.grow(4) || !s->tree.grow(n) || !s->errs.grow(n) || !grow_batch(s->sub, n))
         return sfail(s, HWT_ENOMEM, "pricing buffers");
@@ -1574,8 +1585,9 @@ int hwt_surrogate_price(hwt_surrogate *s, const hwt_options *o, const hwt_yield 
         n_network = 0;
     }
     if (stats) {
-        float t0 = 0, t1 = 0, t2 = 0;
-        cudaEventElapsedTime(&t0, s->ev[0], s->ev[1]);
+        float t0 = 0, t1 = 0, t2 = 0, tc0 = 0;
+        cudaEventElapsedTime(&tc0, s->ev[0], s->ev[4]);
+        cudaEventElapsedTime(&t0, s->ev[4], s->ev[1]);
         cudaEventElapsedTime(&t1, s->ev[0], s->ev[3]);
         cudaEventElapsedTime(&t2, s->ev[1], s->ev[2]);
         stats->n_in_box = n - cnt[KIND_OUTSIDE];
@@ -1593,6 +1605,7 @@ int hwt_surrogate_price(hwt_surrogate *s, const hwt_options *o, const hwt_yield 
         }
         stats->fell_back = fell_back;
         stats->route_tolerance = route_tol;
+        stats->copy_ms = tc0;
         stats->network_ms = t0;
         stats->tree_ms = tree_ms + fallback_ms;
         stats->route_ms = t2;

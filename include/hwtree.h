@@ -283,6 +283,8 @@ typedef struct hwt_train_stats {
                                         (< 0: no kink routing) */
     double ladder_tolerance[7];      /* the routing also calibrated at these tolerances ... */
     double ladder_answered[7];       /* ... answering these fractions of the held-out samples */
+    int64_t holdout_over;            /* held-out samples the network answers above route_tolerance
+                                        (0 for the error head, at most 2 for the kink distance) */
 } hwt_train_stats;
 
 typedef struct hwt_surrogate_stats {
@@ -291,10 +293,14 @@ typedef struct hwt_surrogate_stats {
                                         priced the network's answers too */
     int32_t pad;
     double judge_max_abs, judge_p99_abs, judge_mean_abs; /* |network - tree| on the judged sample */
-    double network_ms, tree_ms, route_ms, total_ms;
+    double network_ms;               /* features, fused network and routing on the device */
+    double tree_ms;                  /* the tree's own pricing calls (routed, judged, fallback) */
+    double route_ms;                 /* from routing to the tree's answers scattered back */
+    double total_ms;                 /* the whole call on the stream, copies included */
     int64_t n_flagged;               /* in-box options the routing sent to the tree */
     int64_t n_network;               /* options answered by the network */
     double route_tolerance;          /* the ladder tolerance the call routed with (NaN: the training one) */
+    double copy_ms;                  /* host-to-device copy of the options */
 } hwt_surrogate_stats;
 
 typedef struct hwt_surrogate hwt_surrogate;
