@@ -528,7 +528,8 @@ class TrainConfig(ctypes.Structure):
     _fields_ = [("epochs", ctypes.c_int32), ("batch", ctypes.c_int32), ("lr", ctypes.c_double),
                 ("lr_min", ctypes.c_double), ("seed", ctypes.c_uint64), ("err_weight", ctypes.c_double),
                 ("route_tolerance", ctypes.c_double), ("holdout", ctypes.c_double),
-                ("kink_oversample", ctypes.c_int32), ("pad", ctypes.c_int32)]
+                ("kink_oversample", ctypes.c_int32), ("hard_every", ctypes.c_int32),
+                ("hard_fraction", ctypes.c_double)]
 
 
 class TrainStats(ctypes.Structure):
@@ -539,7 +540,8 @@ class TrainStats(ctypes.Structure):
                 ("holdout_p99_abs", ctypes.c_double), ("holdout_all_max_abs", ctypes.c_double),
                 ("holdout", ctypes.c_int64), ("n_kinks", ctypes.c_int64), ("kink_delta", ctypes.c_double),
                 ("ladder_tolerance", ctypes.c_double * 7), ("ladder_answered", ctypes.c_double * 7),
-                ("holdout_over", ctypes.c_int64)]
+                ("holdout_over", ctypes.c_int64), ("hard_minings", ctypes.c_int64),
+                ("hard_threshold_abs", ctypes.c_double)]
 
     def as_dict(self) -> dict:
         d = {name: getattr(self, name) for name, _ in self._fields_}
@@ -619,11 +621,15 @@ class Surrogate:
 
     def train(self, samples: Options, yield_: Yield, epochs: int = 1, batch: int = 8192, lr: float = 1e-3,
               lr_min: float = 0.0, seed: int = 7, err_weight: float = 0.0, route_tolerance: float = 1e-4,
-              holdout: float = 0.05, kink_oversample: int = 1) -> dict:
+              holdout: float = 0.05, kink_oversample: int = 1, hard_every: int = 0,
+              hard_fraction: float = 0.0) -> dict:
         """Labels the samples with the FP64 tree and trains; with err_weight > 0 the
         error head is trained too and routes (held-out calibration at route_tolerance);
-        on a single-tree box samples near a payoff kink can be repeated per epoch."""
-        cfg = TrainConfig(epochs, batch, lr, lr_min, seed, err_weight, route_tolerance, holdout, kink_oversample, 0)
+        on a single-tree box samples near a payoff kink can be repeated per epoch;
+        with hard_every > 0 the hard_fraction of training samples with the largest
+        errors is repeated per epoch (mined again every hard_every epochs)."""
+        cfg = TrainConfig(epochs, batch, lr, lr_min, seed, err_weight, route_tolerance, holdout, kink_oversample,
+                          hard_every, hard_fraction)
         o, y = samples._c(), yield_._c()
         self._check(lib().hwt_surrogate_train(self._s, ctypes.byref(o), ctypes.byref(y), ctypes.byref(cfg),
                                               ctypes.byref(self.train_stats)))

@@ -334,6 +334,17 @@ __global__ void targets_kernel(const double *price, const double *F, const doubl
     if (i < n) y[i] = (float)(((price[i] - base[i]) / F[i] - ymean) * yinv);
 }
 
+// Error of the network's price head against the target, in price units up to the
+// constant y_std: |o - y| F (hard-sample mining ranks the training samples by it).
+__global__ void sample_err_kernel(const float *out, const float *y, const double *F, int n, float *err)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        const float e = fabsf(out[2 * i] - y[i]) * (float)F[i];
+        err[i] = e == e ? e : INFINITY;
+    }
+}
+
 __device__ __forceinline__ unsigned long long mix64(unsigned long long x)
 {
     x += 0x9e3779b97f4a7c15ull;
@@ -355,7 +366,7 @@ enum Kind : uint8_t {
 // answers.  counts[k] = options of kind k (k = 1..3).
 __global__ void decode_route_kernel(const float *out, const double *F, const double *base, const uint8_t *inbox,
                                     const double *strike, int n, double ymean, double ystd, float log_tau_over_ystd,
-                                    const double *kinks, int n_kinks, double kink_delta, unsigned long long seed,
+                                    const double *points, const double *deltas, int n_points, unsigned long long seed,
                                     unsigned long long thresh, double *price, uint8_t *kind, int32_t *list,
                                     int32_t *counts)
 {
@@ -369,12 +380,11 @@ __global__ void decode_route_kernel(const float *out, const double *F, const dou
         price[i] = base[i] + F[i] * ((double)o.x * ystd + ymean);
         // predicted |price error| = exp(o1) ystd F > tau  <=>  o1 > log(tau / ystd) - log(F)
         bool flag = o.y > log_tau_over_ystd - logf((float)F[i]);
-        // a strike within kink_delta (moneyness) of a payoff kink of the box's tree
-        if (n_kinks > 0) {
+        // a strike within its own distance (moneyness) of a routing point of a
+        // single-tree box (a payoff kink of the box's tree or a box edge)
+        if (n_points > 0) {
             const double x = strike[i] / F[i];
-            double d = INFINITY;
-            for (int j = 0; j < n_kinks; ++j) d = fmin(d, fabs(x - kinks[j]));
-            flag = flag || d <= kink_delta;
+            for (int j = 0; j < n_points; ++j) flag = flag || fabs(x - points[j]) <= deltas[j];
         }
         if (flag) k = KIND_FLAGGED;
         else if (mix64(seed ^ (unsigned long long)i) < thresh) k = KIND_JUDGED;
@@ -524,10 +534,14 @@ struct hwt_surrogate {
     // Single-tree boxes: the payoff kinks of the box's tree in moneyness (from the
     // training labels) and the distance from them inside which options go to the tree
     std::vector<double> kinks;
+    // per routing point (the kinks, then the box's two moneyness edges): options
+    // within this distance of it go to the tree (< 0: none); kink_delta is the largest
+    std::vector<double> route_delta;
     double kink_delta = -1.0;     // < 0: no kink routing
     // The same routing calibrated at a ladder of tolerances (kCalTol): a call with a
-    // judge tolerance routes with the largest of them at most half that tolerance
+    // judge tolerance routes with the largest of them not above that tolerance
     double cal_tau[7], cal_delta[7], cal_answered[7];
+    std::vector<double> cal_deltas[7];
     int cal_valid = 0;
     Buf<double> dkinks;
     int trained = 0;
@@ -1124,7 +1138,6 @@ double calibrate_tau(const std::vector<double> &pred, const std::vector<double> 
 
 constexpr int kMaxKinks = 256;
 constexpr double kKinkBand = 0.005;  // moneyness: ~0.44 strike units around a kink of the book's tree
-constexpr int kRouteBudget = 2;  // held-out answers above the tolerance the kink distance may leave
 constexpr int kCalTols = 7;
 const double kCalTol[kCalTols] = {2.5e-5, 5e-5, 1e-4, 2e-4, 5e-4, 1e-3, 2e-3};
 
@@ -1179,6 +1192,30 @@ double kink_distance(const std::vector<double> &kinks, double x)
     double d = INFINITY;
     for (double k : kinks) d = std::min(d, fabs(x - k));
     return d;
+}
+
+// Index of the point nearest to x (points non-empty).
+int nearest_point(const std::vector<double> &pts, double x)
+{
+    int b = 0;
+    for (int k = 1; k < (int)pts.size(); ++k)
+        if (fabs(x - pts[k]) < fabs(x - pts[b])) b = k;
+    return b;
+}
+
+// x within its own routing distance of some point (the decode kernel's test).
+bool routed_near(const std::vector<double> &pts, const std::vector<double> &delta, double x)
+{
+    for (size_t k = 0; k < delta.size() && k < pts.size(); ++k)
+        if (fabs(x - pts[k]) <= delta[k]) return true;
+    return false;
+}
+
+double max_of(const std::vector<double> &v)
+{
+    double m = -1.0;
+    for (double x : v) m = std::max(m, x);
+    return m;
 }
 
 // The points the routing measures distance from on a single-tree box: the tree's
@@ -1250,6 +1287,8 @@ int hwt_surrogate_train(hwt_surrogate *s, const hwt_options *samples, const hwt_
     // single-tree box: the tree's payoff kinks from the training part's labels
     s->kinks.clear();
     s->kink_delta = -1.0;
+    s->route_delta.clear();
+    for (auto &v : s->cal_deltas) v.clear();
     if (single_tree_box(s->box)) {
         std::vector<double> k;
         for (int type = 0; type <= 1; ++type) {
@@ -1285,6 +1324,13 @@ int hwt_surrogate_train(hwt_surrogate *s, const hwt_options *samples, const hwt_
                 for (int q = 1; q < reps; ++q) tr.push_back(i);
         }
     }
+    // hard-sample mining: nh more slots per epoch, refilled every hard_every epochs
+    // (from the first quarter of the epochs on) with the training samples the network
+    // prices worst; random training samples until the first mining
+    const int hard_every = cfg->hard_every > 0 && cfg->hard_fraction > 0 ? cfg->hard_every : 0;
+    const int64_t nh = hard_every ? (int64_t)(std::min(cfg->hard_fraction, 0.25) * ntrain) : 0;
+    const std::vector<int32_t> tr0 = tr;
+    for (int64_t j = 0; j < nh; ++j) tr.push_back(idx[rnd() % (unsigned long long)ntrain]);
     const int64_t nlist = (int64_t)tr.size();
     const int64_t nbuf = std::max(nlist, nin);
 
@@ -1293,10 +1339,12 @@ int hwt_surrogate_train(hwt_surrogate *s, const hwt_options *samples, const hwt_
     double *dprice = nullptr;
     int32_t *perm = nullptr;
     StepState *dstate = nullptr;
+    float *derr = nullptr;
     bool ok = cudaMalloc(&yv, 4ull * n) == cudaSuccess && cudaMalloc(&Xs, 4ull * kInPad * nbuf) == cudaSuccess &&
               cudaMalloc(&ys, 4ull * nbuf) == cudaSuccess && cudaMalloc(&dprice, 8ull * n) == cudaSuccess &&
-              cudaMalloc(&perm, 4ull * nbuf) == cudaSuccess && cudaMalloc(&dstate, sizeof(StepState)) == cudaSuccess;
-    guard.ptrs = {yv, Xs, ys, dprice, perm, dstate};
+              cudaMalloc(&perm, 4ull * nbuf) == cudaSuccess && cudaMalloc(&dstate, sizeof(StepState)) == cudaSuccess &&
+              (nh == 0 || cudaMalloc(&derr, 4ull * n) == cudaSuccess);
+    guard.ptrs = {yv, Xs, ys, dprice, perm, dstate, derr};
     if (!ok) {
         cudaGetLastError();
         return sfail(s, HWT_ENOMEM, "training buffers");
@@ -1338,8 +1386,30 @@ int hwt_surrogate_train(hwt_surrogate *s, const hwt_options *samples, const hwt_
         SCUDA(s, ce2, "end capture");
     }
     SCUDA(s, cudaGraphInstantiate(&gexec, graph, 0), "instantiate training graph");
+    if (nh > 0 && !s->out2.grow((size_t)n * kOut)) return sfail(s, HWT_ENOMEM, "mining outputs");
+    std::vector<float> herr(nh > 0 ? n : 0);
+    std::vector<int32_t> cand;
+    int64_t minings = 0;
+    double hard_thr = 0.0;
+    const int first_mining = epochs / 4;
     SCUDA(s, cudaEventRecord(s->ev[0], s->stream), "event");
     for (int ep = 0; ep < epochs; ++ep) {
+        if (nh > 0 && ep >= first_mining && (ep - first_mining) % hard_every == 0) {
+            // price every sample with the current weights, keep the nh worst training samples
+            if ((r = forward_fused(s, s->xf.p, (int)n, s->out2.p))) return r;
+            sample_err_kernel<<<(int)((n + 255) / 256), 256, 0, s->stream>>>(s->out2.p, yv, s->F.p, (int)n, derr);
+            SCUDA(s, cudaGetLastError(), "sample error kernel");
+            SCUDA(s, cudaMemcpyAsync(herr.data(), derr, 4ull * n, cudaMemcpyDeviceToHost, s->stream), "errors D2H");
+            SCUDA(s, cudaStreamSynchronize(s->stream), "mining");
+            if ((r = gemm_status(s))) return r;
+            cand.assign(idx.begin(), idx.begin() + ntrain);
+            std::nth_element(cand.begin(), cand.begin() + (nh - 1), cand.end(),
+                             [&](int32_t a, int32_t b) { return herr[a] > herr[b]; });
+            hard_thr = (double)herr[cand[nh - 1]] * s->ystd;
+            tr.assign(tr0.begin(), tr0.end());
+            tr.insert(tr.end(), cand.begin(), cand.begin() + nh);
+            ++minings;
+        }
         for (int64_t i = nlist - 1; i > 0; --i) std::swap(tr[i], tr[rnd() % (unsigned long long)(i + 1)]);
         SCUDA(s, cudaMemcpyAsync(perm, tr.data(), 4ull * nlist, cudaMemcpyHostToDevice, s->stream), "perm H2D");
         gather_rows_kernel<<<(int)((nlist + 255) / 256), 256, 0, s->stream>>>(s->xf.p, yv, perm, (int)nlist, Xs, ys);
@@ -1389,36 +1459,37 @@ int hwt_surrogate_train(hwt_surrogate *s, const hwt_options *samples, const hwt_
             pred[j] = exp((double)o[2 * j + 1]) * s->ystd * Fh[i];
             max_all = std::max(max_all, err[j]);
         }
-        std::vector<double> d;
-        if (!s->kinks.empty()) {
-            d.resize(nhold);
-            for (int64_t j = 0; j < nhold; ++j) d[j] = kink_distance(rp, samples->strike[hold[j]] / Fh[hold[j]]);
+        // moneyness of the held-out samples on a single-tree box
+        std::vector<double> xm;
+        if (!rp.empty()) {
+            xm.resize(nhold);
+            for (int64_t j = 0; j < nhold; ++j) xm[j] = samples->strike[hold[j]] / Fh[hold[j]];
         }
-        // routing that keeps the held-out answers within tol (all of them for the
-        // error head, all but kRouteBudget for the kink distance): (tau, delta), the
-        // answered fraction and the largest and p99 errors of the answered samples
+        // routing that keeps every held-out answer within tol: the error head's
+        // threshold tau, or on a single-tree box a distance per routing point (each
+        // held-out answer above tol widens the distance of the point nearest to it
+        // to reach it, so a stray error far from the kinks costs the tree only the
+        // options around one point); the answered fraction and the largest and p99
+        // errors of the answered samples
         int64_t over = 0;  // answered held-out samples above the training tolerance
-        auto calibrate = [&](double tol, double *tau, double *delta, double *ans, double *mx, double *p99) {
+        auto calibrate = [&](double tol, double *tau, std::vector<double> *delta, double *ans, double *mx,
+                             double *p99) {
             *tau = INFINITY;
-            *delta = -1.0;
+            delta->clear();
             if (lam > 0) {
                 *tau = calibrate_tau(pred, err, tol, ans, mx, p99);
                 return;
             }
             std::vector<double> e;
-            if (!d.empty()) {
-                // the smallest distance from the kinks beyond which at most
-                // kRouteBudget held-out answers exceed the tolerance (one stray
-                // error far from every kink would otherwise send the box to the tree)
-                std::vector<double> bad;
+            if (!xm.empty()) {
+                delta->assign(rp.size(), -1.0);
                 for (int64_t j = 0; j < nhold; ++j)
-                    if (!(err[j] <= tol)) bad.push_back(d[j]);
-                std::sort(bad.begin(), bad.end(), std::greater<double>());
-                const size_t skip = std::min<size_t>(bad.size(), (size_t)kRouteBudget);
-                const double dl = bad.size() > skip ? bad[skip] : 0.0;
-                *delta = dl;
+                    if (!(err[j] <= tol)) {
+                        const int k = nearest_point(rp, xm[j]);
+                        (*delta)[k] = std::max((*delta)[k], fabs(xm[j] - rp[k]));
+                    }
                 for (int64_t j = 0; j < nhold; ++j)
-                    if (d[j] > dl) e.push_back(err[j]);
+                    if (!routed_near(rp, *delta, xm[j])) e.push_back(err[j]);
             } else {
                 e = err;
             }
@@ -1430,16 +1501,18 @@ int hwt_surrogate_train(hwt_surrogate *s, const hwt_options *samples, const hwt_
                 *p99 = e[std::min(e.size() - 1, (size_t)floor(0.99 * (e.size() - 1)))];
             }
         };
-        calibrate(route_tol, &s->route_tau, &s->kink_delta, &answered, &max_ans, &p99_ans);
+        calibrate(route_tol, &s->route_tau, &s->route_delta, &answered, &max_ans, &p99_ans);
+        s->kink_delta = max_of(s->route_delta);
         for (int64_t j = 0; j < nhold; ++j) {
-            const bool kept = s->route_tau == INFINITY ? (d.empty() || s->kink_delta < 0 || d[j] > s->kink_delta)
+            const bool kept = s->route_tau == INFINITY ? (xm.empty() || !routed_near(rp, s->route_delta, xm[j]))
                                                        : pred[j] <= s->route_tau;
             if (kept && !(err[j] <= route_tol)) ++over;
         }
         holdout_over = over;
         for (int k = 0; k < kCalTols; ++k) {
             double mx, p99;
-            calibrate(kCalTol[k], &s->cal_tau[k], &s->cal_delta[k], &s->cal_answered[k], &mx, &p99);
+            calibrate(kCalTol[k], &s->cal_tau[k], &s->cal_deltas[k], &s->cal_answered[k], &mx, &p99);
+            s->cal_delta[k] = max_of(s->cal_deltas[k]);
         }
         s->cal_valid = 1;
     }
@@ -1460,6 +1533,8 @@ int hwt_surrogate_train(hwt_surrogate *s, const hwt_options *samples, const hwt_
         stats->holdout_all_max_abs = max_all;
         stats->holdout = nhold;
         stats->holdout_over = holdout_over;
+        stats->hard_minings = minings;
+        stats->hard_threshold_abs = hard_thr;
         stats->n_kinks = (int64_t)s->kinks.size();
         stats->kink_delta = s->kink_delta;
         for (int k = 0; k < kCalTols; ++k) {
@@ -1492,26 +1567,29 @@ int hwt_surrogate_price(hwt_surrogate *s, const hwt_options *o, const hwt_yield 
     const unsigned long long thresh = jf >= 1.0 ? ~0ull : (unsigned long long)(jf * 18446744073709551616.0);
     // routing: the training tolerance's calibration, or, with a judge tolerance, the
     // ladder's largest tolerance not above it (the strictest if none is)
-    double tau = s->route_tau, delta = s->kink_delta, route_tol = NAN;
+    double tau = s->route_tau, route_tol = NAN;
+    const std::vector<double> *delta = &s->route_delta;
     if (judge_tolerance > 0 && s->cal_valid) {
         int k = 0;
         for (int q = 0; q < kCalTols; ++q)
             if (kCalTol[q] <= judge_tolerance * (1.0 + 1e-12)) k = q;
         tau = s->cal_tau[k];
-        delta = s->cal_delta[k];
+        delta = &s->cal_deltas[k];
         route_tol = kCalTol[k];
     }
     // flag when exp(o1) ystd F > tau; tau = +inf: the router is off, tau <= 0: nothing is answered
     const float log_tau = std::isinf(tau) ? INFINITY : (tau > 0 ? (float)log(tau / s->ystd) : -INFINITY);
     const std::vector<double> rp = route_points(s);
-    const int nk = delta >= 0 ? (int)rp.size() : 0;
+    const int nk = delta->size() == rp.size() ? (int)rp.size() : 0;
     if (nk > 0) {
-        if (!s->dkinks.grow(kMaxKinks + 2)) return sfail(s, HWT_ENOMEM, "kink buffer");
+        if (!s->dkinks.grow(2 * (kMaxKinks + 2))) return sfail(s, HWT_ENOMEM, "kink buffer");
         SCUDA(s, cudaMemcpyAsync(s->dkinks.p, rp.data(), 8ull * nk, cudaMemcpyHostToDevice, s->stream), "kinks H2D");
+        SCUDA(s, cudaMemcpyAsync(s->dkinks.p + nk, delta->data(), 8ull * nk, cudaMemcpyHostToDevice, s->stream),
+              "distances H2D");
     }
     decode_route_kernel<<<(n + 255) / 256, 256, 0, s->stream>>>(s->out2.p, s->F.p, s->base.p, s->inbox.p,
                                                                s->opts.strike, n, s->ymean, s->ystd, log_tau,
-                                                               s->dkinks.p, nk, delta, seed, thresh,
+                                                               s->dkinks.p, s->dkinks.p + nk, nk, seed, thresh,
                                                                s->price.p, s->kind.p, s->list.p, s->counts.p);
     SCUDA(s, cudaGetLastError(), "decode kernel");
     SCUDA(s, cudaEventRecord(s->ev[1], s->stream), "event");
@@ -1624,16 +1702,22 @@ int hwt_surrogate_save(const hwt_surrogate *s, const char *path)
         return HWT_ECUDA;
     FILE *f = fopen(path, "wb");
     if (!f) return HWT_EINVAL;
-    const uint32_t magic = 0x48575453u, version = 4;
+    const uint32_t magic = 0x48575453u, version = 5;
     const uint64_t np = s->n_params, nk = s->kinks.size();
     const int64_t t = s->adam_t;
+    // per-point routing distances: the training tolerance's, then the ladder's
+    auto put_deltas = [&](const std::vector<double> &d) {
+        const uint64_t c = d.size();
+        return fwrite(&c, 8, 1, f) == 1 && (c == 0 || fwrite(d.data(), 8, c, f) == c);
+    };
     bool ok = fwrite(&magic, 4, 1, f) == 1 && fwrite(&version, 4, 1, f) == 1 && fwrite(&s->box, sizeof(hwt_box), 1, f) == 1 &&
               fwrite(&s->ymean, 8, 1, f) == 1 && fwrite(&s->ystd, 8, 1, f) == 1 && fwrite(&s->route_tau, 8, 1, f) == 1 &&
               fwrite(&s->kink_delta, 8, 1, f) == 1 && fwrite(&nk, 8, 1, f) == 1 &&
               (nk == 0 || fwrite(s->kinks.data(), 8, nk, f) == nk) && fwrite(&s->cal_valid, 4, 1, f) == 1 &&
               fwrite(s->cal_tau, 8, kCalTols, f) == kCalTols && fwrite(s->cal_delta, 8, kCalTols, f) == kCalTols &&
-              fwrite(s->cal_answered, 8, kCalTols, f) == kCalTols &&
-              fwrite(&t, 8, 1, f) == 1 && fwrite(&np, 8, 1, f) == 1 && fwrite(w.data(), 4, np, f) == np &&
+              fwrite(s->cal_answered, 8, kCalTols, f) == kCalTols && put_deltas(s->route_delta);
+    for (int k = 0; k < kCalTols; ++k) ok = ok && put_deltas(s->cal_deltas[k]);
+    ok = ok && fwrite(&t, 8, 1, f) == 1 && fwrite(&np, 8, 1, f) == 1 && fwrite(w.data(), 4, np, f) == np &&
               fwrite(m.data(), 4, np, f) == np && fwrite(v.data(), 4, np, f) == np;
     fclose(f);
     return ok ? HWT_OK : HWT_EINVAL;
@@ -1653,7 +1737,7 @@ int hwt_surrogate_load(hwt_surrogate *s, const char *path)
     std::vector<double> kinks;
     int cal_valid = 0;
     double cal_tau[kCalTols], cal_delta[kCalTols], cal_answered[kCalTols];
-    bool ok = fread(&magic, 4, 1, f) == 1 && fread(&version, 4, 1, f) == 1 && magic == 0x48575453u && version == 4 &&
+    bool ok = fread(&magic, 4, 1, f) == 1 && fread(&version, 4, 1, f) == 1 && magic == 0x48575453u && version == 5 &&
               fread(&box, sizeof(hwt_box), 1, f) == 1 && fread(&ym, 8, 1, f) == 1 && fread(&ysd, 8, 1, f) == 1 &&
               fread(&tau, 8, 1, f) == 1 && fread(&kd, 8, 1, f) == 1 && fread(&nk, 8, 1, f) == 1 && nk <= (uint64_t)kMaxKinks;
     if (ok && nk) {
@@ -1662,6 +1746,15 @@ int hwt_surrogate_load(hwt_surrogate *s, const char *path)
     }
     ok = ok && fread(&cal_valid, 4, 1, f) == 1 && fread(cal_tau, 8, kCalTols, f) == kCalTols &&
          fread(cal_delta, 8, kCalTols, f) == kCalTols && fread(cal_answered, 8, kCalTols, f) == kCalTols;
+    auto get_deltas = [&](std::vector<double> &d) {
+        uint64_t c = 0;
+        if (fread(&c, 8, 1, f) != 1 || c > (uint64_t)kMaxKinks + 2) return false;
+        d.resize(c);
+        return c == 0 || fread(d.data(), 8, c, f) == c;
+    };
+    std::vector<double> rdelta, cdeltas[kCalTols];
+    ok = ok && get_deltas(rdelta);
+    for (int k = 0; k < kCalTols; ++k) ok = ok && get_deltas(cdeltas[k]);
     ok = ok && fread(&t, 8, 1, f) == 1 && fread(&np, 8, 1, f) == 1 && np == s->n_params;
     std::vector<float> w(s->n_params), m(s->n_params), v(s->n_params);
     ok = ok && fread(w.data(), 4, np, f) == np && fread(m.data(), 4, np, f) == np && fread(v.data(), 4, np, f) == np;
@@ -1674,6 +1767,8 @@ int hwt_surrogate_load(hwt_surrogate *s, const char *path)
     s->route_tau = tau;
     s->kink_delta = kd;
     s->kinks = kinks;
+    s->route_delta = rdelta;
+    for (int k = 0; k < kCalTols; ++k) s->cal_deltas[k] = cdeltas[k];
     s->cal_valid = cal_valid;
     memcpy(s->cal_tau, cal_tau, sizeof(cal_tau));
     memcpy(s->cal_delta, cal_delta, sizeof(cal_delta));

@@ -257,13 +257,17 @@ typedef struct hwt_train_config {
     double err_weight;               /* weight of the error head's loss; 0: head untrained, no routing */
     double route_tolerance;          /* price error (per 100 face) that the network's answers must keep
                                         on the held-out samples; sets the routing threshold of the error
-                                        head (every held-out answer within it) or, on a single-tree box,
-                                        the kink distance (all but at most 2 held-out answers within it)
-                                        (default 1e-4) */
+                                        head or, on a single-tree box, a routing distance around each
+                                        payoff kink and box edge, so that every held-out answer the
+                                        network keeps is within it (default 1e-4) */
     double holdout;                  /* fraction of in-box samples held out for that (default 0.05) */
     int32_t kink_oversample;         /* single-tree box: samples within 0.005 in moneyness of a payoff
                                         kink appear this many times per epoch (1 or 0: once) */
-    int32_t pad;
+    int32_t hard_every;              /* hard-sample mining: every this many epochs (0: off), from the
+                                        first quarter of the epochs on, the network prices every training
+                                        sample and ... */
+    double hard_fraction;            /* ... this fraction of them, those with the largest errors, is
+                                        repeated once more per epoch until the next mining (max 0.25) */
 } hwt_train_config;
 
 typedef struct hwt_train_stats {
@@ -279,12 +283,15 @@ typedef struct hwt_train_stats {
     double holdout_all_max_abs;      /* |network - tree| over all held-out samples */
     int64_t holdout;                 /* held-out samples */
     int64_t n_kinks;                 /* single-tree box: payoff kinks found in the labels */
-    double kink_delta;               /* options closer than this (moneyness) to a kink go to the tree
+    double kink_delta;               /* the largest routing distance (moneyness) around a kink or box
+                                        edge; options within a point's own distance go to the tree
                                         (< 0: no kink routing) */
     double ladder_tolerance[7];      /* the routing also calibrated at these tolerances ... */
     double ladder_answered[7];       /* ... answering these fractions of the held-out samples */
     int64_t holdout_over;            /* held-out samples the network answers above route_tolerance
-                                        (0 for the error head, at most 2 for the kink distance) */
+                                        (0 by construction) */
+    int64_t hard_minings;            /* hard-sample minings run */
+    double hard_threshold_abs;       /* smallest price error in the last mined set */
 } hwt_train_stats;
 
 typedef struct hwt_surrogate_stats {

@@ -185,11 +185,14 @@ def test_kink_routing_on_the_single_tree_box(pkg, pricer, orc):
     y = pkg.Yield(rates, days)
     s = pkg.Surrogate(pricer, box=wl.single_tree_box(), seed=4)
     train = pkg.Options.from_batch(wl.single_tree_training_batch(200_000, seed=31))
-    st = s.train(train, y, epochs=4, batch=8192, lr=1e-3, route_tolerance=2e-3, holdout=0.1)
+    st = s.train(train, y, epochs=4, batch=8192, lr=1e-3, route_tolerance=2e-3, holdout=0.1, hard_every=2,
+                 hard_fraction=0.05)
     # the book's tree (t = 5 y, T = 10 y, 12 steps/year) has 12 kinks between strikes 75 and 95
     assert st["n_kinks"] == 12, st["n_kinks"]
-    # every held-out answer within the tolerance but at most two (the routing's budget)
-    assert st["kink_delta"] >= 0.0 and st["holdout_over"] <= 2
+    # hard-sample mining from the first quarter of the epochs on, every second epoch
+    assert st["hard_minings"] == 2 and st["hard_threshold_abs"] > 0.0
+    # every held-out answer the network keeps is within the tolerance
+    assert st["kink_delta"] >= 0.0 and st["holdout_over"] == 0 and st["holdout_max_abs"] <= 2e-3
     # kinks are where the oracle's price changes slope
     q = wl.single_tree_query_batch(20_000, seed=33)
     opts = pkg.Options.from_batch(q)
@@ -207,6 +210,11 @@ def test_kink_routing_on_the_single_tree_box(pkg, pricer, orc):
         s2.load(os.path.join(d, "k.bin"))
     got2 = s2.price(opts, y, judge_fraction=0.02, seed=3, tree_mode=pkg.BATCHED_FP64)
     assert np.array_equal(got, got2) and s2.stats.as_dict()["n_flagged"] == stats["n_flagged"]
+    # and the per-point distances of the tolerance ladder
+    for tol in (5e-4, 2e-3):
+        a = s.price(opts, y, judge_fraction=0.0, seed=3, tree_mode=pkg.BATCHED_FP64, judge_tolerance=tol)
+        b = s2.price(opts, y, judge_fraction=0.0, seed=3, tree_mode=pkg.BATCHED_FP64, judge_tolerance=tol)
+        assert np.array_equal(a, b)
     s.close()
     s2.close()
 
