@@ -609,7 +609,8 @@ struct Slice {
     // applied after the in-place step from old values saved before it, through a
     // switch on ts.  Warp tasks group trees by ts (it is part of the warp class),
     // which keeps the switch uniform across the warp.
-    R jlo, jhi;             // FP64: jump coefficient times the receiving node's G; flux: pu_b, pd_c
+    R jlo, jhi;             // FP64: jump coefficient times the receiving node's G; flux: pu_b, pd_c (1 + g_{W-1})
+    R jg3;                  // flux: pd_c (1 + g_{W-3}), the top jump discounted at the node it lands on
     bool n0, n2, nw1, nw3;  // this thread owns node 0 / 2 / W-1 / W-3 of an edged tree
     int ts;
 
@@ -629,7 +630,7 @@ struct Slice {
     {
         const int W = t.width, jc = t.jc, jmax = t.jmax;
         setup_owners(t, k0);
-        jlo = jhi = (R)0;
+        jlo = jhi = jg3 = (R)0;
         if constexpr (!Mode::kFlux) {
 #pragma unroll
             for (int s = 0; s < K; ++s) {
@@ -697,7 +698,12 @@ struct Slice {
             if (t.edges) {
                 const float xb = (float)(-jmax) * Mf, xt = (float)jmax * Mf;
                 jlo = 1.0f / 6.0f + (xb * xb - xb) * 0.5f;  // pu_b: bottom edge jumps up two
-                jhi = 1.0f / 6.0f + (xt * xt + xt) * 0.5f;  // pd_c: top edge jumps down two
+                // pd_c (top edge jumps down two), times the discount 1 + g of the node it
+                // leaves (W-1) and of the node it reaches (W-3): the top-edge terms are
+                // added to the discounted row, one fused multiply-add each
+                const float pdc = 1.0f / 6.0f + (xt * xt + xt) * 0.5f;
+                jhi = fmaf(pdc, expm1f(-(float)jmax * drdt), pdc);
+                jg3 = fmaf(pdc, expm1f(-(float)(jmax - 2) * drdt), pdc);
             }
         }
     }
@@ -774,13 +780,11 @@ struct Slice {
         }
     }
 
-    // Adds c to the step's pre-discount value at slot S: the row holds
-    // (1+g) v (flux) or the finished value (FP64, c already carries G).
+    // Adds c to the finished value at slot S (gather-form rows: c already carries G).
     template <int S>
     __device__ __forceinline__ void add_at(R c)
     {
-        if constexpr (Mode::kFlux) r[S] += fma(c2[S], c, c);
-        else r[S] += c;
+        r[S] += c;
     }
 
     template <int TS, bool FWD>
@@ -788,17 +792,18 @@ struct Slice {
     {
         if constexpr (kTopSlot<TS>) {
             constexpr int S3 = (TS + 2 * K - 2) % K;
-            if constexpr (FWD) {
-                if constexpr (Mode::kFlux) {
-                    if (nw1) add_at<TS>(-jhi * w1);
+            if constexpr (Mode::kFlux) {
+                // the discounts are in jhi and jg3
+                if constexpr (FWD) {
+                    if (nw1) r[TS] = fma(-jhi, w1, r[TS]);
+                    if (nw3) r[S3] = fma(jg3, w1b, r[S3]);
+                } else {
+                    if (nw1) r[TS] = fma(jhi, w3 - w1, r[TS]);
                 }
+            } else if constexpr (FWD) {
                 if (nw3) add_at<S3>(jhi * w1b);
             } else {
-                if constexpr (Mode::kFlux) {
-                    if (nw1) add_at<TS>(jhi * (w3 - w1));
-                } else {
-                    if (nw1) add_at<TS>(jhi * w3);
-                }
+                if (nw1) add_at<TS>(jhi * w3);
             }
         }
     }
@@ -963,14 +968,14 @@ struct Slice {
             for (int q = 0; q < H; ++q) {
                 const float2 d = (q == H - 1) ? d_last : __ffma2_rn(r.v[q], m1, r.v[q + 1]);
                 const float2 nd = (q == 0) ? make_float2(cd0, c1.pair(H - 1).x) : c1.pair(q - 1);
-                float2 v = __fadd2_rn(r.v[q], __ffma2_rn(c0.pair(q), d, __fmul2_rn(nd, dp)));
+                float2 v = __ffma2_rn(nd, dp, __ffma2_rn(c0.pair(q), d, r.v[q]));
                 if (edge_live && q == 0) v.x = fma(j0, o2 - r.v[0].x, v.x);
                 r.v[q] = __ffma2_rn(c2.pair(q), __fadd2_rn(v, b2), v);
                 dp = d;
             }
         } else {
             // differences D_k = r_{k+1} - r_k, each computed once:
-            // v_k = r_k + up_k D_k - down_k D_{k-1}
+            // v_k = r_k + up_k D_k - down_k D_{k-1}, as two fused multiply-adds
             R dprev = r[0] - prev;
 #pragma unroll
             for (int s = 0; s < K; ++s) {
@@ -978,7 +983,7 @@ struct Slice {
                 const R nxt = (s < K - 1) ? r[s + 1] : h.r1;
                 const R d = nxt - cur;
                 const R ndown = (s == 0) ? cd0 : c1[s - 1];  // -down of this node
-                R v = cur + fma(c0[s], d, ndown * dprev);
+                R v = fma(ndown, dprev, fma(c0[s], d, cur));
                 if (s == 0) v = fma(j0, o2 - cur, v);
                 r[s] = fma(c2[s], v + base, v);
                 dprev = d;
