@@ -346,7 +346,7 @@ def surrogate_run(pkg, pricer, y, box, train, queries, epochs: int, reps: int, b
     sur = pkg.Surrogate(pricer, box=box, seed=1)
     t0 = time.perf_counter()
     tstats = sur.train(pkg.Options.from_batch(train), y, epochs=epochs, batch=8192, lr=2e-3, lr_min=2e-6,
-                       route_tolerance=1e-4, holdout=0.05, kink_oversample=kink_oversample)
+                       route_tolerance=1e-4, holdout=0.1, kink_oversample=kink_oversample)
     train_s = time.perf_counter() - t0
     qo = pkg.Options.from_batch(queries)
     trees = {}

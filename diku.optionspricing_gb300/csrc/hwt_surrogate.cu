@@ -53,14 +53,18 @@ struct FeatureNorm {
 
 // Hull-White closed-form price of a European option on a zero-coupon bond
 // (Jamshidian 1989) with face 100: the control variate of the residual network.
-__device__ double hw_closed_form(double t, double T, double X, double a, double sigma, double Pt, double PT, int type)
+// In terms of the forward bond price fwd = 100 P(T) / P(t) and the moneyness
+// mny = X / fwd: bond = fwd P(t), strike = X P(t), log(bond / strike) = -log(mny)
+// (no divisions beyond 1 / a: the FP64 pipe is this kernel's bound).
+__device__ double hw_closed_form(double t, double T, double X, double a, double sigma, double Pt, double fwd,
+                                 double mny, int type)
 {
-    const double B = -expm1(-a * (T - t)) / a;
-    const double sp = sigma * B * sqrt(-expm1(-2.0 * a * t) / (2.0 * a));
-    const double bond = 100.0 * PT, strike = X * Pt;
-    if (!(sp > 1e-12)) return type == 1 ? fmax(strike - bond, 0.0) : fmax(bond - strike, 0.0);
-    const double h = log(bond / strike) / sp + 0.5 * sp;
-    return type == 1 ? strike * normcdf(-h + sp) - bond * normcdf(-h) : bond * normcdf(h) - strike * normcdf(h - sp);
+    const double ia = 1.0 / a;
+    const double B = -expm1(-a * (T - t)) * ia;
+    const double sp = sigma * B * sqrt(-expm1(-2.0 * a * t) * (0.5 * ia));
+    if (!(sp > 1e-12)) return Pt * (type == 1 ? fmax(X - fwd, 0.0) : fmax(fwd - X, 0.0));
+    const double h = -log(mny) / sp + 0.5 * sp;
+    return Pt * (type == 1 ? X * normcdf(-h + sp) - fwd * normcdf(-h) : fwd * normcdf(h) - X * normcdf(h - sp));
 }
 
 // fp32 features, forward bond price, control-variate price and in-box flag of each option.
@@ -71,28 +75,34 @@ __global__ void features_kernel(DevOptions o, DevYield yc, hwt_box box, FeatureN
     if (i >= o.n) return;
     const double t = o.option_maturity[i], T = o.bond_maturity[i];
     const int tu = o.term_unit[i];
-    const double Pt = exp(-yield_at_year<double>(t, tu, yc.rate, yc.day, yc.n) * t);
-    const double PT = exp(-yield_at_year<double>(T, tu, yc.rate, yc.day, yc.n) * T);
-    const double fwd = 100.0 * PT / Pt;
+    const double rtt = yield_at_year<double>(t, tu, yc.rate, yc.day, yc.n) * t;
+    const double rTT = yield_at_year<double>(T, tu, yc.rate, yc.day, yc.n) * T;
+    const double Pt = exp(-rtt);
+    const double fwd = 100.0 * exp(rtt - rTT);  // 100 P(T) / P(t)
     const double mny = o.strike[i] / fwd;
     const double a = o.a[i], sg = o.sigma[i];
     const int steps = o.term_steps[i];
-    const double v[kIn] = {t, T, mny, a, sg, (double)steps, (double)o.type[i]};
+    // moneyness standardised in double (the price moves with it at about the forward
+    // price per unit); the other features are exact or smooth, standardised in float
+    const float v[kIn] = {(float)t, (float)T, 0.f, (float)a, (float)sg, (float)steps, (float)o.type[i]};
     float x[kInPad];
 #pragma unroll
-    for (int q = 0; q < kIn; ++q) x[q] = (float)((v[q] - fn.mean[q]) * fn.inv_std[q]);
+    for (int q = 0; q < kIn; ++q) x[q] = (v[q] - (float)fn.mean[q]) * (float)fn.inv_std[q];
+    x[2] = (float)((mny - fn.mean[2]) * fn.inv_std[2]);
     x[kIn] = 0.f;
     float4 *xr = reinterpret_cast<float4 *>(X + (size_t)i * kInPad);
     xr[0] = make_float4(x[0], x[1], x[2], x[3]);
     xr[1] = make_float4(x[4], x[5], x[6], x[7]);
     F[i] = fwd;
-    base[i] = box.residual ? hw_closed_form(t, T, o.strike[i], a, sg, Pt, PT, o.type[i]) : 0.0;
     const double span = T - t;
     const bool in = t >= box.t_min && t <= box.t_max && span >= box.span_min && span <= box.span_max &&
                     mny >= box.moneyness_min && mny <= box.moneyness_max && a >= box.a_min && a <= box.a_max &&
                     sg >= box.sigma_min && sg <= box.sigma_max && steps >= box.steps_min && steps <= box.steps_max &&
                     tu == box.term_unit && (o.type[i] == 0 || o.type[i] == 1) && isfinite(mny);
     inbox[i] = in ? 1 : 0;
+    // the control variate only where the network answers (the FP64 closed form is
+    // most of this kernel's time)
+    base[i] = (box.residual && in) ? hw_closed_form(t, T, o.strike[i], a, sg, Pt, fwd, mny, o.type[i]) : 0.0;
 }
 
 // Layer 0 of the training path: Z0 = X W0 + b0 (fp32) and layer 1's input H1 =
@@ -371,9 +381,10 @@ __global__ void decode_route_kernel(const float *out, const double *F, const dou
                                     int32_t *counts)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    const bool valid = i < n;  // no early return: the whole warp takes part in the append below
     uint8_t k = KIND_NETWORK;
-    if (!inbox[i]) {
+    if (!valid) {
+    } else if (!inbox[i]) {
         k = KIND_OUTSIDE;
     } else {
         const float2 o = reinterpret_cast<const float2 *>(out)[i];
@@ -389,10 +400,22 @@ __global__ void decode_route_kernel(const float *out, const double *F, const dou
         if (flag) k = KIND_FLAGGED;
         else if (mix64(seed ^ (unsigned long long)i) < thresh) k = KIND_JUDGED;
     }
-    kind[i] = k;
-    if (k != KIND_NETWORK) {
-        list[atomicAdd(counts, 1)] = i;
-        atomicAdd(counts + k, 1);
+    if (valid) kind[i] = k;
+    // warp-aggregated append to the tree's list: one atomic per warp, and one per
+    // kind present (a batch that routes most options would otherwise serialise on
+    // the two counters)
+    const bool app = valid && k != KIND_NETWORK;
+    const unsigned m = __ballot_sync(0xffffffffu, app);
+    if (m != 0u) {
+        const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+        int at = 0;
+        if (lane == leader) at = atomicAdd(counts, __popc(m));
+        at = __shfl_sync(0xffffffffu, at, leader);
+        if (app) list[at + __popc(m & ((1u << lane) - 1u))] = i;
+        for (int kk = KIND_OUTSIDE; kk <= KIND_FLAGGED; ++kk) {
+            const unsigned mk = __ballot_sync(0xffffffffu, app && k == kk);
+            if (mk != 0u && lane == __ffs(mk) - 1) atomicAdd(counts + kk, __popc(mk));
+        }
     }
 }
 

