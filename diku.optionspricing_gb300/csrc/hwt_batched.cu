@@ -611,7 +611,7 @@ struct Slice {
     // which keeps the switch uniform across the warp.
     R jlo, jhi;             // FP64: jump coefficient times the receiving node's G; flux: pu_b, pd_c (1 + g_{W-1})
     R jg3;                  // flux: pd_c (1 + g_{W-3}), the top jump discounted at the node it lands on
-    bool n0, n2, nw1, nw3;  // this thread owns node 0 / 2 / W-1 / W-3 of an edged tree
+    bool n0, n1, n2, nw1, nw3;  // this thread owns node 0 / 1 / 2 / W-1 / W-3 of an edged tree
     int ts;
 
     __device__ __forceinline__ void setup_owners(const Tree &t, int k0)
@@ -619,6 +619,7 @@ struct Slice {
         const int W = t.width;
         const bool e = t.edges != 0;
         n0 = e && k0 == 0;
+        n1 = e && k0 <= 1 && 1 < k0 + K;
         n2 = e && k0 <= 2 && 2 < k0 + K;
         nw1 = e && k0 <= W - 1 && W - 1 < k0 + K;
         nw3 = e && k0 <= W - 3 && W - 3 < k0 + K;
@@ -661,7 +662,10 @@ struct Slice {
                     const float x = (float)j * Mf, x2 = x * x;
                     g = expm1f(-(float)j * drdt);
                     if (j == -jmax) {
-                        u = -1.0f / 3.0f - x2 + 2.0f * x;   // pm_b
+                        // pm_b, plus pu_b on an edged tree: node 0's jump up two crosses
+                        // this link and the next one (the step adds it to the next)
+                        u = -1.0f / 3.0f - x2 + 2.0f * x;
+                        if (t.edges) u += 1.0f / 6.0f + (x2 - x) * 0.5f;
                         d = 0.f;
                     } else if (j == jmax) {
                         u = 0.f;
@@ -683,6 +687,7 @@ struct Slice {
                     const int j = kl - jc;
                     const float x = (float)j * Mf, x2 = x * x;
                     cl = (j == -jmax) ? (-1.0f / 3.0f - x2 + 2.0f * x) : (j == jmax ? 0.f : 1.0f / 6.0f + (x2 + x) * 0.5f);
+                    if (j == -jmax && t.edges) cl += 1.0f / 6.0f + (x2 - x) * 0.5f;
                 }
                 if (kr < W) {
                     const int j = kr - jc;
@@ -848,10 +853,11 @@ struct Slice {
     {
         constexpr int S2 = 2 % K;  // slot of node 2
         R w1 = (R)0, w3 = (R)0, w1b = (R)0;
-        // bottom-edge jump weights of this thread's nodes 0 and 2 (zero elsewhere)
-        const R jout = (edge_live && n0) ? jlo : (R)0;
+        // bottom-edge jump: gather rows add it at node 2 (its weight jin, zero on other
+        // threads); flux rows carry it on link 1, owned by node 1's thread (jl1)
         const R jin = (edge_live && n2) ? jlo : (R)0;
         const R src2 = old_at<S2, -2>(h);  // node 0 seen from node 2 (read before the update)
+        const R jl1 = n1 ? jlo : (R)0;
         if (TOP && edge_live) top_values(h, w1, w3, w1b);
         if constexpr (!Mode::kFlux && Nodes<R, K>::kPaired) {
             // double-float rows on pairs (node q, node q+H): the compensated products
@@ -885,37 +891,41 @@ struct Slice {
             // the same operations on pairs (node p, node p+H); a - b as fma(b, -1, a)
             // rounds as the subtraction, so the results are the unpaired ones
             constexpr int H = K / 2;
+            constexpr int S1 = 1 % K, Q1 = S1 % H;  // node 1's slot and pair
             const float2 m1 = make_float2(-1.f, -1.f);
+            // bottom edge: node 0's jump up two rides on links 0 (its coefficient) and
+            // 1 (this term, node 0's old value, added to link 1's flux)
+            const float jq = edge_live ? jl1 * old_at<S1, -1>(h) : 0.f;
+            const float2 jadd = (S1 >= H) ? make_float2(0.f, jq) : make_float2(jq, 0.f);
             // pair H-1's right neighbours are node H (pair 0's second) and the halo
-            const float2 e_last =
-                __ffma2_rn(c0.pair(H - 1), r.v[H - 1], __fmul2_rn(c1.pair(H - 1), make_float2(r.v[0].y, h.r1)));
+            const float2 nl = make_float2(r.v[0].y, h.r1);
+            const float2 e_last = __ffma2_rn(c0.pair(H - 1), r.v[H - 1],
+                                             (edge_live && Q1 == H - 1) ? __ffma2_rn(c1.pair(H - 1), nl, jadd)
+                                                                        : __fmul2_rn(c1.pair(H - 1), nl));
             float2 ep = make_float2(fma(cl, h.l1, cd0 * r[0]), e_last.x);  // links k0-1 and k0+H-1
 #pragma unroll
             for (int q = 0; q < H; ++q) {
-                const float2 e = (q == H - 1) ? e_last : __ffma2_rn(c0.pair(q), r.v[q], __fmul2_rn(c1.pair(q), r.v[q + 1]));
-                float2 v = __fadd2_rn(r.v[q], __ffma2_rn(e, m1, ep));
-                if (edge_live) {  // a constant in the step loops: no dead fix-ups
-                    if (q == 0) v.x = fma(-jout, r.v[0].x, v.x);
-                    if (q == S2 % H) {
-                        if (S2 < H) v.x = fma(jin, src2, v.x);
-                        else v.y = fma(jin, src2, v.y);
-                    }
-                }
+                const float2 e =
+                    (q == H - 1) ? e_last
+                                 : __ffma2_rn(c0.pair(q), r.v[q],
+                                              (edge_live && q == Q1) ? __ffma2_rn(c1.pair(q), r.v[q + 1], jadd)
+                                                                     : __fmul2_rn(c1.pair(q), r.v[q + 1]));
+                const float2 v = __fadd2_rn(r.v[q], __ffma2_rn(e, m1, ep));
                 r.v[q] = __ffma2_rn(c2.pair(q), v, v);
                 ep = e;
             }
         } else {
             // net flux e_k = up_k r_k - down_{k+1} r_{k+1} across each link, computed
             // once and used by both ends (the row's sum is kept exactly)
+            constexpr int S1 = 1 % K;  // node 1's slot
+            const R jq = edge_live ? jl1 * old_at<S1, -1>(h) : (R)0;  // node 0's jump, on link 1
             R eprev = fma(cl, h.l1, cd0 * r[0]);
 #pragma unroll
             for (int s = 0; s < K; ++s) {
                 const R cur = r[s];
                 const R nxt = (s < K - 1) ? r[s + 1] : h.r1;
-                const R e = fma(c0[s], cur, c1[s] * nxt);
-                R v = cur + (eprev - e);
-                if (s == 0) v = fma(-jout, cur, v);
-                if (s == S2) v = fma(jin, src2, v);
+                const R e = fma(c0[s], cur, (edge_live && s == S1) ? fma(c1[s], nxt, jq) : c1[s] * nxt);
+                const R v = cur + (eprev - e);
                 r[s] = fma(c2[s], v, v);
                 eprev = e;
             }
@@ -930,6 +940,7 @@ struct Slice {
         R w1 = (R)0, w3 = (R)0, w1b = (R)0;
         const R j0 = (edge_live && n0) ? jlo : (R)0;  // bottom-edge jump weight of node 0
         const R o2 = old_at<0, 2>(h);                 // node 2 seen from node 0 (read before the update)
+        const R o1 = old_at<0, 1>(h);                 // node 1 seen from node 0
         if (TOP && edge_live) top_values(h, w1, w3, w1b);
         R prev = h.l1;
         if constexpr (!Mode::kFlux && Nodes<R, K>::kPaired) {
@@ -969,7 +980,7 @@ struct Slice {
                 const float2 d = (q == H - 1) ? d_last : __ffma2_rn(r.v[q], m1, r.v[q + 1]);
                 const float2 nd = (q == 0) ? make_float2(cd0, c1.pair(H - 1).x) : c1.pair(q - 1);
                 float2 v = __ffma2_rn(nd, dp, __ffma2_rn(c0.pair(q), d, r.v[q]));
-                if (edge_live && q == 0) v.x = fma(j0, o2 - r.v[0].x, v.x);
+                if (edge_live && q == 0) v.x = fma(j0, o2 - o1, v.x);  // up two: r2 - r1 (r1 - r0 in up)
                 r.v[q] = __ffma2_rn(c2.pair(q), __fadd2_rn(v, b2), v);
                 dp = d;
             }
@@ -984,7 +995,7 @@ struct Slice {
                 const R d = nxt - cur;
                 const R ndown = (s == 0) ? cd0 : c1[s - 1];  // -down of this node
                 R v = fma(ndown, dprev, fma(c0[s], d, cur));
-                if (s == 0) v = fma(j0, o2 - cur, v);
+                if (s == 0) v = fma(j0, o2 - o1, v);  // up two: r2 - r1 (r1 - r0 in up)
                 r[s] = fma(c2[s], v + base, v);
                 dprev = d;
             }
