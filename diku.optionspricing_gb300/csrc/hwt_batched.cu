@@ -858,6 +858,9 @@ struct Slice {
         const R jin = (edge_live && n2) ? jlo : (R)0;
         const R src2 = old_at<S2, -2>(h);  // node 0 seen from node 2 (read before the update)
         const R jl1 = n1 ? jlo : (R)0;
+        // K <= 2: link 1 also starts a thread (the one whose first node is node 2), which
+        // computes its flux from the left halo and adds the same term (node 0 = l2)
+        const R jl2 = (K <= 2 && n2 && !n1) ? jlo : (R)0;
         if (TOP && edge_live) top_values(h, w1, w3, w1b);
         if constexpr (!Mode::kFlux && Nodes<R, K>::kPaired) {
             // double-float rows on pairs (node q, node q+H): the compensated products
@@ -902,7 +905,8 @@ struct Slice {
             const float2 e_last = __ffma2_rn(c0.pair(H - 1), r.v[H - 1],
                                              (edge_live && Q1 == H - 1) ? __ffma2_rn(c1.pair(H - 1), nl, jadd)
                                                                         : __fmul2_rn(c1.pair(H - 1), nl));
-            float2 ep = make_float2(fma(cl, h.l1, cd0 * r[0]), e_last.x);  // links k0-1 and k0+H-1
+            const float lk = (K <= 2 && edge_live) ? fma(cd0, r[0], jl2 * h.l2) : cd0 * r[0];
+            float2 ep = make_float2(fma(cl, h.l1, lk), e_last.x);  // links k0-1 and k0+H-1
 #pragma unroll
             for (int q = 0; q < H; ++q) {
                 const float2 e =
@@ -919,7 +923,7 @@ struct Slice {
             // once and used by both ends (the row's sum is kept exactly)
             constexpr int S1 = 1 % K;  // node 1's slot
             const R jq = edge_live ? jl1 * old_at<S1, -1>(h) : (R)0;  // node 0's jump, on link 1
-            R eprev = fma(cl, h.l1, cd0 * r[0]);
+            R eprev = fma(cl, h.l1, (K <= 2 && edge_live) ? fma(cd0, r[0], jl2 * h.l2) : cd0 * r[0]);
 #pragma unroll
             for (int s = 0; s < K; ++s) {
                 const R cur = r[s];
