@@ -27,6 +27,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libhwtree.so")
+ABI_VERSION = 2  # include/hwtree.h HWT_ABI_VERSION
 
 # Status codes (hwtree.h)
 HWT_OK, HWT_EINVAL, HWT_ECUDA, HWT_ENOMEM, HWT_EUNSUPPORTED, HWT_ENODEV, HWT_ETIMEOUT = 0, -1, -2, -3, -4, -5, -6
@@ -105,6 +106,7 @@ _lib = None
 # Every function the header declares, with its ctypes signature.
 _SIGNATURES = {
     "hwt_abi_version": (ctypes.c_int, []),
+    "hwt_struct_size": (ctypes.c_size_t, [ctypes.c_char_p]),
     "hwt_create": (ctypes.c_void_p, [ctypes.c_int, ctypes.c_char_p]),
     "hwt_create_status": (ctypes.c_int, []),
     "hwt_destroy": (None, [ctypes.c_void_p]),
@@ -147,6 +149,13 @@ def lib() -> ctypes.CDLL:
             fn = getattr(handle, name)
             fn.restype = res
             fn.argtypes = args
+        if handle.hwt_abi_version() != ABI_VERSION:
+            raise ImportError(f"{LIB_PATH} has ABI version {handle.hwt_abi_version()}, this binding {ABI_VERSION}: "
+                              "rebuild the native library")
+        for cname, cls in _RECORDS.items():
+            if handle.hwt_struct_size(cname.encode()) != ctypes.sizeof(cls):
+                raise ImportError(f"{cname}: {handle.hwt_struct_size(cname.encode())} bytes in {LIB_PATH}, "
+                                  f"{ctypes.sizeof(cls)} in this binding: rebuild the native library")
         _lib = handle
     return _lib
 
@@ -559,6 +568,11 @@ class SurrogateStats(ctypes.Structure):
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+# Records whose layout must match the library's (checked when it is loaded).
+_RECORDS = {"hwt_options": _Options, "hwt_yield": _Yield, "hwt_config": Config, "hwt_stats": Stats, "hwt_box": Box,
+            "hwt_train_config": TrainConfig, "hwt_train_stats": TrainStats, "hwt_surrogate_stats": SurrogateStats}
 
 
 _SIGNATURES.update({

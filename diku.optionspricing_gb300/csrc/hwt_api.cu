@@ -443,6 +443,21 @@ extern "C" {
 
 int hwt_abi_version(void) { return HWT_ABI_VERSION; }
 
+size_t hwt_struct_size(const char *name)
+{
+    if (!name) return 0;
+    const struct {
+        const char *name;
+        size_t size;
+    } records[] = {{"hwt_options", sizeof(hwt_options)},         {"hwt_yield", sizeof(hwt_yield)},
+                   {"hwt_config", sizeof(hwt_config)},           {"hwt_stats", sizeof(hwt_stats)},
+                   {"hwt_box", sizeof(hwt_box)},                 {"hwt_train_config", sizeof(hwt_train_config)},
+                   {"hwt_train_stats", sizeof(hwt_train_stats)}, {"hwt_surrogate_stats", sizeof(hwt_surrogate_stats)}};
+    for (const auto &r : records)
+        if (strcmp(r.name, name) == 0) return r.size;
+    return 0;
+}
+
 int hwt_create_status(void) { return g_create_status; }
 
 hwt_ctx *hwt_create(int device, const char *tune_cache)

@@ -23,13 +23,16 @@
 #ifndef HWTREE_H
 #define HWTREE_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
 extern "C" {
 #endif
 
-#define HWT_ABI_VERSION 1
+/* 2: hwt_train_config, hwt_train_stats and hwt_surrogate_stats grew (hard-sample
+ * mining, held-out violations, options copy time); hwt_struct_size added. */
+#define HWT_ABI_VERSION 2
 
 /* Status codes. */
 #define HWT_OK 0
@@ -134,6 +137,12 @@ typedef struct hwt_ctx hwt_ctx;
 
 /* Library ABI version (HWT_ABI_VERSION). */
 int hwt_abi_version(void);
+
+/* Size in bytes of the named record as this library was built ("hwt_options",
+ * "hwt_yield", "hwt_config", "hwt_stats", "hwt_box", "hwt_train_config",
+ * "hwt_train_stats", "hwt_surrogate_stats"), 0 for any other name: a binding
+ * checks its own layouts against it before passing a record. */
+size_t hwt_struct_size(const char *name);
 
 /* Creates a context on CUDA device `device`: stream, events, and buffers that
  * grow with the largest batch seen.  tune_cache: path of the autotuner's cache

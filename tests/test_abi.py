@@ -30,7 +30,17 @@ def test_python_binding_covers_header(pkg):
 
 
 def test_abi_version(pkg):
-    assert pkg.lib().hwt_abi_version() == 1
+    assert pkg.lib().hwt_abi_version() == 2
+
+
+def test_record_layouts_match_the_library(pkg):
+    """Every record the binding passes has the size the library was built with
+    (hwt_struct_size); an unknown name answers 0."""
+    import ctypes
+    lib = pkg.lib()
+    for cname, cls in pkg._RECORDS.items():
+        assert lib.hwt_struct_size(cname.encode()) == ctypes.sizeof(cls), cname
+    assert lib.hwt_struct_size(b"hwt_nothing") == 0 and lib.hwt_struct_size(None) == 0
 
 
 def test_active_nodes_formula(pkg):
