@@ -548,7 +548,7 @@ class TrainStats(ctypes.Structure):
                 ("holdout_answered", ctypes.c_double), ("holdout_max_abs", ctypes.c_double),
                 ("holdout_p99_abs", ctypes.c_double), ("holdout_all_max_abs", ctypes.c_double),
                 ("holdout", ctypes.c_int64), ("n_kinks", ctypes.c_int64), ("kink_delta", ctypes.c_double),
-                ("ladder_tolerance", ctypes.c_double * 7), ("ladder_answered", ctypes.c_double * 7),
+                ("ladder_tolerance", ctypes.c_double * 12), ("ladder_answered", ctypes.c_double * 12),
                 ("holdout_over", ctypes.c_int64), ("hard_minings", ctypes.c_int64),
                 ("hard_threshold_abs", ctypes.c_double)]
 

@@ -43,6 +43,13 @@ const int kFanOut[kLayers] = {kHidden, kHidden, kHidden, kHidden, kOut};
 constexpr float kErrEps = 1e-3f;  // floor of the error head's target log(|r| + eps), standardised units
 constexpr int kMaxCurve = 4096;
 
+// Tolerances the routing is calibrated at (kCalTol, after the training loop); a call
+// with a judge tolerance routes with the largest of them not above kJudgeMargin times
+// it, so that answers just under the judge's tolerance on the held-out samples go to
+// the tree too and the judge's sample rarely meets one above it.
+constexpr int kCalTols = 12;
+constexpr double kJudgeMargin = 0.9;
+
 struct FeatureNorm {
     double mean[kIn], inv_std[kIn];
 };
@@ -561,10 +568,9 @@ struct hwt_surrogate {
     // within this distance of it go to the tree (< 0: none); kink_delta is the largest
     std::vector<double> route_delta;
     double kink_delta = -1.0;     // < 0: no kink routing
-    // The same routing calibrated at a ladder of tolerances (kCalTol): a call with a
-    // judge tolerance routes with the largest of them not above that tolerance
-    double cal_tau[7], cal_delta[7], cal_answered[7];
-    std::vector<double> cal_deltas[7];
+    // The same routing calibrated at a ladder of tolerances (kCalTol)
+    double cal_tau[kCalTols], cal_delta[kCalTols], cal_answered[kCalTols];
+    std::vector<double> cal_deltas[kCalTols];
     int cal_valid = 0;
     Buf<double> dkinks;
     int trained = 0;
@@ -1161,8 +1167,7 @@ double calibrate_tau(const std::vector<double> &pred, const std::vector<double> 
 
 constexpr int kMaxKinks = 256;
 constexpr double kKinkBand = 0.005;  // moneyness: ~0.44 strike units around a kink of the book's tree
-constexpr int kCalTols = 7;
-const double kCalTol[kCalTols] = {2.5e-5, 5e-5, 1e-4, 2e-4, 5e-4, 1e-3, 2e-3};
+const double kCalTol[kCalTols] = {2.5e-5, 5e-5, 9e-5, 1e-4, 1.8e-4, 2e-4, 4.5e-4, 5e-4, 9e-4, 1e-3, 1.8e-3, 2e-3};
 
 // A box that pins every tree parameter (maturities, a, sigma, steps): all its
 // options share one tree, and only strike and type vary.
@@ -1589,13 +1594,13 @@ int hwt_surrogate_price(hwt_surrogate *s, const hwt_options *o, const hwt_yield 
     const double jf = std::min(std::max(judge_fraction, 0.0), 1.0);
     const unsigned long long thresh = jf >= 1.0 ? ~0ull : (unsigned long long)(jf * 18446744073709551616.0);
     // routing: the training tolerance's calibration, or, with a judge tolerance, the
-    // ladder's largest tolerance not above it (the strictest if none is)
+    // ladder's largest tolerance not above kJudgeMargin times it (the strictest if none is)
     double tau = s->route_tau, route_tol = NAN;
     const std::vector<double> *delta = &s->route_delta;
     if (judge_tolerance > 0 && s->cal_valid) {
         int k = 0;
         for (int q = 0; q < kCalTols; ++q)
-            if (kCalTol[q] <= judge_tolerance * (1.0 + 1e-12)) k = q;
+            if (kCalTol[q] <= kJudgeMargin * judge_tolerance * (1.0 + 1e-12)) k = q;
         tau = s->cal_tau[k];
         delta = &s->cal_deltas[k];
         route_tol = kCalTol[k];
@@ -1725,7 +1730,7 @@ int hwt_surrogate_save(const hwt_surrogate *s, const char *path)
         return HWT_ECUDA;
     FILE *f = fopen(path, "wb");
     if (!f) return HWT_EINVAL;
-    const uint32_t magic = 0x48575453u, version = 5;
+    const uint32_t magic = 0x48575453u, version = 6;
     const uint64_t np = s->n_params, nk = s->kinks.size();
     const int64_t t = s->adam_t;
     // per-point routing distances: the training tolerance's, then the ladder's
@@ -1760,7 +1765,7 @@ int hwt_surrogate_load(hwt_surrogate *s, const char *path)
     std::vector<double> kinks;
     int cal_valid = 0;
     double cal_tau[kCalTols], cal_delta[kCalTols], cal_answered[kCalTols];
-    bool ok = fread(&magic, 4, 1, f) == 1 && fread(&version, 4, 1, f) == 1 && magic == 0x48575453u && version == 5 &&
+    bool ok = fread(&magic, 4, 1, f) == 1 && fread(&version, 4, 1, f) == 1 && magic == 0x48575453u && version == 6 &&
               fread(&box, sizeof(hwt_box), 1, f) == 1 && fread(&ym, 8, 1, f) == 1 && fread(&ysd, 8, 1, f) == 1 &&
               fread(&tau, 8, 1, f) == 1 && fread(&kd, 8, 1, f) == 1 && fread(&nk, 8, 1, f) == 1 && nk <= (uint64_t)kMaxKinks;
     if (ok && nk) {

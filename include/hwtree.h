@@ -295,8 +295,8 @@ typedef struct hwt_train_stats {
     double kink_delta;               /* the largest routing distance (moneyness) around a kink or box
                                         edge; options within a point's own distance go to the tree
                                         (< 0: no kink routing) */
-    double ladder_tolerance[7];      /* the routing also calibrated at these tolerances ... */
-    double ladder_answered[7];       /* ... answering these fractions of the held-out samples */
+    double ladder_tolerance[12];     /* the routing also calibrated at these tolerances ... */
+    double ladder_answered[12];      /* ... answering these fractions of the held-out samples */
     int64_t holdout_over;            /* held-out samples the network answers above route_tolerance
                                         (0 by construction) */
     int64_t hard_minings;            /* hard-sample minings run */
@@ -329,7 +329,9 @@ const char *hwt_surrogate_last_error(const hwt_surrogate *s);
 int hwt_surrogate_train(hwt_surrogate *s, const hwt_options *samples, const hwt_yield *yield,
                         const hwt_train_config *cfg, hwt_train_stats *stats);
 /* Routing tolerance: with judge_tolerance > 0 the call routes with the calibration
- * (of the training ladder) for the largest tolerance not above judge_tolerance;
+ * (of the training ladder: 2.5e-5, 5e-5, 9e-5, 1e-4, 1.8e-4, 2e-4, 4.5e-4, 5e-4,
+ * 9e-4, 1e-3, 1.8e-3, 2e-3) for the largest tolerance not above 0.9 judge_tolerance,
+ * a margin that sends the answers just under the judge's tolerance to the tree;
  * otherwise with the training's route_tolerance.
  * Prices host options: network inside the box unless the option is flagged - by
  * the error head, or, on a single-tree box (every tree parameter pinned, so the
