@@ -603,10 +603,11 @@ struct Slice {
         }
     }
     R cl, cd0;              // flux: up of node k0-1, -down of node k0
-    // Edge jumps (+-jmax branch two nodes away).  Nodes 0 and 2 sit at compile-time
-    // slots (0 and 2 % K) and their terms are part of the step loop; node W-1 sits
-    // at slot ts = (W-1) % K, known only at run time, so the top-edge terms are
-    // applied after the in-place step from old values saved before it, through a
+    // Edge jumps (+-jmax branch two nodes away).  Nodes 0, 1 and 2 sit at compile-time
+    // slots (0, 1 % K, 2 % K) and their terms are part of the step loop (flux rows: the
+    // bottom jump rides on links 0 and 1, node 0's up coefficient holding pu_b); node
+    // W-1 sits at slot ts = (W-1) % K, known only at run time, so the top-edge terms
+    // are applied after the in-place step from old values saved before it, through a
     // switch on ts.  Warp tasks group trees by ts (it is part of the warp class),
     // which keeps the switch uniform across the warp.
     R jlo, jhi;             // FP64: jump coefficient times the receiving node's G; flux: pu_b, pd_c (1 + g_{W-1})
