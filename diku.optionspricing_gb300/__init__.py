@@ -594,6 +594,11 @@ _SIGNATURES.update({
     "hwt_surrogate_forward_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
                                                     ctypes.POINTER(ctypes.c_double)]),
     "hwt_surrogate_inject_stall": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "hwt_find_kinks": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+                                      ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32)]),
+    "hwt_route_distances": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
+                                           ctypes.c_int64, ctypes.c_double, ctypes.c_void_p,
+                                           ctypes.POINTER(ctypes.c_double)]),
     "hwt_surrogate_loss_grads": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                                                 ctypes.c_double, ctypes.POINTER(ctypes.c_double), ctypes.c_void_p]),
 })
@@ -719,3 +724,33 @@ class Surrogate:
 
 
 from . import workloads  # noqa: E402  (seeded synthetic batches)
+
+
+def find_kinks(x, price, type_, cap: int = 256) -> np.ndarray:
+    """Payoff kinks (moneyness, ascending) of one tree from labelled samples
+    (hwt_find_kinks; host only, the surrogate training's own code)."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    price = np.ascontiguousarray(price, dtype=np.float64)
+    t = np.ascontiguousarray(type_, dtype=np.int8)
+    out = np.empty(cap, dtype=np.float64)
+    count = ctypes.c_int32(0)
+    rc = lib().hwt_find_kinks(x.ctypes.data, price.ctypes.data, t.ctypes.data, len(x), out.ctypes.data, cap,
+                              ctypes.byref(count))
+    if rc != 0:
+        raise ValueError(f"hwt_find_kinks: {count.value} kinks (cap {cap}), status {rc}")
+    return out[:count.value].copy()
+
+
+def route_distances(points, x, err, tol: float) -> tuple[np.ndarray, float]:
+    """Routing distance per point and the answered fraction (hwt_route_distances;
+    host only, the surrogate training's calibration)."""
+    p = np.ascontiguousarray(points, dtype=np.float64)
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    e = np.ascontiguousarray(err, dtype=np.float64)
+    d = np.empty(len(p), dtype=np.float64)
+    ans = ctypes.c_double(0.0)
+    rc = lib().hwt_route_distances(p.ctypes.data, len(p), x.ctypes.data, e.ctypes.data, len(x), tol, d.ctypes.data,
+                                   ctypes.byref(ans))
+    if rc != 0:
+        raise ValueError(f"hwt_route_distances: status {rc}")
+    return d, ans.value

@@ -1239,6 +1239,34 @@ bool routed_near(const std::vector<double> &pts, const std::vector<double> &delt
     return false;
 }
 
+// Distances per routing point: each sample above tol widens the distance of the
+// point nearest to it until it is reached (-1: no such sample).
+void route_distances(const std::vector<double> &pts, const double *x, const double *err, int64_t n, double tol,
+                     std::vector<double> &delta)
+{
+    delta.assign(pts.size(), -1.0);
+    if (pts.empty()) return;
+    for (int64_t j = 0; j < n; ++j)
+        if (!(err[j] <= tol)) {
+            const int k = nearest_point(pts, x[j]);
+            delta[k] = std::max(delta[k], fabs(x[j] - pts[k]));
+        }
+}
+
+// Kinks of one tree from (moneyness, price, type) samples: detect_kinks per type,
+// then merge_kinks.
+std::vector<double> find_kinks(const double *x, const double *price, const int8_t *type, int64_t n)
+{
+    std::vector<double> k;
+    for (int t = 0; t <= 1; ++t) {
+        std::vector<std::pair<double, double>> pts;
+        for (int64_t i = 0; i < n; ++i)
+            if (type[i] == t) pts.emplace_back(x[i], price[i]);
+        detect_kinks(pts, 1e-3, k);
+    }
+    return merge_kinks(k);
+}
+
 double max_of(const std::vector<double> &v)
 {
     double m = -1.0;
@@ -1318,16 +1346,15 @@ int hwt_surrogate_train(hwt_surrogate *s, const hwt_options *samples, const hwt_
     s->route_delta.clear();
     for (auto &v : s->cal_deltas) v.clear();
     if (single_tree_box(s->box)) {
-        std::vector<double> k;
-        for (int type = 0; type <= 1; ++type) {
-            std::vector<std::pair<double, double>> pts;
-            for (int64_t j = 0; j < ntrain; ++j) {
-                const int i = idx[j];
-                if (samples->type[i] == type) pts.emplace_back(samples->strike[i] / Fh[i], price[i]);
-            }
-            detect_kinks(pts, 1e-3, k);
+        std::vector<double> kx(ntrain), kp(ntrain);
+        std::vector<int8_t> kt(ntrain);
+        for (int64_t j = 0; j < ntrain; ++j) {
+            const int i = idx[j];
+            kx[j] = samples->strike[i] / Fh[i];
+            kp[j] = price[i];
+            kt[j] = samples->type[i];
         }
-        s->kinks = merge_kinks(k);
+        s->kinks = find_kinks(kx.data(), kp.data(), kt.data(), ntrain);
         if (s->kinks.size() > (size_t)kMaxKinks) s->kinks.clear();  // not one tree after all
     }
     if (ntrain < batch) return sfail(s, HWT_EINVAL, "fewer in-box training samples than one batch");
@@ -1510,12 +1537,7 @@ int hwt_surrogate_train(hwt_surrogate *s, const hwt_options *samples, const hwt_
             }
             std::vector<double> e;
             if (!xm.empty()) {
-                delta->assign(rp.size(), -1.0);
-                for (int64_t j = 0; j < nhold; ++j)
-                    if (!(err[j] <= tol)) {
-                        const int k = nearest_point(rp, xm[j]);
-                        (*delta)[k] = std::max((*delta)[k], fabs(xm[j] - rp[k]));
-                    }
+                route_distances(rp, xm.data(), err.data(), nhold, tol, *delta);
                 for (int64_t j = 0; j < nhold; ++j)
                     if (!routed_near(rp, *delta, xm[j])) e.push_back(err[j]);
             } else {
@@ -1809,6 +1831,33 @@ int hwt_surrogate_load(hwt_surrogate *s, const char *path)
     if (r) return r;
     SCUDA(s, cudaStreamSynchronize(s->stream), "load");
     s->trained = 1;
+    return HWT_OK;
+}
+
+int hwt_find_kinks(const double *x, const double *price, const int8_t *type, int64_t n, double *kinks, int32_t cap,
+                   int32_t *count)
+{
+    if (n < 0 || cap < 0 || !count || (n > 0 && (!x || !price || !type)) || (cap > 0 && !kinks)) return HWT_EINVAL;
+    const std::vector<double> k = find_kinks(x, price, type, n);
+    *count = (int32_t)std::min<size_t>(k.size(), (size_t)INT32_MAX);
+    if (k.size() > (size_t)cap) return HWT_EINVAL;
+    for (size_t j = 0; j < k.size(); ++j) kinks[j] = k[j];
+    return HWT_OK;
+}
+
+int hwt_route_distances(const double *points, int32_t n_points, const double *x, const double *err, int64_t n,
+                        double tol, double *delta, double *answered)
+{
+    if (n_points < 0 || n < 0 || (n_points > 0 && (!points || !delta)) || (n > 0 && (!x || !err))) return HWT_EINVAL;
+    const std::vector<double> pts(points, points + n_points);
+    std::vector<double> d;
+    route_distances(pts, x, err, n, tol, d);
+    for (int32_t k = 0; k < n_points; ++k) delta[k] = d[k];
+    if (answered) {
+        int64_t kept = 0;
+        for (int64_t j = 0; j < n; ++j) kept += routed_near(pts, d, x[j]) ? 0 : 1;
+        *answered = n > 0 ? (double)kept / (double)n : 1.0;
+    }
     return HWT_OK;
 }
 

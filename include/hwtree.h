@@ -378,6 +378,26 @@ int hwt_surrogate_loss_grads(hwt_surrogate *s, const float *x, const float *y, i
  * call returns HWT_ETIMEOUT with the context still usable. */
 int hwt_surrogate_inject_stall(hwt_surrogate *s, int mode);
 
+/* Host helpers of the single-tree routing (no GPU), the same code the training runs.
+ *
+ * hwt_find_kinks: payoff kinks of one tree from labelled samples of options that
+ * share it - x[i] the moneyness (strike / forward bond price), price[i] the tree's
+ * price, type[i] 0 (call) or 1 (put).  The price is piecewise linear in the strike;
+ * a slope change above 1e-3 (price per unit of moneyness) between neighbouring
+ * samples of one type marks a kink, and detections closer than 1e-4 are merged to
+ * their midpoint.  Writes the kinks, ascending, to kinks[cap] and their number to
+ * *count; HWT_EINVAL if more than cap were found (the samples are not one tree).
+ *
+ * hwt_route_distances: the routing calibration - for each of the n_points routing
+ * points (moneyness), the distance that reaches every sample (moneyness x[i],
+ * absolute price error err[i]) above tol whose nearest point it is, -1 where there
+ * is none; *answered = the fraction of the samples outside every point's distance
+ * (those the network keeps, all within tol; 1 for n = 0). */
+int hwt_find_kinks(const double *x, const double *price, const int8_t *type, int64_t n, double *kinks, int32_t cap,
+                   int32_t *count);
+int hwt_route_distances(const double *points, int32_t n_points, const double *x, const double *err, int64_t n,
+                        double tol, double *delta, double *answered);
+
 /* ---- Input files ------------------------------------------------------------
  * Replace trinom::Options(const std::string&) and trinom::Yield(const
  * std::string&) (common/Options.hpp:73-98, common/Yield.hpp:20-38), which read
