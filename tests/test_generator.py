@@ -76,3 +76,28 @@ def test_generated_set_priced_by_oracle_like_reference_file(pkg, orc):
         gold = np.array(pkg.read_arrays(f.read())[0], dtype=np.float64)
     assert np.all(np.isfinite(p))
     assert gold.min() - 0.5 <= np.median(p) <= gold.max() + 0.5
+
+
+def test_single_tree_workloads(pkg):
+    """The surrogate's single-tree box and batches (configs[4] as written): training
+    samples drawn as the 1,000-option book (only strike and type vary), queries with
+    exactly 10% outside the box, each flagged one outside it in one parameter."""
+    import numpy as np
+    wl = pkg.workloads
+    box = wl.single_tree_box()
+    tr = wl.single_tree_training_batch(50_000, seed=3)
+    for k in ("bond_maturity", "option_maturity", "a", "sigma", "term_steps"):
+        assert np.unique(tr[k]).size == 1, k
+    assert set(np.unique(tr["type"])) == {0, 1}
+    q = wl.single_tree_query_batch(100_000, seed=4)
+    assert q["outside"].sum() == 10_000
+    fwd = wl.forward_bond_price(q["option_maturity"], q["bond_maturity"])
+    mny = q["strike"] / fwd
+    span = q["bond_maturity"] - q["option_maturity"]
+    inside = ((q["option_maturity"] >= box["t_min"]) & (q["option_maturity"] <= box["t_max"])
+              & (span >= box["span_min"]) & (span <= box["span_max"])
+              & (mny >= box["moneyness_min"]) & (mny <= box["moneyness_max"])
+              & (q["a"] >= box["a_min"]) & (q["a"] <= box["a_max"])
+              & (q["sigma"] >= box["sigma_min"]) & (q["sigma"] <= box["sigma_max"])
+              & (q["term_steps"] >= box["steps_min"]) & (q["term_steps"] <= box["steps_max"]))
+    assert np.array_equal(inside, ~q["outside"])
