@@ -138,8 +138,9 @@ __global__ void layer0_kernel(const float *X, const float *W0, const float *b0, 
     }
 }
 
-// dW0[k][c] += sum over rows of X[r][k] dZ0[r][c] (fp32), a slice of rows per block.
-__global__ void dw0_kernel(const float *X, const float *dZ, int n, float *dW0)
+// Partial dW0[k][c] = sum over a slice of rows of X[r][k] dZ0[r][c] (fp32), one
+// slice of rows per block, into part[block][k][c] (summed in block order afterwards).
+__global__ void dw0_kernel(const float *X, const float *dZ, int n, float *part)
 {
     const int c = threadIdx.x;  // kHidden threads
     const int per = (n + gridDim.x - 1) / gridDim.x;
@@ -154,8 +155,7 @@ __global__ void dw0_kernel(const float *X, const float *dZ, int n, float *dW0)
         acc[4] = fmaf(xb.x, d, acc[4]); acc[5] = fmaf(xb.y, d, acc[5]);
         acc[6] = fmaf(xb.z, d, acc[6]); acc[7] = fmaf(xb.w, d, acc[7]);
     }
-    if (r1 > r0)
-        for (int k = 0; k < kInPad; ++k) atomicAdd(dW0 + k * kHidden + c, acc[k]);
+    for (int k = 0; k < kInPad; ++k) part[((size_t)blockIdx.x * kInPad + k) * kHidden + c] = acc[k];
 }
 
 // Layer 4 of the training path in fp32: out[r][c] = b4[c] + sum_k silu(Z3[r][k]) W4[k][c],
@@ -193,8 +193,9 @@ __global__ void layer4_back_kernel(const float *Z3, const float *dZ4, const floa
     }
 }
 
-// dW4[k][c] += sum over rows of silu(Z3[r][k]) dZ4[r][c] (fp32), a slice of rows per block.
-__global__ void dw4_kernel(const float *Z3, const float *dZ4, int n, float *dW4)
+// Partial dW4[k][c] = sum over a slice of rows of silu(Z3[r][k]) dZ4[r][c] (fp32), one
+// slice of rows per block, into part[block][k][c].
+__global__ void dw4_kernel(const float *Z3, const float *dZ4, int n, float *part)
 {
     const int k = threadIdx.x;  // kHidden threads
     const int per = (n + gridDim.x - 1) / gridDim.x;
@@ -205,10 +206,8 @@ __global__ void dw4_kernel(const float *Z3, const float *dZ4, int n, float *dW4)
         a0 = fmaf(h, __ldg(dZ4 + 2 * r), a0);
         a1 = fmaf(h, __ldg(dZ4 + 2 * r + 1), a1);
     }
-    if (r1 > r0) {
-        atomicAdd(dW4 + 2 * k, a0);
-        atomicAdd(dW4 + 2 * k + 1, a1);
-    }
+    part[(size_t)blockIdx.x * kHidden * 2 + 2 * k] = a0;
+    part[(size_t)blockIdx.x * kHidden * 2 + 2 * k + 1] = a1;
 }
 
 // Outputs [n][2] against targets y: r = o0 - y; error-head target g = log(|r| + eps)
@@ -233,8 +232,9 @@ __global__ void loss_kernel(const float *out, const float *y, int n, float lam, 
     if ((threadIdx.x & 31) == 0 && l != 0.0) atomicAdd(loss, l);
 }
 
-// db[c] += sum over rows of d[r][c]  (d fp32 [n][ld])
-__global__ void colsum_kernel(const float *d, int n, int cols, int ld, float *db)
+// Partial column sums of d (fp32 [n][ld]) over a slice of rows per block row:
+// part[blockIdx.y][c].
+__global__ void colsum_kernel(const float *d, int n, int cols, int ld, float *part)
 {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= cols) return;
@@ -249,7 +249,19 @@ __global__ void colsum_kernel(const float *d, int n, int cols, int ld, float *db
         s3 += d[(size_t)(r + 3) * ld + c];
     }
     for (; r < r1; ++r) s0 += d[(size_t)r * ld + c];
-    atomicAdd(db + c, (s0 + s1) + (s2 + s3));
+    part[(size_t)blockIdx.y * cols + c] = (s0 + s1) + (s2 + s3);
+}
+
+// out[e] = sum over slices s of part[s][e], in slice order: the partial sums of the
+// gradient kernels above and of the split-K GEMM, added the same way every step
+// (the training is reproducible bit for bit).
+__global__ void reduce_slices_kernel(const float *part, int slices, int len, float *out)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= len) return;
+    float acc = 0.f;
+    for (int z = 0; z < slices; ++z) acc += part[(size_t)z * len + e];
+    out[e] = acc;
 }
 
 struct AdamArgs {
@@ -589,6 +601,7 @@ struct hwt_surrogate {
     float *d_z[kLayers] = {};              // pre-activations (z[4] = outputs [rows][2])
     __nv_bfloat16 *d_dz = nullptr, *d_dz2 = nullptr;
     float *d_dzf = nullptr;
+    float *d_part = nullptr;               // per-slice partial gradients, summed in order
     float *d_dz4 = nullptr;                // [rows][2] fp32 output gradients
     double *d_loss = nullptr;
     float *d_y = nullptr;
@@ -625,6 +638,9 @@ int sfail(hwt_surrogate *s, int code, const std::string &m)
         }                                                                                         \
     } while (0)
 
+// Split-K slices of the weight-gradient GEMMs for a batch of `rows` samples.
+int grad_splits(int rows) { return std::max(1, std::min(64, rows / 512)); }
+
 int ensure_act(hwt_surrogate *s, int rows)
 {
     if (rows <= s->act_cap) return HWT_OK;
@@ -634,7 +650,8 @@ int ensure_act(hwt_surrogate *s, int rows)
         cudaFree(s->d_z[l]); s->d_z[l] = nullptr;
     }
     cudaFree(s->d_dz); cudaFree(s->d_dz2); cudaFree(s->d_dzf); cudaFree(s->d_y); cudaFree(s->d_dz4);
-    s->d_dz = s->d_dz2 = nullptr; s->d_dzf = nullptr; s->d_y = nullptr; s->d_dz4 = nullptr;
+    cudaFree(s->d_part);
+    s->d_dz = s->d_dz2 = nullptr; s->d_dzf = nullptr; s->d_y = nullptr; s->d_dz4 = nullptr; s->d_part = nullptr;
     s->act_cap = 0;
     SCUDA(s, cudaMalloc(&s->d_x, sizeof(float) * (size_t)rows * kInPad), "alloc X");
     for (int l = 1; l < kLayers; ++l)  // H1 holds layer 1's hi / lo input pair
@@ -645,6 +662,10 @@ int ensure_act(hwt_surrogate *s, int rows)
     SCUDA(s, cudaMalloc(&s->d_dzf, sizeof(float) * (size_t)rows * kHidden), "alloc dZf");
     SCUDA(s, cudaMalloc(&s->d_y, sizeof(float) * (size_t)rows), "alloc y");
     SCUDA(s, cudaMalloc(&s->d_dz4, sizeof(float) * (size_t)rows * kOut), "alloc dZ4");
+    // partials: the weight-gradient GEMM's split-K slices (at most 64 of [256][256]) or
+    // 256 row slices of the fp32 kernels (at most [8][256] each)
+    const size_t part = std::max((size_t)grad_splits(rows) * kHidden * kHidden, (size_t)256 * kInPad * kHidden);
+    SCUDA(s, cudaMalloc(&s->d_part, sizeof(float) * part), "alloc partials");
     s->act_cap = rows;
     return HWT_OK;
 }
@@ -769,18 +790,24 @@ int backward(hwt_surrogate *s, int rows, float lam, bool zero_loss)
                                                            s->d_loss);
     SCUDA(s, cudaGetLastError(), "loss kernel");
     __nv_bfloat16 *dz = s->d_dz, *dz_next = s->d_dz2;
-    const int splits = std::max(1, std::min(64, rows / 512));
+    const int splits = grad_splits(rows);
     int kc = (rows + splits - 1) / splits;
     kc = (kc + BK - 1) / BK * BK;
+    const int nslice = std::max(1, std::min(256, rows / 32));  // row slices of the fp32 kernels
+    auto reduce = [&](int slices, int len, float *out) {
+        reduce_slices_kernel<<<(len + 255) / 256, 256, 0, s->stream>>>(s->d_part, slices, len, out);
+        return cudaGetLastError();
+    };
     // layer 4 in fp32: dW4 = silu(Z3)^T dZ4, db4 = column sums of dZ4, dZ3 = (dZ4 W4^T) silu'(Z3)
     {
         const float *dz4 = s->d_dz4;
-        dw4_kernel<<<std::max(1, std::min(256, rows / 32)), kHidden, 0, s->stream>>>(s->d_z[kLayers - 2], dz4, rows,
-                                                                                     s->d_g + s->w_off[kLayers - 1]);
+        dw4_kernel<<<nslice, kHidden, 0, s->stream>>>(s->d_z[kLayers - 2], dz4, rows, s->d_part);
         SCUDA(s, cudaGetLastError(), "dW4 kernel");
-        dim3 cg(1, std::max(1, std::min(256, rows / 32)));
-        colsum_kernel<<<cg, 256, 0, s->stream>>>(dz4, rows, kOut, kOut, s->d_g + s->b_off[kLayers - 1]);
+        SCUDA(s, reduce(nslice, kHidden * kOut, s->d_g + s->w_off[kLayers - 1]), "dW4 sum");
+        dim3 cg(1, nslice);
+        colsum_kernel<<<cg, 256, 0, s->stream>>>(dz4, rows, kOut, kOut, s->d_part);
         SCUDA(s, cudaGetLastError(), "db4 kernel");
+        SCUDA(s, reduce(nslice, kOut, s->d_g + s->b_off[kLayers - 1]), "db4 sum");
         layer4_back_kernel<<<(rows * 32 + 255) / 256, 256, 0, s->stream>>>(s->d_z[kLayers - 2], dz4,
                                                                            s->d_w + s->w_off[kLayers - 1], rows, dz,
                                                                            s->d_dzf);
@@ -789,15 +816,18 @@ int backward(hwt_surrogate *s, int rows, float lam, bool zero_loss)
     for (int l = kLayers - 2; l >= 1; --l) {
         const int in = kFanIn[l], out = kFanOut[l];
         // dW_l[in][out] = H_l^T dZ_l   (split-K over the batch; layer 1 from the hi parts)
-        GemmArgs gw = gargs(s, s->d_h[l], dz, in, out, rows, l == 1 ? 2 * in : in, out, EPI_ATOMIC);
-        gw.Cf = s->d_g + s->w_off[l];
+        GemmArgs gw = gargs(s, s->d_h[l], dz, in, out, rows, l == 1 ? 2 * in : in, out, EPI_SLICE);
+        gw.Cf = s->d_part;
         gw.ldc = out;
         gw.k_chunk = kc;
-        SCUDA(s, (gemm<true, true>(gw, (rows + kc - 1) / kc, s->stream)), "dW gemm");
+        const int zs = (rows + kc - 1) / kc;  // every slice holds at least one K block
+        SCUDA(s, (gemm<true, true>(gw, zs, s->stream)), "dW gemm");
+        SCUDA(s, reduce(zs, in * out, s->d_g + s->w_off[l]), "dW sum");
         // db_l = column sums of dZ_l (fp32 copy in d_dzf)
-        dim3 cg((out + 255) / 256, std::max(1, std::min(256, rows / 32)));
-        colsum_kernel<<<cg, 256, 0, s->stream>>>(s->d_dzf, rows, out, out, s->d_g + s->b_off[l]);
+        dim3 cg((out + 255) / 256, nslice);
+        colsum_kernel<<<cg, 256, 0, s->stream>>>(s->d_dzf, rows, out, out, s->d_part);
         SCUDA(s, cudaGetLastError(), "db kernel");
+        SCUDA(s, reduce(nslice, out, s->d_g + s->b_off[l]), "db sum");
         // dZ_{l-1} = (dZ_l W_l^T) * silu'(Z_{l-1})
         GemmArgs gd = gargs(s, dz, s->d_wb[l], rows, in, out, out, out, EPI_DSILU);
         gd.Zin = s->d_z[l - 1];
@@ -809,12 +839,13 @@ int backward(hwt_surrogate *s, int rows, float lam, bool zero_loss)
         std::swap(dz, dz_next);
     }
     // layer 0 in fp32: dW0 = X^T dZ0, db0 = column sums of dZ0
-    dw0_kernel<<<std::max(1, std::min(256, rows / 32)), kHidden, 0, s->stream>>>(s->d_x, s->d_dzf, rows,
-                                                                                 s->d_g + s->w_off[0]);
+    dw0_kernel<<<nslice, kHidden, 0, s->stream>>>(s->d_x, s->d_dzf, rows, s->d_part);
     SCUDA(s, cudaGetLastError(), "dW0 kernel");
-    dim3 cg(1, std::max(1, std::min(256, rows / 32)));
-    colsum_kernel<<<cg, 256, 0, s->stream>>>(s->d_dzf, rows, kHidden, kHidden, s->d_g + s->b_off[0]);
+    SCUDA(s, reduce(nslice, kInPad * kHidden, s->d_g + s->w_off[0]), "dW0 sum");
+    dim3 cg(1, nslice);
+    colsum_kernel<<<cg, 256, 0, s->stream>>>(s->d_dzf, rows, kHidden, kHidden, s->d_part);
     SCUDA(s, cudaGetLastError(), "db0 kernel");
+    SCUDA(s, reduce(nslice, kHidden, s->d_g + s->b_off[0]), "db0 sum");
     return HWT_OK;
 }
 
@@ -973,6 +1004,7 @@ void hwt_surrogate_destroy(hwt_surrogate *s)
     cudaFree(s->d_w); cudaFree(s->d_m); cudaFree(s->d_v); cudaFree(s->d_g); cudaFree(s->d_loss); cudaFree(s->d_gemm_err);
     cudaFree(s->d_wp); cudaFree(s->d_x);
     for (int l = 0; l < kLayers; ++l) { cudaFree(s->d_wt[l]); cudaFree(s->d_wb[l]); cudaFree(s->d_z[l]); cudaFree(s->d_h[l]); }
+    cudaFree(s->d_part);
     cudaFree(s->d_dz); cudaFree(s->d_dz2); cudaFree(s->d_dzf); cudaFree(s->d_y); cudaFree(s->d_dz4);
     free_batch(s->opts);
     free_batch(s->sub);

@@ -21,7 +21,7 @@
 // MN-direction one (each reading checked on GB300 against the swapped one).  The epilogue reads the accumulator
 // with tcgen05.ld (warp w owns TMEM lanes 32w..32w+31 = tile rows), 16 columns at
 // a time, and applies the surrogate's fused operations (bias + SiLU, bias,
-// dY * SiLU'(Z), split-K atomics) with 16-byte loads and stores.
+// dY * SiLU'(Z), split-K partials per slice or atomics) with 16-byte loads and stores.
 //
 // Every wait on an mbarrier is bounded: past the limit the CTA raises *err, stops
 // issuing work, waits (bounded) for the MMAs it already committed, frees its TMEM
@@ -46,6 +46,7 @@ enum Epilogue : int {
     EPI_BIAS = 1,        // Y = acc + bias -> store fp32 (and bf16 if given)
     EPI_DSILU = 2,       // dZ = acc * silu'(Z) -> store bf16 (and fp32 if given)
     EPI_ATOMIC = 3,      // C += acc (fp32 atomics, split-K)
+    EPI_SLICE = 4,       // C[z] = acc: split-K slice z's partial (fp32), summed in order afterwards
 };
 
 struct GemmArgs {
@@ -413,8 +414,14 @@ __global__ void __launch_bounds__(THREADS) umma_gemm_kernel(GemmArgs p)
             const int n = n0 + c;
             if (m >= p.M || n >= p.N) continue;
             const bool full = n + 16 <= p.N;
-            if (full && vf && (p.epi == EPI_ATOMIC || vb || !p.Cb)) {
+            if (full && vf && (p.epi == EPI_ATOMIC || p.epi == EPI_SLICE || vb || !p.Cb)) {
                 float4 *cf = p.Cf ? reinterpret_cast<float4 *>(p.Cf + (size_t)m * p.ldc + n) : nullptr;
+                if (p.epi == EPI_SLICE) {
+                    float4 *cz = reinterpret_cast<float4 *>(p.Cf + ((size_t)blockIdx.z * p.M + m) * p.ldc + n);
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) cz[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+                    continue;
+                }
                 if (p.epi == EPI_ATOMIC) {
 #pragma unroll
                     for (int q = 0; q < 4; ++q) atomicAdd(cf + q, make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]));
@@ -474,6 +481,9 @@ __global__ void __launch_bounds__(THREADS) umma_gemm_kernel(GemmArgs p)
                         p.Cb[(size_t)m * p.ldcb + nn] = __float2bfloat16(d);
                         break;
                     }
+                    case EPI_SLICE:
+                        p.Cf[((size_t)blockIdx.z * p.M + m) * p.ldc + nn] = a;
+                        break;
                     default:
                         if (a != 0.f) atomicAdd(p.Cf + (size_t)m * p.ldc + nn, a);
                         break;

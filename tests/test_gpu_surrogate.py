@@ -266,3 +266,20 @@ def test_single_tree_surrogate_prices_faster_than_the_mixed_tree(pkg, pricer):
     s.close()
     assert len(passed) >= 3, len(passed)
     assert max(passed) < t_tree, (passed, t_tree)
+
+
+def test_training_is_reproducible(pkg, pricer):
+    """Every gradient is summed per slice in a fixed order (no atomics): two trainings
+    with one seed give the same weights bit for bit."""
+    wl = pkg.workloads
+    rates, days = wl.yield_curve()
+    y = pkg.Yield(rates, days)
+    train = pkg.Options.from_batch(wl.single_tree_training_batch(100_000, seed=41))
+    outs = []
+    for _ in range(2):
+        s = pkg.Surrogate(pricer, box=wl.single_tree_box(), seed=4)
+        s.train(train, y, epochs=2, batch=8192, lr=1e-3, seed=9)
+        outs.append(s.params())
+        s.close()
+    for (wa, ba), (wb, bb) in zip(*outs):
+        assert np.array_equal(wa, wb) and np.array_equal(ba, bb)
